@@ -1,0 +1,169 @@
+/*
+ * tuna_gpu.h — C ABI of the GB300 k-mer counting library (libtuna_gpu.so).
+ *
+ * Drop-in boundary for tuna's two-phase counting path. The reference runs the
+ * path inside C++ templates; each entry point below replaces one piece of it
+ * (paths relative to the reference project root):
+ *
+ *   tg_ctx_create / tg_ctx_destroy   the worker-thread pools and per-thread
+ *                                    tables of src/count.hpp:720-970 and
+ *                                    src/partition_hash.hpp:259-338
+ *   tg_job_begin                     Config (src/Config.hpp:10-26) + the
+ *                                    partition count of include/tuna/tuna.hpp:116-119
+ *   tg_job_feed_fastx / _file        SeqSource::process (src/seq_source.hpp:190-205)
+ *   tg_job_feed_seq / _seq_device    the ACTG chunks handed to
+ *                                    extract_superkmers_from_actg (src/partition_hash.hpp:48)
+ *   tg_job_run                       run<k,m> / run_callback<k,m> phases 1+2
+ *                                    (src/pipeline.hpp:64-330)
+ *   tg_job_drain                     write_counts / write_counts_kff /
+ *                                    write_counts_callback (src/count.hpp:180-298)
+ *   tg_job_result_copy               count_to_raw (include/tuna/tuna.hpp:181-195)
+ *   tg_job_export_partitions         the hash_<p>.superkmers files of the disk
+ *                                    pipeline (src/superkmer_io.hpp:3-19, -tp -kt)
+ *   tg_job_stats                     the phase1:/phase2:/superkmers:/unique_kmers:
+ *                                    stderr lines (src/pipeline.hpp:174-178)
+ *
+ * Conventions: every function returns a tg_status (0 = ok); no exception
+ * crosses the ABI; tg_last_error() gives the message of the last failure on a
+ * context. A context is owned by one host thread at a time; jobs of one
+ * context run in submission order on its stream.
+ *
+ * Input convention of the *_seq entry points: a byte stream in which every
+ * byte outside [ACGTacgt] separates runs (the ACGT-only chunks of the
+ * reference's parser). Runs never continue across two feed calls.
+ *
+ * Output: canonical k-mers as ceil((k+1)/32) little-endian u64 words with
+ * the layout of tuna::Kmer<k> (word 0 holds the last 32 bases, last base in
+ * the two low bits, kache codes A0 C1 G2 T3), and u32 counts. For k <= 31
+ * that is one word per k-mer, for 32 <= k <= 63 two.
+ */
+#ifndef TUNA_GPU_H
+#define TUNA_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    TG_OK = 0,
+    TG_ERR_ARG = 1,        /* bad parameter (k, m, n, sizes, null pointers) */
+    TG_ERR_CUDA = 2,       /* a CUDA call failed; see tg_last_error */
+    TG_ERR_OOM = 3,        /* device or pinned memory exhausted */
+    TG_ERR_STATE = 4,      /* call out of order (e.g. feed after run) */
+    TG_ERR_IO = 5,         /* file could not be opened / read / written */
+    TG_ERR_PARSE = 6,      /* empty input file ("Empty file") */
+    TG_ERR_TABLE = 7,      /* a counting table could not hold a partition */
+    TG_ERR_DEVICE = 8,     /* a device-side wait gave up (bounded spin) */
+    TG_ERR_UNSUPPORTED = 9 /* parameters valid for tuna but not on this GPU path */
+} tg_status;
+
+typedef struct tg_ctx tg_ctx;
+typedef struct tg_job tg_job;
+
+typedef struct {
+    int device;                 /* CUDA device ordinal */
+    uint64_t hbm_budget_bytes;  /* 0 = free HBM minus a reserve */
+    uint32_t host_threads;      /* host parser / formatter threads; 0 = all cores */
+    uint32_t flags;             /* reserved, 0 */
+} tg_ctx_opts;
+
+typedef struct {
+    uint16_t k;          /* 2..63 on this path */
+    uint16_t m;          /* 1..min(k-1, 32) */
+    uint32_t n_parts;    /* tuna -n: power of two, used for exported partition
+                            files and reported; 0 = 16 */
+    uint64_t ci;         /* keep k-mers with ci <= count <= cx */
+    uint64_t cx;
+    uint32_t gpu_parts;  /* internal bucket count (power of two); 0 = auto */
+    uint32_t flags;      /* reserved, 0 */
+} tg_job_opts;
+
+typedef struct {
+    uint64_t input_bytes;     /* bytes fed (sequence stream bytes) */
+    uint64_t bases;           /* ACGT bases fed */
+    uint64_t runs;            /* ACGT runs of length >= k */
+    uint64_t kmers;           /* k-mer instances */
+    uint64_t superkmers;      /* superkmer records (reference's superkmers:) */
+    uint64_t distinct;        /* distinct canonical k-mers before ci/cx */
+    uint64_t out;             /* k-mers after ci/cx (reference's unique_kmers:) */
+    uint32_t gpu_parts;       /* internal bucket count used */
+    uint32_t fine_groups_max; /* largest fine split of one bucket */
+    uint64_t fallback_groups; /* groups counted in a global-memory table */
+    double h2d_ms;            /* host->device copy time of the input */
+    double pack_ms;           /* device time: 2-bit packing */
+    double phase1_ms;         /* device time: minimizers, superkmers, buckets */
+    double phase2_ms;         /* device time: counting, filter, compaction */
+    double d2h_ms;            /* device->host time of results (copy / drain) */
+    double phase1_cut_ms;     /* part of phase1_ms: the superkmer cut kernel */
+    double phase1_scatter_ms; /* part of phase1_ms: the bucket scatter kernel */
+    uint64_t record_bytes;    /* bytes of bucket records written */
+    uint64_t gpu_launches;    /* kernels launched by the last tg_job_run */
+} tg_stats;
+
+/* Output formats of tg_job_drain. */
+typedef enum {
+    TG_FMT_TSV = 0,   /* "<kmer>\t<count>\n", as write_counts (count.hpp:180-216) */
+    TG_FMT_KFF = 1,   /* KFF raw section body: ceil(k/4) B MSB-first + u32 BE */
+    TG_FMT_RAW = 2    /* words u64 x ceil((k+1)/32) then u32 count, packed */
+} tg_format;
+
+/* Sink of tg_job_drain: called with consecutive output chunks from the
+ * calling thread; return 0 to continue, non-zero to stop with TG_ERR_IO. */
+typedef int (*tg_sink_fn)(const void* data, size_t bytes, uint64_t n_kmers, void* user);
+
+/* ---- context ---------------------------------------------------------- */
+tg_status tg_ctx_create(const tg_ctx_opts* opts, tg_ctx** out);
+tg_status tg_ctx_destroy(tg_ctx* ctx);
+const char* tg_last_error(const tg_ctx* ctx);
+/* Library version string and whether a CUDA device is usable. */
+const char* tg_version(void);
+int tg_device_count(void);
+
+/* ---- jobs ------------------------------------------------------------- */
+tg_status tg_job_begin(tg_ctx* ctx, const tg_job_opts* opts, tg_job** out);
+/* Host bytes of a sequence stream (non-ACGT separates runs). */
+tg_status tg_job_feed_seq(tg_job* job, const uint8_t* seq, size_t len);
+/* Same, already in device memory on the context's device; the buffer must stay
+ * valid and unchanged until tg_job_run returns. No copy is made. */
+tg_status tg_job_feed_seq_device(tg_job* job, const uint8_t* dseq, size_t len);
+/* FASTA/FASTQ bytes (FASTQ iff the first byte is '@'), parsed on the host with
+ * the reference's rules. An empty buffer fails with TG_ERR_PARSE. */
+tg_status tg_job_feed_fastx(tg_job* job, const uint8_t* data, size_t len);
+/* A FASTA/FASTQ file, plain or gzip (by the ".gz" suffix). */
+tg_status tg_job_feed_file(tg_job* job, const char* path);
+/* Phase 1 + Phase 2 on the device. Blocks until the counts are ready. */
+tg_status tg_job_run(tg_job* job);
+tg_status tg_job_stats(const tg_job* job, tg_stats* out);
+/* Number of k-mers after the ci/cx filter. */
+uint64_t tg_job_result_size(const tg_job* job);
+/* Words per k-mer in RAW output (1 for k <= 31, 2 for k <= 63). */
+int tg_job_key_words(const tg_job* job);
+/* Copy results [first, first + n) to host memory (any order of k-mers, the
+ * same order every call). keys: n * key_words u64; counts: n u32. */
+tg_status tg_job_result_copy(tg_job* job, uint64_t* keys, uint32_t* counts,
+                             uint64_t first, uint64_t n);
+/* Format results on the device and hand them to sink in chunks. */
+tg_status tg_job_drain(tg_job* job, tg_format fmt, tg_sink_fn sink, void* user);
+/* Write results to a file: TSV, or a complete KFF file when fmt == TG_FMT_KFF. */
+tg_status tg_job_write(tg_job* job, tg_format fmt, const char* path);
+/* Phase 1 partitions in the reference's superkmer file layout for tuna -n
+ * (job opts n_parts): sink(p, bytes, len) once per partition in order. */
+typedef int (*tg_part_sink_fn)(uint32_t part, const uint8_t* data, size_t len, void* user);
+tg_status tg_job_export_partitions(tg_job* job, tg_part_sink_fn sink, void* user);
+tg_status tg_job_end(tg_job* job);
+
+/* ---- one-call helpers --------------------------------------------------- */
+/* Count a host sequence stream end to end: H2D, both phases, D2H of the
+ * filtered pairs into caller buffers of capacity cap (n_out receives the
+ * number of pairs; TG_ERR_ARG if cap is too small, with n_out set). */
+tg_status tg_count_seq(tg_ctx* ctx, const tg_job_opts* opts, const uint8_t* seq, size_t len,
+                       uint64_t* keys, uint32_t* counts, uint64_t cap, uint64_t* n_out,
+                       tg_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

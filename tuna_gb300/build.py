@@ -98,7 +98,7 @@ def gpu_lib(build_if_missing: bool = True, verbose: bool = False) -> str:
             for o in outs:
                 sys.stdout.write(o)
     if jobs or not os.path.exists(GPU_LIB):
-        _run([nvcc, *ARCH, "-shared", "-o", GPU_LIB + ".tmp", *objs, "-lcudart", "-lpthread"])
+        _run([nvcc, *ARCH, "-shared", "-o", GPU_LIB + ".tmp", *objs, "-lcudart", "-lpthread", "-ldl"])
         os.replace(GPU_LIB + ".tmp", GPU_LIB)
     return GPU_LIB
 

@@ -1,0 +1,770 @@
+// tg_api.cu — the C ABI of libtuna_gpu.so (include/tuna_gpu.h): contexts,
+// jobs, the device pipeline driver and result access.
+//
+// A job runs, on the context's stream:
+//   k_pack      ASCII stream -> 2-bit codes + validity bits
+//   k_cut       minimizers, chain starts, forced splits -> record descriptors
+//               and per (bucket, CTA) histograms
+//   k_scan_*    exclusive scans of the histograms -> bucket offsets
+//   k_sizes     per-bucket record counts (sizing; one host sync here)
+//   k_scatter   descriptors -> bucket records + record index
+//   k_count     per bucket: fine split, shared-memory counting, ci/cx, compaction
+//   k_fb_*      (rare) groups that overflowed shared memory, global tables
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "host/tg_host.h"
+#include "tg_internal.cuh"
+#include "tuna_gpu.h"
+
+namespace tg {
+size_t cut_smem_bytes(int w, uint32_t p1, bool exp);
+cudaError_t launch_pack(const uint8_t* seq, uint64_t n, uint32_t* packed, uint32_t* valid, uint64_t n_words,
+                        unsigned long long* n_bases, cudaStream_t st);
+cudaError_t launch_cut(const CutParams& P, const HashTables* gT, bool exp, cudaStream_t st);
+cudaError_t launch_scan(const uint32_t* in, uint64_t n, unsigned long long* out, unsigned long long* sums,
+                        unsigned long long* total, cudaStream_t st, int* launches);
+cudaError_t launch_scatter(const ScatterParams& P, cudaStream_t st);
+size_t count_smem_bytes(int W, uint32_t slots);
+size_t key_bytes(int W);
+cudaError_t launch_count(int W, const Phase2Params& P, uint32_t grid, cudaStream_t st);
+struct FallbackParams {
+    const uint32_t* records;
+    const uint32_t* index;
+    uint64_t wb;
+    uint64_t r0, nrec;
+    uint32_t group, F;
+    int k;
+    void* keys;
+    uint32_t* cnt;
+    uint32_t mask;
+    uint32_t* fail;
+};
+cudaError_t launch_fallback(int W, const FallbackParams& F, uint64_t S, const Phase2Params& P, uint32_t grid,
+                            cudaStream_t st, int* launches);
+
+// per-bucket record / word / k-mer totals from the scanned offsets
+__global__ void k_sizes(const unsigned long long* off_r, const unsigned long long* off_w, uint32_t n_buckets,
+                        uint32_t C, unsigned long long* out_recs, unsigned long long* out_words) {
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n_buckets) return;
+    out_recs[b] = off_r[(uint64_t)(b + 1) * C] - off_r[(uint64_t)b * C];
+    out_words[b] = off_w[(uint64_t)(b + 1) * C] - off_w[(uint64_t)b * C];
+}
+}  // namespace tg
+
+using namespace tg;
+
+namespace {
+
+constexpr uint64_t FWD_SEED[4] = {0x3c8bfbb395c60474ULL, 0x3193c18562a02b4cULL, 0x295549f54be24456ULL,
+                                  0x20323ed082572324ULL};  // A C T G (nt codes), include/nt_hash.hpp:26-31
+
+inline uint64_t hrol(uint64_t x, int s) { s &= 63; return s ? (x << s) | (x >> (64 - s)) : x; }
+inline uint64_t hror(uint64_t x, int s) { s &= 63; return s ? (x >> s) | (x << (64 - s)) : x; }
+
+HashTables make_tables(int m) {
+    HashTables T;
+    for (int b = 0; b < 4; ++b) {
+        const int nt = b ^ (b >> 1);  // kache A0 C1 G2 T3 -> nt A0 C1 T2 G3
+        T.FW[b] = FWD_SEED[nt];
+        T.RV[b] = FWD_SEED[nt ^ 2];   // REV[b] = FWD[complement(b)], complement = b ^ 2
+    }
+    for (int o = 0; o < 4; ++o)
+        for (int i = 0; i < 4; ++i) {
+            T.CTF[o * 4 + i] = hrol(T.FW[o], m) ^ T.FW[i];
+            T.CTR[o * 4 + i] = hror(T.RV[o], 1) ^ hrol(T.RV[i], m - 1);
+        }
+    for (int v = 0; v < 256; ++v) {
+        uint64_t f = 0, r = 0;
+        for (int j = 0; j < 4; ++j) {
+            const int b = (v >> (6 - 2 * j)) & 3;
+            f ^= hrol(T.FW[b], 3 - j);
+            r ^= hrol(T.RV[b], j);
+        }
+        T.GF[v] = f;
+        T.GR[v] = r;
+    }
+    return T;
+}
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+uint32_t next_pow2_u32(uint64_t v) {
+    uint32_t p = 1;
+    while (p < v && p < (1u << 31)) p <<= 1;
+    return p;
+}
+
+// Layout of the small device counter buffer ctx->misc (byte offsets).
+constexpr size_t MISC_CUT_STATS = 0;    // u64[3]: k-mers, records, runs (k_cut)
+constexpr size_t MISC_BASES = 24;       // u64: ACGT bases (k_pack)
+constexpr size_t MISC_OVERFLOW = 32;    // u32: descriptor list overflow (k_cut)
+constexpr size_t MISC_OUT = 64;         // u64[3]: output cursor, distinct, fallback groups (k_count)
+constexpr size_t MISC_WORK = 96;        // u32: bucket queue head (k_count)
+constexpr size_t MISC_FAIL = 100;       // u32: fallback table overflow
+constexpr size_t MISC_NDESC = 256;      // u32[C]: descriptors per Phase-1 CTA
+constexpr size_t MISC_BYTES = MISC_NDESC + 4 * 65536;
+
+double now_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+struct tg_ctx {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    int n_sm = 0;
+    size_t smem_optin = 0;
+    unsigned host_threads = 1;
+    std::string err;
+    DevBuf seq, packed, valid, desc, xdesc, hist, offw, offr, sums, sizes, records, index, scratch, okeys, ocnt,
+        misc, fallback, fbtab, order, tables;
+    cudaEvent_t ev[12] = {};
+    tg_job* active = nullptr;
+    int prepared_m = -1;
+
+    tg_status fail(tg_status s, const std::string& msg) {
+        err = msg;
+        return s;
+    }
+    tg_status cuda_fail(cudaError_t e, const char* what) {
+        err = std::string(what) + ": " + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? TG_ERR_OOM : TG_ERR_CUDA;
+    }
+    cudaError_t ensure(DevBuf& b, size_t bytes) {
+        if (bytes <= b.cap && b.p) return cudaSuccess;
+        if (b.p) { cudaFree(b.p); b.p = nullptr; b.cap = 0; }
+        const size_t want = std::max<size_t>(bytes, 256);
+        cudaError_t e = cudaMalloc(&b.p, want);
+        if (e != cudaSuccess) { b.p = nullptr; return e; }
+        b.cap = want;
+        return cudaSuccess;
+    }
+};
+
+struct tg_job {
+    tg_ctx* ctx = nullptr;
+    tg_job_opts o{};
+    int W = 1;
+    int w = 0;
+    uint32_t L = 0;
+    // input stream
+    size_t n = 0;                  // bytes in ctx->seq (or the external buffer)
+    const uint8_t* ext = nullptr;  // single device feed, used in place
+    bool used_ctx_seq = false;
+    bool ran = false;
+    // layout of the last run
+    uint32_t p1_bits = 0, n_cta = 0;
+    uint64_t chunk = 0, desc_cap = 0, packed_words = 0;
+    // results
+    uint64_t n_out = 0;
+    tg_stats st{};
+    const uint8_t* seq_ptr() const { return ext ? ext : ctx->seq.as<uint8_t>(); }
+};
+
+#define CK(call, what)                                   \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return ctx->cuda_fail(e_, what); \
+    } while (0)
+
+extern "C" {
+
+const char* tg_version(void) { return "tuna-gb300 0.1 (sm_103a)"; }
+
+int tg_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+    return n;
+}
+
+tg_status tg_ctx_create(const tg_ctx_opts* opts, tg_ctx** out) {
+    if (!out) return TG_ERR_ARG;
+    *out = nullptr;
+    tg_ctx_opts o{};
+    if (opts) o = *opts;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return TG_ERR_CUDA;
+    if (o.device < 0 || o.device >= ndev) return TG_ERR_ARG;
+    tg_ctx* ctx = new tg_ctx();
+    ctx->device = o.device;
+    ctx->host_threads = o.host_threads ? o.host_threads : std::max(1u, std::thread::hardware_concurrency());
+    cudaError_t e = cudaSetDevice(o.device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->n_sm, cudaDevAttrMultiProcessorCount, o.device);
+    int optin = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, o.device);
+    ctx->smem_optin = (size_t)optin;
+    for (int i = 0; i < 12 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->ev[i]);
+    if (e != cudaSuccess) {
+        delete ctx;
+        return TG_ERR_CUDA;
+    }
+    *out = ctx;
+    return TG_OK;
+}
+
+tg_status tg_ctx_destroy(tg_ctx* ctx) {
+    if (!ctx) return TG_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->st) cudaStreamSynchronize(ctx->st);
+    DevBuf* bufs[] = {&ctx->seq, &ctx->packed, &ctx->valid, &ctx->desc, &ctx->xdesc, &ctx->hist, &ctx->offw,
+                      &ctx->offr, &ctx->sums, &ctx->sizes, &ctx->records, &ctx->index, &ctx->scratch,
+                      &ctx->okeys, &ctx->ocnt, &ctx->misc, &ctx->fallback, &ctx->fbtab, &ctx->order,
+                      &ctx->tables};
+    for (DevBuf* b : bufs)
+        if (b->p) cudaFree(b->p);
+    for (auto& e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->st) cudaStreamDestroy(ctx->st);
+    delete ctx;
+    return TG_OK;
+}
+
+const char* tg_last_error(const tg_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+tg_status tg_job_begin(tg_ctx* ctx, const tg_job_opts* opts, tg_job** out) {
+    if (!ctx || !opts || !out) return TG_ERR_ARG;
+    *out = nullptr;
+    const tg_job_opts& o = *opts;
+    if (o.k < 2 || o.k > 256) return ctx->fail(TG_ERR_ARG, "k-mer length must be in [2, 256]");
+    if (o.m < 1 || o.m > 32) return ctx->fail(TG_ERR_ARG, "minimizer length must be in [1, 32]");
+    if (o.m >= o.k) return ctx->fail(TG_ERR_ARG, "minimizer length must be strictly less than k-mer length");
+    if (o.k > 63) return ctx->fail(TG_ERR_UNSUPPORTED, "this GPU path supports k <= 63");
+    if (o.n_parts & (o.n_parts - 1)) return ctx->fail(TG_ERR_ARG, "n_parts must be a power of two");
+    if (o.gpu_parts & (o.gpu_parts - 1)) return ctx->fail(TG_ERR_ARG, "gpu_parts must be a power of two");
+    if (o.gpu_parts > P1_MAX) return ctx->fail(TG_ERR_ARG, "gpu_parts must be <= 4096");
+    if (ctx->active) return ctx->fail(TG_ERR_STATE, "another job is active on this context");
+    tg_job* j = new tg_job();
+    j->ctx = ctx;
+    j->o = o;
+    if (j->o.n_parts == 0) j->o.n_parts = 16;
+    j->W = o.k <= 31 ? 1 : 2;
+    j->w = o.k - o.m;
+    const uint32_t hdr_max = (2u * o.k - o.m <= 255u) ? 255u : 65535u;
+    j->L = hdr_max + 1 - o.k;
+    ctx->active = j;
+    *out = j;
+    return TG_OK;
+}
+
+static tg_status append_stream(tg_job* j, const uint8_t* src, size_t len, cudaMemcpyKind kind) {
+    tg_ctx* ctx = j->ctx;
+    if (j->ran) return ctx->fail(TG_ERR_STATE, "feed after run");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    // a previous single device feed used in place is moved into the context buffer
+    if (j->ext) {
+        const size_t need = j->n + 1;
+        CK(ctx->ensure(ctx->seq, need + len + 1), "alloc seq");
+        CK(cudaMemcpyAsync(ctx->seq.p, j->ext, j->n, cudaMemcpyDeviceToDevice, ctx->st), "copy seq");
+        j->ext = nullptr;
+        j->used_ctx_seq = true;
+    }
+    const size_t need = j->n + len + 1;
+    if (need > ctx->seq.cap) {
+        DevBuf nb;
+        CK(cudaMalloc(&nb.p, std::max(need, 2 * ctx->seq.cap)), "alloc seq");
+        nb.cap = std::max(need, 2 * ctx->seq.cap);
+        if (j->n) CK(cudaMemcpyAsync(nb.p, ctx->seq.p, j->n, cudaMemcpyDeviceToDevice, ctx->st), "grow seq");
+        CK(cudaStreamSynchronize(ctx->st), "grow seq");
+        if (ctx->seq.p) cudaFree(ctx->seq.p);
+        ctx->seq = nb;
+    }
+    uint8_t* d = ctx->seq.as<uint8_t>();
+    const double t0 = now_ms();
+    if (len) CK(cudaMemcpyAsync(d + j->n, src, len, kind, ctx->st), "copy input");
+    CK(cudaMemsetAsync(d + j->n + len, '\n', 1, ctx->st), "separator");
+    CK(cudaStreamSynchronize(ctx->st), "copy input");
+    if (kind == cudaMemcpyHostToDevice) j->st.h2d_ms += now_ms() - t0;
+    j->n += len + 1;
+    j->used_ctx_seq = true;
+    j->st.input_bytes += len;
+    return TG_OK;
+}
+
+tg_status tg_job_feed_seq(tg_job* j, const uint8_t* seq, size_t len) {
+    if (!j || (!seq && len)) return TG_ERR_ARG;
+    return append_stream(j, seq, len, cudaMemcpyHostToDevice);
+}
+
+tg_status tg_job_feed_seq_device(tg_job* j, const uint8_t* dseq, size_t len) {
+    if (!j || (!dseq && len)) return TG_ERR_ARG;
+    if (j->ran) return j->ctx->fail(TG_ERR_STATE, "feed after run");
+    if (j->n == 0 && !j->used_ctx_seq) {
+        j->ext = dseq;
+        j->n = len;
+        j->st.input_bytes += len;
+        return TG_OK;
+    }
+    return append_stream(j, dseq, len, cudaMemcpyDeviceToDevice);
+}
+
+tg_status tg_job_feed_fastx(tg_job* j, const uint8_t* data, size_t len) {
+    if (!j || (!data && len)) return TG_ERR_ARG;
+    if (len == 0) return j->ctx->fail(TG_ERR_PARSE, "Empty file");
+    std::vector<uint8_t> s;
+    tgh::fastx_to_stream(data, len, s);
+    return append_stream(j, s.data(), s.size(), cudaMemcpyHostToDevice);
+}
+
+tg_status tg_job_feed_file(tg_job* j, const char* path) {
+    if (!j || !path) return TG_ERR_ARG;
+    std::vector<uint8_t> raw;
+    const std::string err = tgh::read_input_file(path, raw);
+    if (!err.empty()) {
+        const bool empty = err.rfind("Empty file", 0) == 0;
+        return j->ctx->fail(empty ? TG_ERR_PARSE : TG_ERR_IO, err);
+    }
+    std::vector<uint8_t> s;
+    tgh::fastx_to_stream(raw.data(), raw.size(), s);
+    raw.clear();
+    raw.shrink_to_fit();
+    return append_stream(j, s.data(), s.size(), cudaMemcpyHostToDevice);
+}
+
+// Phase 1 cut (optionally the export variant) over the current stream.
+static tg_status run_cut(tg_job* j, bool exp, uint32_t p1_bits, int* launches) {
+    tg_ctx* ctx = j->ctx;
+    const uint64_t n = j->n;
+    const uint32_t p1 = 1u << p1_bits;
+    const size_t smem = cut_smem_bytes(j->w, p1, exp);
+    if (smem > ctx->smem_optin) return ctx->fail(TG_ERR_UNSUPPORTED, "phase-1 tile does not fit in shared memory");
+    const uint32_t per_sm = std::max<uint32_t>(1, std::min<uint32_t>(2, (uint32_t)(228u * 1024u / (smem + 1024))));
+    uint32_t C = (uint32_t)ctx->n_sm * per_sm;
+    uint64_t chunk = (n + C - 1) / C;
+    chunk = std::max<uint64_t>(CUT_TILE, (chunk + CUT_TILE - 1) / CUT_TILE * CUT_TILE);
+    C = (uint32_t)std::max<uint64_t>(1, (n + chunk - 1) / chunk);
+    j->n_cta = C;
+    j->chunk = chunk;
+    j->p1_bits = p1_bits;
+    // descriptors: about 2/(w+2) records per k-mer for random minimizers; grow on overflow
+    double factor = std::min(1.0, 3.0 / (j->w + 2));
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        const uint64_t cap = (uint64_t)(chunk * factor) + 2ull * CUT_TILE + j->L + 64;
+        j->desc_cap = cap;
+        CK(ctx->ensure(ctx->desc, (size_t)C * cap * 8), "alloc descriptors");
+        if (exp) CK(ctx->ensure(ctx->xdesc, (size_t)C * cap * 24), "alloc export descriptors");
+        const size_t hist_bytes = (size_t)2 * p1 * C * 4 + (size_t)p1 * 8;
+        CK(ctx->ensure(ctx->hist, hist_bytes), "alloc histograms");
+        CK(cudaMemsetAsync(ctx->hist.as<uint8_t>() + (size_t)2 * p1 * C * 4, 0, (size_t)p1 * 8, ctx->st), "memset");
+        CK(cudaMemsetAsync(ctx->misc.as<uint8_t>() + MISC_CUT_STATS, 0, 24, ctx->st), "memset");
+        CK(cudaMemsetAsync(ctx->misc.as<uint8_t>() + MISC_OVERFLOW, 0, 4, ctx->st), "memset");
+        CutParams P{};
+        P.packed = ctx->packed.as<uint32_t>();
+        P.valid = ctx->valid.as<uint32_t>();
+        P.n = n;
+        P.k = j->o.k; P.m = j->o.m; P.w = j->w; P.L = j->L;
+        P.p1_bits = p1_bits;
+        P.n_cta = C;
+        P.chunk = chunk;
+        P.desc = ctx->desc.as<uint64_t>();
+        P.desc_cap = cap;
+        P.n_desc = reinterpret_cast<uint32_t*>(ctx->misc.as<uint8_t>() + MISC_NDESC);
+        P.hist = ctx->hist.as<uint32_t>();
+        P.stats = reinterpret_cast<unsigned long long*>(ctx->misc.as<uint8_t>() + MISC_CUT_STATS);
+        P.overflow = reinterpret_cast<uint32_t*>(ctx->misc.as<uint8_t>() + MISC_OVERFLOW);
+        P.xdesc = exp ? ctx->xdesc.as<uint64_t>() : nullptr;
+        CK(cudaEventRecord(ctx->ev[2], ctx->st), "event");
+        CK(launch_cut(P, ctx->tables.as<HashTables>(), exp, ctx->st), "k_cut");
+        CK(cudaEventRecord(ctx->ev[3], ctx->st), "event");
+        ++*launches;
+        uint32_t ovf = 0;
+        CK(cudaMemcpyAsync(&ovf, ctx->misc.as<uint8_t>() + MISC_OVERFLOW, 4, cudaMemcpyDeviceToHost, ctx->st), "d2h");
+        CK(cudaStreamSynchronize(ctx->st), "k_cut");
+        if (!ovf) return TG_OK;
+        factor = 1.0;  // every k-mer start can open a record at most once
+    }
+    return ctx->fail(TG_ERR_DEVICE, "descriptor capacity exceeded");
+}
+
+tg_status tg_job_run(tg_job* j) {
+    if (!j) return TG_ERR_ARG;
+    tg_ctx* ctx = j->ctx;
+    if (j->ran) return ctx->fail(TG_ERR_STATE, "job already ran");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    int launches = 0;
+    const uint64_t n = j->n;
+    const int k = j->o.k;
+    const int W = j->W;
+    j->ran = true;
+    // hash tables for m
+    CK(ctx->ensure(ctx->tables, sizeof(HashTables)), "alloc tables");
+    if (ctx->prepared_m != j->o.m) {
+        const HashTables T = make_tables(j->o.m);
+        CK(cudaMemcpy(ctx->tables.p, &T, sizeof T, cudaMemcpyHostToDevice), "upload tables");
+        ctx->prepared_m = j->o.m;
+    }
+    CK(ctx->ensure(ctx->misc, MISC_BYTES), "alloc misc");
+    // ---- pack
+    uint64_t pw = (TG_PAD + n + CUT_TILE + 2 * MAX_W + 640) / 16 + 16;
+    pw = (pw + 1) & ~uint64_t(1);
+    j->packed_words = pw;
+    CK(ctx->ensure(ctx->packed, pw * 4), "alloc packed");
+    CK(ctx->ensure(ctx->valid, (pw / 2) * 4 + 64), "alloc valid");
+    CK(cudaMemsetAsync(ctx->misc.p, 0, MISC_NDESC, ctx->st), "memset");
+    CK(cudaEventRecord(ctx->ev[0], ctx->st), "event");
+    CK(launch_pack(j->seq_ptr(), n, ctx->packed.as<uint32_t>(), ctx->valid.as<uint32_t>(), pw,
+                   reinterpret_cast<unsigned long long*>(ctx->misc.as<uint8_t>() + MISC_BASES), ctx->st), "k_pack");
+    ++launches;
+    CK(cudaEventRecord(ctx->ev[1], ctx->st), "event");
+    unsigned long long n_bases = 0;
+    CK(cudaMemcpyAsync(&n_bases, ctx->misc.as<uint8_t>() + MISC_BASES, 8, cudaMemcpyDeviceToHost, ctx->st), "d2h");
+    // ---- phase 1: cut
+    uint32_t p1 = j->o.gpu_parts;
+    if (!p1) p1 = std::min<uint32_t>(P1_MAX, std::max<uint32_t>(16, next_pow2_u32(n / 32768)));
+    uint32_t p1_bits = 0;
+    while ((1u << p1_bits) < p1) ++p1_bits;
+    tg_status s = run_cut(j, false, p1_bits, &launches);
+    if (s != TG_OK) return s;
+    unsigned long long cstats[3] = {0, 0, 0};
+    CK(cudaMemcpyAsync(cstats, ctx->misc.as<uint8_t>() + MISC_CUT_STATS, 24, cudaMemcpyDeviceToHost, ctx->st), "d2h");
+    const uint32_t C = j->n_cta;
+    const uint64_t nhist = (uint64_t)p1 * C;
+    // ---- scans: offsets over [bucket][cta] of words and records
+    CK(ctx->ensure(ctx->offw, (nhist + 1) * 8), "alloc offsets");
+    CK(ctx->ensure(ctx->offr, (nhist + 1) * 8), "alloc offsets");
+    CK(ctx->ensure(ctx->sums, ((nhist + 8191) / 8192 + 2) * 8 * 2), "alloc sums");
+    unsigned long long* sums = ctx->sums.as<unsigned long long>();
+    const uint64_t nsum = (nhist + 8191) / 8192 + 1;
+    CK(cudaEventRecord(ctx->ev[4], ctx->st), "event");
+    CK(launch_scan(ctx->hist.as<uint32_t>(), nhist, ctx->offw.as<unsigned long long>(), sums,
+                   ctx->offw.as<unsigned long long>() + nhist, ctx->st, &launches), "scan");
+    CK(launch_scan(ctx->hist.as<uint32_t>() + nhist, nhist, ctx->offr.as<unsigned long long>(), sums + nsum,
+                   ctx->offr.as<unsigned long long>() + nhist, ctx->st, &launches), "scan");
+    CK(ctx->ensure(ctx->sizes, (size_t)p1 * 16), "alloc sizes");
+    k_sizes<<<(p1 + 255) / 256, 256, 0, ctx->st>>>(ctx->offr.as<unsigned long long>(), ctx->offw.as<unsigned long long>(),
+                                                   p1, C, ctx->sizes.as<unsigned long long>(),
+                                                   ctx->sizes.as<unsigned long long>() + p1);
+    ++launches;
+    CK(cudaGetLastError(), "k_sizes");
+    std::vector<unsigned long long> hsz(2 * (size_t)p1), hk(p1);
+    unsigned long long tot_w = 0, tot_r = 0;
+    CK(cudaMemcpyAsync(hsz.data(), ctx->sizes.p, (size_t)p1 * 16, cudaMemcpyDeviceToHost, ctx->st), "d2h");
+    CK(cudaMemcpyAsync(hk.data(), ctx->hist.as<uint8_t>() + (size_t)2 * nhist * 4, (size_t)p1 * 8,
+                       cudaMemcpyDeviceToHost, ctx->st), "d2h");
+    CK(cudaMemcpyAsync(&tot_w, ctx->offw.as<unsigned long long>() + nhist, 8, cudaMemcpyDeviceToHost, ctx->st), "d2h");
+    CK(cudaMemcpyAsync(&tot_r, ctx->offr.as<unsigned long long>() + nhist, 8, cudaMemcpyDeviceToHost, ctx->st), "d2h");
+    CK(cudaStreamSynchronize(ctx->st), "phase 1");
+    // ---- buffers for records, index, scratch, output
+    uint64_t max_recs = 0;
+    for (uint32_t b = 0; b < p1; ++b) max_recs = std::max<uint64_t>(max_recs, hsz[b]);
+    const uint64_t n_kmers = cstats[0];
+    CK(ctx->ensure(ctx->records, tot_w * 4 + 64), "alloc records");
+    CK(ctx->ensure(ctx->index, tot_r * 4 + 64), "alloc index");
+    const uint32_t slots = W == 1 ? 8192 : 4096;
+    const size_t smem2 = count_smem_bytes(W, slots);
+    const uint32_t per_sm2 = std::max<uint32_t>(1, std::min<uint32_t>(2, (uint32_t)(228u * 1024u / (smem2 + 1024))));
+    const uint32_t grid2 = (uint32_t)ctx->n_sm * per_sm2;
+    CK(ctx->ensure(ctx->scratch, (size_t)grid2 * (max_recs + 1) * 4), "alloc scratch");
+    const uint64_t out_cap = std::max<uint64_t>(n_kmers, 1);
+    CK(ctx->ensure(ctx->okeys, out_cap * key_bytes(W)), "alloc output keys");
+    CK(ctx->ensure(ctx->ocnt, out_cap * 4), "alloc output counts");
+    CK(ctx->ensure(ctx->fallback, 4096 * 12), "alloc fallback list");
+    // bucket order: most k-mers first
+    std::vector<uint32_t> order(p1);
+    std::iota(order.begin(), order.end(), 0u);
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return hk[a] > hk[b]; });
+    CK(ctx->ensure(ctx->order, (size_t)p1 * 4), "alloc order");
+    CK(cudaMemcpyAsync(ctx->order.p, order.data(), (size_t)p1 * 4, cudaMemcpyHostToDevice, ctx->st), "h2d");
+    // ---- scatter
+    ScatterParams SP{};
+    SP.packed = ctx->packed.as<uint32_t>();
+    SP.k = k;
+    SP.p1_bits = p1_bits;
+    SP.n_cta = C;
+    SP.chunk = j->chunk;
+    SP.desc = ctx->desc.as<uint64_t>();
+    SP.desc_cap = j->desc_cap;
+    SP.n_desc = reinterpret_cast<const uint32_t*>(ctx->misc.as<uint8_t>() + MISC_NDESC);
+    SP.off_w = ctx->offw.as<unsigned long long>();
+    SP.off_r = ctx->offr.as<unsigned long long>();
+    SP.records = ctx->records.as<uint32_t>();
+    SP.index = ctx->index.as<uint32_t>();
+    CK(cudaEventRecord(ctx->ev[5], ctx->st), "event");
+    CK(launch_scatter(SP, ctx->st), "k_scatter");
+    ++launches;
+    CK(cudaEventRecord(ctx->ev[6], ctx->st), "event");
+    // ---- phase 2
+    unsigned long long* out_n = reinterpret_cast<unsigned long long*>(ctx->misc.as<uint8_t>() + MISC_OUT);
+    uint32_t* work = reinterpret_cast<uint32_t*>(ctx->misc.as<uint8_t>() + MISC_WORK);
+    CK(cudaMemsetAsync(out_n, 0, 24, ctx->st), "memset");
+    CK(cudaMemsetAsync(work, 0, 4, ctx->st), "memset");
+    Phase2Params QP{};
+    QP.records = ctx->records.as<uint32_t>();
+    QP.index = ctx->index.as<uint32_t>();
+    QP.off_w = ctx->offw.as<unsigned long long>();
+    QP.off_r = ctx->offr.as<unsigned long long>();
+    QP.n_cta1 = C;
+    QP.n_buckets = p1;
+    QP.order = ctx->order.as<uint32_t>();
+    QP.k = k;
+    QP.fine_bits = 24 - p1_bits;
+    QP.target = slots / 2;
+    QP.ci = j->o.ci;
+    QP.cx = j->o.cx;
+    QP.work = work;
+    QP.scratch = ctx->scratch.as<uint32_t>();
+    QP.scratch_cap = max_recs + 1;
+    QP.out_keys = ctx->okeys.p;
+    QP.out_counts = ctx->ocnt.as<uint32_t>();
+    QP.out_n = out_n;
+    QP.out_cap = out_cap;
+    QP.fallback = ctx->fallback.as<uint32_t>();
+    QP.fallback_cap = 4096;
+    QP.bucket_kmers = reinterpret_cast<const unsigned long long*>(ctx->hist.as<uint8_t>() + (size_t)2 * nhist * 4);
+    QP.smem_slots = slots;
+    CK(launch_count(W, QP, grid2, ctx->st), "k_count");
+    ++launches;
+    CK(cudaEventRecord(ctx->ev[7], ctx->st), "event");
+    unsigned long long on[3] = {0, 0, 0};
+    CK(cudaMemcpyAsync(on, out_n, 24, cudaMemcpyDeviceToHost, ctx->st), "d2h");
+    CK(cudaStreamSynchronize(ctx->st), "phase 2");
+    // ---- groups that did not fit in shared memory
+    if (on[2] > 0) {
+        if (on[2] > 4096) return ctx->fail(TG_ERR_TABLE, "too many overflowing groups");
+        std::vector<uint32_t> fl(3 * on[2]);
+        CK(cudaMemcpy(fl.data(), ctx->fallback.p, fl.size() * 4, cudaMemcpyDeviceToHost), "d2h");
+        std::vector<unsigned long long> offr_h(2), offw_h(1);
+        for (unsigned long long i = 0; i < on[2]; ++i) {
+            const uint32_t b = fl[3 * i], g = fl[3 * i + 1], F = fl[3 * i + 2];
+            unsigned long long r01[2], wb;
+            CK(cudaMemcpy(&r01[0], ctx->offr.as<unsigned long long>() + (uint64_t)b * C, 8, cudaMemcpyDeviceToHost), "d2h");
+            CK(cudaMemcpy(&r01[1], ctx->offr.as<unsigned long long>() + (uint64_t)(b + 1) * C, 8, cudaMemcpyDeviceToHost), "d2h");
+            CK(cudaMemcpy(&wb, ctx->offw.as<unsigned long long>() + (uint64_t)b * C, 8, cudaMemcpyDeviceToHost), "d2h");
+            uint64_t S = 1024;
+            while (S < 2 * hk[b] + 2) S <<= 1;
+            const size_t kbytes = (size_t)S * key_bytes(W);
+            CK(ctx->ensure(ctx->fbtab, kbytes + (size_t)S * 4 + 16), "alloc fallback table");
+            FallbackParams FP{};
+            FP.records = ctx->records.as<uint32_t>();
+            FP.index = ctx->index.as<uint32_t>();
+            FP.wb = wb;
+            FP.r0 = r01[0];
+            FP.nrec = r01[1] - r01[0];
+            FP.group = g;
+            FP.F = F;
+            FP.k = k;
+            FP.keys = ctx->fbtab.p;
+            FP.cnt = reinterpret_cast<uint32_t*>(ctx->fbtab.as<uint8_t>() + kbytes);
+            FP.mask = (uint32_t)(S - 1);
+            FP.fail = reinterpret_cast<uint32_t*>(ctx->misc.as<uint8_t>() + MISC_FAIL);
+            if (S > (1ull << 32)) return ctx->fail(TG_ERR_TABLE, "fallback table too large");
+            CK(cudaMemsetAsync(FP.fail, 0, 4, ctx->st), "memset");
+            CK(launch_fallback(W, FP, S, QP, (uint32_t)ctx->n_sm * 4, ctx->st, &launches), "fallback");
+            uint32_t failed = 0;
+            CK(cudaMemcpyAsync(&failed, FP.fail, 4, cudaMemcpyDeviceToHost, ctx->st), "d2h");
+            CK(cudaStreamSynchronize(ctx->st), "fallback");
+            if (failed) return ctx->fail(TG_ERR_TABLE, "fallback table overflow");
+        }
+        CK(cudaMemcpyAsync(on, out_n, 16, cudaMemcpyDeviceToHost, ctx->st), "d2h");
+        CK(cudaStreamSynchronize(ctx->st), "fallback");
+    }
+    CK(cudaEventRecord(ctx->ev[8], ctx->st), "event");
+    CK(cudaEventSynchronize(ctx->ev[8]), "sync");
+    if (on[0] > out_cap) return ctx->fail(TG_ERR_TABLE, "output capacity exceeded");
+    j->n_out = on[0];
+    // ---- stats
+    float ms = 0;
+    tg_stats& S = j->st;
+    S.bases = n_bases;
+    S.runs = cstats[2];
+    S.kmers = cstats[0];
+    S.superkmers = cstats[1];
+    S.distinct = on[1];
+    S.out = on[0];
+    S.gpu_parts = p1;
+    S.fallback_groups = on[2];
+    S.record_bytes = tot_w * 4;
+    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]); S.pack_ms = ms;
+    cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]); S.phase1_cut_ms = ms;
+    float scan_ms = 0;
+    cudaEventElapsedTime(&scan_ms, ctx->ev[4], ctx->ev[5]);
+    cudaEventElapsedTime(&ms, ctx->ev[5], ctx->ev[6]); S.phase1_scatter_ms = ms;
+    S.phase1_ms = S.phase1_cut_ms + scan_ms + S.phase1_scatter_ms;
+    cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[8]); S.phase2_ms = ms;
+    S.gpu_launches = (uint64_t)launches;
+    uint32_t fmax = 1;
+    for (uint32_t b = 0; b < p1; ++b) {
+        uint32_t F = 1;
+        while ((uint64_t)F * (slots / 2) < hk[b] && F < 1024 && F < (1u << (24 - p1_bits))) F <<= 1;
+        fmax = std::max(fmax, F);
+    }
+    S.fine_groups_max = fmax;
+    return TG_OK;
+}
+
+tg_status tg_job_stats(const tg_job* j, tg_stats* out) {
+    if (!j || !out) return TG_ERR_ARG;
+    *out = j->st;
+    return TG_OK;
+}
+
+uint64_t tg_job_result_size(const tg_job* j) { return j ? j->n_out : 0; }
+int tg_job_key_words(const tg_job* j) { return j ? j->W : 0; }
+
+tg_status tg_job_result_copy(tg_job* j, uint64_t* keys, uint32_t* counts, uint64_t first, uint64_t n) {
+    if (!j) return TG_ERR_ARG;
+    tg_ctx* ctx = j->ctx;
+    if (!j->ran) return ctx->fail(TG_ERR_STATE, "result before run");
+    if (first + n > j->n_out) return ctx->fail(TG_ERR_ARG, "result range out of bounds");
+    if (!n) return TG_OK;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const double t0 = now_ms();
+    if (keys)
+        CK(cudaMemcpyAsync(keys, ctx->okeys.as<uint8_t>() + first * key_bytes(j->W), n * key_bytes(j->W),
+                           cudaMemcpyDeviceToHost, ctx->st), "d2h keys");
+    if (counts)
+        CK(cudaMemcpyAsync(counts, ctx->ocnt.as<uint32_t>() + first, n * 4, cudaMemcpyDeviceToHost, ctx->st),
+           "d2h counts");
+    CK(cudaStreamSynchronize(ctx->st), "d2h");
+    j->st.d2h_ms += now_ms() - t0;
+    return TG_OK;
+}
+
+struct DrainCtx {
+    tg_sink_fn sink;
+    void* user;
+};
+static bool drain_sink(const std::string& chunk, uint64_t npairs, void* u) {
+    DrainCtx* d = static_cast<DrainCtx*>(u);
+    return d->sink(chunk.data(), chunk.size(), npairs, d->user) == 0;
+}
+
+static tg_status host_results(tg_job* j, std::vector<uint64_t>& keys, std::vector<uint32_t>& cnt) {
+    keys.resize(std::max<uint64_t>(1, j->n_out) * j->W);
+    cnt.resize(std::max<uint64_t>(1, j->n_out));
+    return tg_job_result_copy(j, keys.data(), cnt.data(), 0, j->n_out);
+}
+
+tg_status tg_job_drain(tg_job* j, tg_format fmt, tg_sink_fn sink, void* user) {
+    if (!j || !sink || (int)fmt < 0 || (int)fmt > 2) return TG_ERR_ARG;
+    std::vector<uint64_t> keys;
+    std::vector<uint32_t> cnt;
+    tg_status s = host_results(j, keys, cnt);
+    if (s != TG_OK) return s;
+    tgh::Pairs p{keys.data(), cnt.data(), j->n_out, j->W, j->o.k};
+    DrainCtx d{sink, user};
+    if (!tgh::format_parallel(p, (int)fmt, j->ctx->host_threads, drain_sink, &d))
+        return j->ctx->fail(TG_ERR_IO, "output sink stopped");
+    return TG_OK;
+}
+
+struct FileSink {
+    FILE* f;
+};
+static int file_sink(const void* data, size_t bytes, uint64_t, void* u) {
+    FileSink* fs = static_cast<FileSink*>(u);
+    return fwrite(data, 1, bytes, fs->f) == bytes ? 0 : 1;
+}
+
+tg_status tg_job_write(tg_job* j, tg_format fmt, const char* path) {
+    if (!j || !path) return TG_ERR_ARG;
+    FILE* f = fopen(path, "wb");
+    if (!f) return j->ctx->fail(TG_ERR_IO, std::string("cannot open output file: ") + path);
+    FileSink fs{f};
+    tg_status s = TG_OK;
+    if (fmt == TG_FMT_KFF) {
+        const std::string h = tgh::kff_header(j->o.k, j->n_out);
+        if (fwrite(h.data(), 1, h.size(), f) != h.size()) s = TG_ERR_IO;
+    }
+    if (s == TG_OK) s = tg_job_drain(j, fmt, file_sink, &fs);
+    if (s == TG_OK && fmt == TG_FMT_KFF) {
+        const std::string t = tgh::kff_footer();
+        if (fwrite(t.data(), 1, t.size(), f) != t.size()) s = TG_ERR_IO;
+    }
+    if (fclose(f) != 0 && s == TG_OK) s = TG_ERR_IO;
+    if (s == TG_ERR_IO) j->ctx->fail(s, std::string("failed while writing output file: ") + path);
+    return s;
+}
+
+tg_status tg_job_export_partitions(tg_job* j, tg_part_sink_fn sink, void* user) {
+    if (!j || !sink) return TG_ERR_ARG;
+    tg_ctx* ctx = j->ctx;
+    if (!j->ran) return ctx->fail(TG_ERR_STATE, "export before run");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    int launches = 0;
+    // packed bases stay valid until the next run on this context
+    tg_status s = run_cut(j, true, 0, &launches);
+    if (s != TG_OK) return s;
+    const uint32_t C = j->n_cta;
+    std::vector<uint32_t> nd(C);
+    CK(cudaMemcpy(nd.data(), ctx->misc.as<uint8_t>() + MISC_NDESC, (size_t)C * 4, cudaMemcpyDeviceToHost), "d2h");
+    std::vector<uint32_t> pk(j->packed_words);
+    CK(cudaMemcpy(pk.data(), ctx->packed.p, pk.size() * 4, cudaMemcpyDeviceToHost), "d2h packed");
+    const uint32_t np = j->o.n_parts;
+    std::vector<std::vector<uint8_t>> parts(np);
+    std::vector<uint64_t> xd;
+    const int k = j->o.k;
+    const bool u16hdr = (2 * k - j->o.m) > 255;
+    for (uint32_t c = 0; c < C; ++c) {
+        xd.resize((size_t)nd[c] * 3);
+        if (!nd[c]) continue;
+        CK(cudaMemcpy(xd.data(), ctx->xdesc.as<uint64_t>() + (size_t)c * j->desc_cap * 3, xd.size() * 8,
+                      cudaMemcpyDeviceToHost), "d2h");
+        for (uint32_t i = 0; i < nd[c]; ++i) {
+            const uint64_t st = xd[3 * i], mh = xd[3 * i + 1], x = xd[3 * i + 2];
+            const uint32_t nk = (uint32_t)(x & 0xFFFFFFFFu), mp = (uint32_t)(x >> 32);
+            const uint32_t len = nk + k - 1;
+            std::vector<uint8_t>& out = parts[mh & (np - 1)];
+            if (u16hdr) {
+                const uint16_t l16 = (uint16_t)len, p16 = (uint16_t)mp;
+                out.insert(out.end(), reinterpret_cast<const uint8_t*>(&l16), reinterpret_cast<const uint8_t*>(&l16) + 2);
+                out.insert(out.end(), reinterpret_cast<const uint8_t*>(&p16), reinterpret_cast<const uint8_t*>(&p16) + 2);
+            } else {
+                out.push_back((uint8_t)len);
+                out.push_back((uint8_t)mp);
+            }
+            const size_t o = out.size();
+            out.resize(o + (len + 3) / 4, 0);
+            for (uint32_t b = 0; b < len; ++b) {
+                const uint64_t a = st + b + TG_PAD;
+                const uint32_t code = (pk[a >> 4] >> (30 - 2 * (a & 15))) & 3u;
+                out[o + (b >> 2)] |= (uint8_t)(code << (6 - 2 * (b & 3)));
+            }
+        }
+    }
+    for (uint32_t p = 0; p < np; ++p)
+        if (sink(p, parts[p].data(), parts[p].size(), user) != 0) return ctx->fail(TG_ERR_IO, "partition sink stopped");
+    return TG_OK;
+}
+
+tg_status tg_job_end(tg_job* j) {
+    if (!j) return TG_ERR_ARG;
+    if (j->ctx->active == j) j->ctx->active = nullptr;
+    delete j;
+    return TG_OK;
+}
+
+tg_status tg_count_seq(tg_ctx* ctx, const tg_job_opts* opts, const uint8_t* seq, size_t len, uint64_t* keys,
+                       uint32_t* counts, uint64_t cap, uint64_t* n_out, tg_stats* stats) {
+    if (!ctx || !opts || !n_out) return TG_ERR_ARG;
+    tg_job* j = nullptr;
+    tg_status s = tg_job_begin(ctx, opts, &j);
+    if (s != TG_OK) return s;
+    s = tg_job_feed_seq(j, seq, len);
+    if (s == TG_OK) s = tg_job_run(j);
+    if (s == TG_OK) {
+        *n_out = j->n_out;
+        if (j->n_out > cap) s = ctx->fail(TG_ERR_ARG, "result buffer too small");
+        else s = tg_job_result_copy(j, keys, counts, 0, j->n_out);
+    }
+    if (stats) *stats = j->st;
+    tg_job_end(j);
+    return s;
+}
+
+}  // extern "C"

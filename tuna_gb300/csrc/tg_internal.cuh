@@ -1,0 +1,206 @@
+// tg_internal.cuh — shared definitions of the GB300 counting kernels.
+//
+// Data layout in HBM for one job (N = bytes of the sequence stream):
+//   seq     u8[N]            ASCII stream; any byte outside [ACGTacgt] separates runs
+//   packed  u32[]            2-bit kache codes (A0 C1 G2 T3), 16 bases per word,
+//                            first base in bits 31:30 (MSB-first, like the
+//                            reference's superkmer bytes); base g is stored at
+//                            index g + TG_PAD, the TG_PAD leading bases are 0
+//   valid   u32[]            1 bit per base, LSB-first, same TG_PAD offset
+//   desc    u64[C][cap]      per Phase-1 CTA: one descriptor per superkmer record
+//                            (start relative to the CTA chunk, k-mer count, the low
+//                            24 bits of its minimizer hash)
+//   hist    u32[2][P][C]     record words / record count per (bucket, CTA)
+//   records u32[]            bucket-major: [hdr][ceil(len/16) packed words] ...
+//   index   u32[]            bucket-major: word offset of each record in its bucket
+//   out     keys + u32 counts of the distinct k-mers that pass ci/cx
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace tg {
+
+constexpr int TG_PAD = 32;          // leading invalid bases in packed/valid
+constexpr int CUT_TILE = 1024;      // k-mer start positions per Phase-1 tile
+constexpr int CUT_THREADS = 256;
+constexpr int MAX_W = 255;          // w = k - m
+constexpr int P1_MAX = 4096;        // max internal buckets (smem histogram)
+constexpr uint32_t NONE32 = 0xFFFFFFFFu;
+
+// Event types of the Phase-1 tile event list.
+constexpr uint32_t EV_OWNED = 1u;   // record start owned by this CTA
+constexpr uint32_t EV_CUT = 2u;     // cut (record start of any owner or run end)
+
+struct HashTables {
+    // indexed by kache codes: FW[b] = FWD[nt(b)], RV[b] = REV[nt(b)]
+    uint64_t FW[4], RV[4];
+    uint64_t CTF[16], CTR[16];   // roll terms, index (out << 2) | in
+    uint64_t GF[256], GR[256];   // 4-base group terms for initialisation
+};
+
+struct CutParams {
+    const uint32_t* packed;
+    const uint32_t* valid;
+    uint64_t n;              // sequence stream length (positions)
+    int k, m, w;
+    uint32_t L;              // max k-mers per record (forced split period)
+    uint32_t p1_bits;        // log2 internal bucket count
+    uint32_t n_cta;
+    uint64_t chunk;          // k-mer start positions per CTA (multiple of CUT_TILE)
+    uint64_t* desc;          // [n_cta][desc_cap]
+    uint64_t desc_cap;
+    uint32_t* n_desc;        // [n_cta]
+    uint32_t* hist;          // [2][P][n_cta] words, records
+    unsigned long long* stats;  // [0] kmers, [1] records, [2] runs
+    uint32_t* overflow;      // set when a CTA's descriptor list is full
+    // export mode: full descriptors (start, minimizer hash, min_pos, nk)
+    uint64_t* xdesc;         // [n_cta][desc_cap][3] or null
+};
+
+struct ScatterParams {
+    const uint32_t* packed;
+    int k;
+    uint32_t p1_bits;
+    uint32_t n_cta;
+    uint64_t chunk;
+    const uint64_t* desc;
+    uint64_t desc_cap;
+    const uint32_t* n_desc;
+    const unsigned long long* off_w;   // exclusive scan over [P][C] of words
+    const unsigned long long* off_r;   // exclusive scan over [P][C] of records
+    uint32_t* records;
+    uint32_t* index;
+};
+
+struct Phase2Params {
+    const uint32_t* records;
+    const uint32_t* index;
+    const unsigned long long* off_w;   // [P][C] (bucket start = off_w[p*C])
+    const unsigned long long* off_r;
+    uint32_t n_cta1;                   // C of phase 1
+    uint32_t n_buckets;
+    const uint32_t* order;             // bucket processing order
+    int k;
+    uint32_t fine_bits;                // bits available for fine groups
+    uint32_t target;                   // k-mer instances per fine group
+    uint64_t ci, cx;
+    uint32_t* work;                    // [0] next bucket
+    uint32_t* scratch;                 // [n_cta2][scratch_cap]
+    uint64_t scratch_cap;
+    void* out_keys;                    // u64 x W per k-mer
+    uint32_t* out_counts;
+    unsigned long long* out_n;         // [0] out cursor, [1] distinct, [2] fallback groups
+    uint64_t out_cap;
+    uint32_t* fallback;                // [cap][3]: bucket, group, F
+    uint32_t fallback_cap;
+    const unsigned long long* bucket_kmers;  // per bucket k-mer instances
+    uint32_t smem_slots;               // table capacity in shared memory
+};
+
+// ---------------------------------------------------------------- bit helpers
+__device__ __forceinline__ uint64_t rol64(uint64_t x, int s) {
+    s &= 63;
+    return s ? (x << s) | (x >> (64 - s)) : x;
+}
+__device__ __forceinline__ uint64_t ror64(uint64_t x, int s) {
+    s &= 63;
+    return s ? (x >> s) | (x << (64 - s)) : x;
+}
+
+// 32 bases (64 bits, MSB-first) starting at array base index a.
+__device__ __forceinline__ uint64_t window64(const uint32_t* pk, uint64_t a) {
+    const uint64_t w = a >> 4;
+    const uint32_t o = (uint32_t)(a & 15);
+    const uint64_t hi = ((uint64_t)pk[w] << 32) | pk[w + 1];
+    if (o == 0) return hi;
+    return (hi << (2 * o)) | (pk[w + 2] >> (32 - 2 * o));
+}
+
+__device__ __forceinline__ uint32_t base_at(const uint32_t* pk, uint64_t a) {
+    return (pk[a >> 4] >> (30 - 2 * (uint32_t)(a & 15))) & 3u;
+}
+
+// 64 validity bits starting at array base index a (bit 0 = base a).
+__device__ __forceinline__ uint64_t valid64(const uint32_t* vb, uint64_t a) {
+    const uint64_t w = a >> 5;
+    const uint32_t o = (uint32_t)(a & 31);
+    const uint64_t lo = ((uint64_t)vb[w + 1] << 32) | vb[w];
+    if (o == 0) return lo;
+    return (lo >> o) | ((uint64_t)vb[w + 2] << (64 - o));
+}
+
+__device__ __forceinline__ bool valid_base(const uint32_t* vb, uint64_t a) {
+    return (vb[a >> 5] >> (a & 31)) & 1u;
+}
+
+// Canonical ntHash of the m-mer at array base index a, from scratch.
+__device__ __forceinline__ void nt_init(const HashTables& T, const uint32_t* pk, uint64_t a, int m,
+                                        uint64_t& fwd, uint64_t& rev) {
+    const uint64_t win = window64(pk, a);
+    uint64_t f = 0, r = 0;
+    const int ng = m >> 2;
+    for (int c = 0; c < ng; ++c) {
+        const uint32_t v = (uint32_t)(win >> (56 - 8 * c)) & 0xFFu;
+        f ^= rol64(T.GF[v], m - 4 - 4 * c);
+        r ^= rol64(T.GR[v], 4 * c);
+    }
+    for (int i = 4 * ng; i < m; ++i) {
+        const uint32_t b = (uint32_t)(win >> (62 - 2 * i)) & 3u;
+        f ^= rol64(T.FW[b], m - 1 - i);
+        r ^= rol64(T.RV[b], i);
+    }
+    fwd = f;
+    rev = r;
+}
+
+__device__ __forceinline__ void nt_roll(const HashTables& T, uint32_t out, uint32_t in,
+                                        uint64_t& fwd, uint64_t& rev) {
+    const uint32_t idx = (out << 2) | in;
+    fwd = rol64(fwd, 1) ^ T.CTF[idx];
+    rev = ror64(rev, 1) ^ T.CTR[idx];
+}
+
+// ---------------------------------------------------------------- k-mer keys
+// Reverse complement of a k-mer held in the low 2k bits (k <= 32).
+__device__ __forceinline__ uint64_t revcomp64(uint64_t x, int k) {
+    x = ~x;
+    // reverse the order of 2-bit groups
+    x = ((x >> 2) & 0x3333333333333333ull) | ((x & 0x3333333333333333ull) << 2);
+    x = ((x >> 4) & 0x0F0F0F0F0F0F0F0Full) | ((x & 0x0F0F0F0F0F0F0F0Full) << 4);
+    x = ((x >> 8) & 0x00FF00FF00FF00FFull) | ((x & 0x00FF00FF00FF00FFull) << 8);
+    x = ((x >> 16) & 0x0000FFFF0000FFFFull) | ((x & 0x0000FFFF0000FFFFull) << 16);
+    x = (x >> 32) | (x << 32);
+    return x >> (64 - 2 * k);
+}
+
+struct K2 {
+    uint64_t lo, hi;  // lo = last 32 bases, hi = the bases before them
+};
+
+__device__ __forceinline__ bool k2_less(const K2& a, const K2& b) {
+    return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo);
+}
+
+// Reverse complement of a k-mer of 33..64 bases stored as (hi, lo).
+__device__ __forceinline__ K2 revcomp128(const K2& x, int k) {
+    // full 128-bit reversal of 2-bit groups, then shift right by 128 - 2k
+    const uint64_t rlo = revcomp64(x.hi, 32);  // reversed hi becomes the low part
+    const uint64_t rhi = revcomp64(x.lo, 32);
+    const int sh = 128 - 2 * k;  // 2..64 for k in [32, 63]
+    K2 r;
+    if (sh >= 64) { r.lo = rhi >> (sh - 64); r.hi = 0; }
+    else { r.lo = (rlo >> sh) | (rhi << (64 - sh)); r.hi = rhi >> sh; }
+    return r;
+}
+
+__device__ __forceinline__ uint64_t mix_key1(uint64_t x) {
+    x ^= x >> 31;
+    x *= 0x9E3779B97F4A7C15ull;
+    x ^= x >> 29;
+    return x;
+}
+__device__ __forceinline__ uint64_t mix_key2(const K2& k) {
+    return mix_key1(k.lo ^ mix_key1(k.hi + 0x632BE59BD9B4E019ull));
+}
+
+}  // namespace tg

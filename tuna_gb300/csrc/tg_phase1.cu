@@ -1,0 +1,606 @@
+// tg_phase1.cu — Phase 1 on the GPU: 2-bit packing, superkmer cutting and the
+// scatter of superkmer records into HBM buckets.
+//
+// Reference behaviour (paths relative to the reference project root):
+//   ASCII -> kache 2-bit          src/partition_hash.hpp:68-70
+//   canonical ntHash per m-mer    include/nt_hash.hpp:74-124
+//   minimizer of each k-mer       include/minimizer_window.hpp (value = min over
+//                                 the k-m+1 m-mer hashes of the k-mer)
+//   superkmer boundaries          src/partition_hash.hpp:78-93: a new record at
+//                                 a minimizer change, or when the record would
+//                                 exceed hdr_t::max bases
+//   partition of a record         src/partition_hash.hpp:550-552 (hash & (n-1))
+//
+// The reference walks each run sequentially. Here every k-mer start position
+// is decided independently: a k-mer starts a "chain" when it is the first
+// k-mer of its run or its minimizer differs from the previous k-mer's; inside
+// a chain a forced split falls every L = hdr_max + 1 - k k-mers after the
+// chain start (the cap of partition_hash.hpp:81 replayed from the chain
+// start); a record ends at the next cut or at the end of the run.
+#include "tg_internal.cuh"
+
+namespace tg {
+
+// ---------------------------------------------------------------- packing
+// One thread per packed word (16 bases). Array base index a = global base + TG_PAD.
+__global__ void k_pack(const uint8_t* __restrict__ seq, uint64_t n, uint32_t* __restrict__ packed,
+                       uint32_t* __restrict__ valid, uint64_t n_words,
+                       unsigned long long* __restrict__ n_bases) {
+    const uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t code = 0, vbits = 0;
+    if (w < n_words) {
+        const int64_t g0 = (int64_t)(w * 16) - TG_PAD;
+        uint8_t b[16];
+        if (g0 >= 0 && (uint64_t)g0 + 16 <= n && ((reinterpret_cast<uintptr_t>(seq + g0) & 15) == 0)) {
+            const uint4 v = *reinterpret_cast<const uint4*>(seq + g0);
+            const uint32_t vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int i = 0; i < 16; ++i) b[i] = (uint8_t)(vv[i >> 2] >> (8 * (i & 3)));
+        } else {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                const int64_t g = g0 + i;
+                b[i] = (g >= 0 && (uint64_t)g < n) ? seq[g] : 0;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const uint32_t c = b[i];
+            // ACGTacgt test of include/helicase_cpp/simd.hpp:316: (c & 0xDF) == "A_C_T_G_"[c & 6]
+            const uint32_t want = (uint32_t)(0x0047005400430041ull >> (8 * (c & 6))) & 0xFFu;
+            const bool ok = (c & 0xDFu) == want;
+            const uint32_t kc = ok ? (((c >> 2) ^ (c >> 1)) & 3u) : 0u;
+            code |= kc << (30 - 2 * i);
+            vbits |= (ok ? 1u : 0u) << i;
+        }
+        packed[w] = code;
+    }
+    // two consecutive words form one 32-bit validity word (lane pairs)
+    const uint32_t other = __shfl_down_sync(0xffffffffu, vbits, 1);
+    if (w < n_words && (w & 1) == 0) valid[w >> 1] = vbits | (other << 16);
+    // count of ACGT bases
+    unsigned cnt = __popc(vbits);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(n_bases, (unsigned long long)cnt);
+}
+
+// ---------------------------------------------------------------- block scans
+template <int NT>
+struct BlockScan {
+    // exclusive prefix sum of v over the block; returns it and the block total
+    __device__ static uint32_t excl_sum(uint32_t v, uint32_t* s_warp, uint32_t& total) {
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        uint32_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_warp[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            uint32_t t = lane < NT / 32 ? s_warp[lane] : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+                if (lane >= o) t += y;
+            }
+            if (lane < NT / 32) s_warp[lane] = t;
+        }
+        __syncthreads();
+        total = s_warp[NT / 32 - 1];
+        const uint32_t before = wid ? s_warp[wid - 1] : 0;
+        __syncthreads();
+        return before + x - v;
+    }
+    // exclusive prefix max of v (int64, -1 = none)
+    __device__ static int64_t excl_max(int64_t v, int64_t* s_warp) {
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        int64_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x = max(x, y);
+        }
+        int64_t ex = __shfl_up_sync(0xffffffffu, x, 1);
+        if (lane == 0) ex = -1;
+        if (lane == 31) s_warp[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            int64_t t = lane < NT / 32 ? s_warp[lane] : -1;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int64_t y = __shfl_up_sync(0xffffffffu, t, o);
+                if (lane >= o) t = max(t, y);
+            }
+            if (lane < NT / 32) s_warp[lane] = t;
+        }
+        __syncthreads();
+        const int64_t before = wid ? s_warp[wid - 1] : -1;
+        __syncthreads();
+        return max(before, ex);
+    }
+};
+
+// Shared-memory layout of k_cut, sized at launch from w and the bucket count.
+struct CutSmem {
+    size_t tables, hist_w, hist_r, hist_k, h, a, b, ev, evm, pk, vb, scan, total;
+    int hn;
+    __host__ __device__ static size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+    __host__ __device__ void layout(int w, uint32_t p1, bool exp) {
+        hn = CUT_TILE + w + 2;
+        size_t o = 0;
+        tables = o; o = align16(o + sizeof(HashTables));
+        hist_w = o; o = align16(o + 4 * (size_t)p1);
+        hist_r = o; o = align16(o + 4 * (size_t)p1);
+        hist_k = o; o = align16(o + 4 * (size_t)p1);
+        h = o; o = align16(o + 8 * (size_t)hn);
+        a = o; o = align16(o + 8 * (size_t)hn);
+        b = o; o = align16(o + 8 * (size_t)hn);
+        ev = o; o = align16(o + 8 * (size_t)(CUT_TILE + 1));
+        evm = o; o = align16(o + (exp ? 16 * (size_t)(CUT_TILE + 1) : 0));
+        pk = o; o = align16(o + 4 * (size_t)(CUT_TILE + 2 * MAX_W + 320) / 16 + 64);
+        vb = o; o = align16(o + 4 * (size_t)(CUT_TILE + 2 * MAX_W + 320) / 32 + 64);
+        scan = o; o = align16(o + 8 * 64);
+        total = o;
+    }
+};
+
+// Exact min_pos of the reference's two-stack window (minimizer_window.hpp:
+// 192-225, 317-325) for the k-mer whose m-mers are hashes hw[0..w]; q_off =
+// (position of its last m-mer - run start) mod (w+1). Blocks of w+1 m-mers
+// are aligned to the run start; the older block's minimum keeps its rightmost
+// position on ties, the newer block's its leftmost, and a tie between the two
+// goes to the newer block. When the k-mer's window is exactly one block
+// (q_off == w) the rightmost minimum wins.
+__device__ int ref_min_pos(const uint64_t* hw, int w, int q_off) {
+    if (q_off == w) {
+        uint64_t best = hw[0];
+        int bp = 0;
+        for (int j = 1; j <= w; ++j)
+            if (hw[j] <= best) { best = hw[j]; bp = j; }
+        return bp;
+    }
+    const int b0 = w - q_off;  // first index of the newer block
+    uint64_t mo = ~0ull;
+    int po = -1;
+    for (int j = 0; j < b0; ++j)
+        if (hw[j] <= mo) { mo = hw[j]; po = j; }
+    uint64_t mn = hw[b0];
+    int pn = b0;
+    for (int j = b0 + 1; j <= w; ++j)
+        if (hw[j] < mn) { mn = hw[j]; pn = j; }
+    return (po >= 0 && mo < mn) ? po : pn;
+}
+
+// ---------------------------------------------------------------- superkmer cut
+// One CTA per chunk of CTA-chunk k-mer start positions, walked in tiles of
+// CUT_TILE. A CTA owns the chains that start inside its chunk and follows
+// them past the chunk end until they close.
+template <bool EXPORT>
+__global__ void __launch_bounds__(CUT_THREADS, 2)
+k_cut(CutParams P, const HashTables* __restrict__ gT) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    CutSmem L;
+    L.layout(P.w, 1u << P.p1_bits, EXPORT);
+    HashTables& T = *reinterpret_cast<HashTables*>(smem + L.tables);
+    uint32_t* s_hw = reinterpret_cast<uint32_t*>(smem + L.hist_w);
+    uint32_t* s_hr = reinterpret_cast<uint32_t*>(smem + L.hist_r);
+    uint32_t* s_hk = reinterpret_cast<uint32_t*>(smem + L.hist_k);
+    uint64_t* s_h = reinterpret_cast<uint64_t*>(smem + L.h);
+    uint64_t* s_a = reinterpret_cast<uint64_t*>(smem + L.a);
+    uint64_t* s_b = reinterpret_cast<uint64_t*>(smem + L.b);
+    uint2* s_ev = reinterpret_cast<uint2*>(smem + L.ev);
+    uint64_t* s_evm = reinterpret_cast<uint64_t*>(smem + L.evm);  // EXPORT: hash, min_pos
+    uint32_t* s_pk = reinterpret_cast<uint32_t*>(smem + L.pk);
+    uint32_t* s_vb = reinterpret_cast<uint32_t*>(smem + L.vb);
+    int64_t* s_scan64 = reinterpret_cast<int64_t*>(smem + L.scan);
+    uint32_t* s_scan32 = reinterpret_cast<uint32_t*>(smem + L.scan + 8 * 32);
+    __shared__ int64_t s_cs_carry;       // last chain start before the tile (-1: none)
+    __shared__ int64_t s_open;           // start of the open owned record (-1: none)
+    __shared__ uint32_t s_open_mlo;
+    __shared__ uint64_t s_open_hash;
+    __shared__ uint32_t s_open_mp;
+    __shared__ uint32_t s_ndesc;
+    __shared__ uint32_t s_nev;
+
+    const int tid = threadIdx.x;
+    const uint32_t p1 = 1u << P.p1_bits;
+    const int k = P.k, m = P.m, w = P.w;
+    const uint32_t c = blockIdx.x;
+    {
+        const uint64_t* src = reinterpret_cast<const uint64_t*>(gT);
+        uint64_t* dst = reinterpret_cast<uint64_t*>(&T);
+        for (int i = tid; i < (int)(sizeof(HashTables) / 8); i += CUT_THREADS) dst[i] = src[i];
+        for (uint32_t i = tid; i < p1; i += CUT_THREADS) { s_hw[i] = 0; s_hr[i] = 0; s_hk[i] = 0; }
+        if (tid == 0) { s_cs_carry = -1; s_open = -1; s_ndesc = 0; }
+    }
+    __syncthreads();
+
+    const uint64_t cstart = (uint64_t)c * P.chunk;
+    const uint64_t cend = min(cstart + P.chunk, P.n);
+    const int hn = L.hn;
+    int plog = 0;
+    while ((2 << plog) <= w + 1) ++plog;  // 2^plog <= w+1 < 2^(plog+1)
+    const int pw = 1 << plog;
+    uint64_t kmask_valid = (k >= 64) ? ~0ull : ((1ull << k) - 1);
+    unsigned long long loc_kmers = 0, loc_recs = 0, loc_runs = 0;
+    bool overflowed = false;
+
+    for (uint64_t t0 = cstart; t0 < P.n; t0 += CUT_TILE) {
+        if (t0 >= cend && s_open < 0) break;  // nothing of ours is still open
+        // ---- stage packed and validity words: array bases [A0, A0 + NB)
+        const uint64_t A0 = (t0 + TG_PAD - 1) & ~uint64_t(31);
+        const int npk = (CUT_TILE + 2 * MAX_W + 320) / 16;
+        for (int i = tid; i < npk; i += CUT_THREADS) s_pk[i] = P.packed[(A0 >> 4) + i];
+        for (int i = tid; i < npk / 2; i += CUT_THREADS) s_vb[i] = P.valid[(A0 >> 5) + i];
+        __syncthreads();
+        // relative array index of global position g: g + TG_PAD - A0
+        const uint64_t rel0 = TG_PAD - A0;  // add to g (mod 2^64)
+
+        // ---- 1. canonical ntHash of m-mers q in [t0-1, t0+T+w]: index i = q - (t0-1)
+        {
+            constexpr int SEG = 8;
+            for (int s0 = tid * SEG; s0 < hn; s0 += CUT_THREADS * SEG) {
+                const uint64_t a = (t0 - 1) + (uint64_t)s0 + rel0;  // relative array index
+                uint64_t f, r;
+                nt_init(T, s_pk, a, m, f, r);
+                s_h[s0] = f ^ r;
+                const int e = min(SEG, hn - s0);
+                for (int j = 1; j < e; ++j) {
+                    const uint32_t out = base_at(s_pk, a + j - 1);
+                    const uint32_t in = base_at(s_pk, a + j - 1 + m);
+                    nt_roll(T, out, in, f, r);
+                    s_h[s0 + j] = f ^ r;
+                }
+            }
+        }
+        __syncthreads();
+
+        // ---- 2. minimizer of k-mers s in [t0-1, t0+T): M[i] = min h[i .. i+w]
+        const uint64_t* Mv;
+        {
+            const uint64_t* src = s_h;
+            uint64_t* bufs[2] = {s_a, s_b};
+            for (int j = 1; j <= plog; ++j) {
+                const int half = 1 << (j - 1);
+                const int cnt = hn - ((1 << j) - 1);
+                uint64_t* dst = bufs[(j - 1) & 1];
+                for (int i = tid; i < cnt; i += CUT_THREADS) dst[i] = min(src[i], src[i + half]);
+                __syncthreads();
+                src = dst;
+            }
+            uint64_t* mdst = (src == s_a) ? s_b : s_a;
+            const int off = w + 1 - pw;
+            for (int i = tid; i <= CUT_TILE; i += CUT_THREADS) mdst[i] = min(src[i], src[i + off]);
+            __syncthreads();
+            Mv = mdst;
+        }
+
+        // ---- 3. flags of this thread's PT positions
+        constexpr int PT = CUT_TILE / CUT_THREADS;
+        bool vk[PT + 1];
+        bool csf[PT], rs[PT], ev[PT];
+        const uint64_t sbase = t0 + (uint64_t)tid * PT;
+#pragma unroll
+        for (int i = 0; i <= PT; ++i) {
+            const uint64_t s = sbase + i - 1;  // i = 0 is the position before
+            const uint64_t a = s + rel0;
+            const uint64_t bits = valid64(s_vb, a);
+            vk[i] = (s + 1 > 0) && s < P.n && ((~bits & kmask_valid) == 0);
+            if (s == ~0ull) vk[i] = false;
+        }
+        int64_t last_cs = -1;
+#pragma unroll
+        for (int i = 0; i < PT; ++i) {
+            const uint64_t s = sbase + i;
+            const bool v = vk[i + 1];
+            const bool prev_base = valid_base(s_vb, s - 1 + rel0);
+            const bool first = v && !prev_base;
+            const int mi = (int)(s - (t0 - 1));
+            const bool hc = v && !first && Mv[mi] != Mv[mi - 1];
+            csf[i] = first || hc;
+            rs[i] = !v && vk[i];  // first invalid k-mer after a run: run end
+            if (csf[i]) last_cs = (int64_t)s;
+            if (first) ++loc_runs;
+        }
+        // chain start in force at each position: scan max across the tile
+        int64_t before = BlockScan<CUT_THREADS>::excl_max(last_cs, s_scan64);
+        before = max(before, s_cs_carry);
+        uint32_t nev_local = 0;
+        uint32_t owned_mask = 0;
+        int64_t cs = before;
+#pragma unroll
+        for (int i = 0; i < PT; ++i) {
+            const uint64_t s = sbase + i;
+            const bool v = vk[i + 1];
+            if (csf[i]) cs = (int64_t)s;
+            bool forced = false;
+            if (v && !csf[i] && cs >= 0) {
+                const uint64_t d = s - (uint64_t)cs;
+                forced = (d >= P.L) && (d % P.L == 0);
+            }
+            const bool cut = v && (csf[i] || forced);
+            const bool owned = cut && cs >= (int64_t)cstart && cs < (int64_t)cend;
+            ev[i] = cut || rs[i];
+            if (owned) owned_mask |= 1u << i;
+            nev_local += ev[i] ? 1u : 0u;
+        }
+        uint32_t nev_total;
+        uint32_t ev_off = BlockScan<CUT_THREADS>::excl_sum(nev_local, s_scan32, nev_total);
+        // ---- 4. event list (position order)
+#pragma unroll
+        for (int i = 0; i < PT; ++i) {
+            if (!ev[i]) continue;
+            const uint64_t s = sbase + i;
+            const int mi = (int)(s - (t0 - 1));
+            const bool own = (owned_mask >> i) & 1u;
+            const uint64_t mval = Mv[mi];
+            s_ev[ev_off] = make_uint2(((uint32_t)(s - t0) << 2) | (own ? EV_OWNED : 0u) | EV_CUT,
+                                      (uint32_t)(mval & 0xFFFFFFu));
+            if (EXPORT) {
+                int mp = 0;
+                if (own) {
+                    // run start: scan validity bits backwards (export only)
+                    uint64_t rsx = s;
+                    while (rsx > 0 && valid_base(P.valid, rsx - 1 + TG_PAD)) {
+                        const uint64_t aa = rsx - 1 + TG_PAD;
+                        const uint32_t word = P.valid[aa >> 5];
+                        const uint32_t bit = (uint32_t)(aa & 31);
+                        const uint32_t below = (bit == 31) ? word : (word & ((2u << bit) - 1));
+                        if (below == ((bit == 31) ? 0xFFFFFFFFu : ((2u << bit) - 1))) {
+                            rsx -= bit + 1;  // whole word prefix valid
+                        } else {
+                            --rsx;
+                        }
+                    }
+                    const int q_off = (int)((s + w - rsx) % (uint64_t)(w + 1));
+                    mp = ref_min_pos(&s_h[mi], w, q_off);
+                }
+                s_evm[2 * ev_off] = mval;
+                s_evm[2 * ev_off + 1] = (uint64_t)mp;
+            }
+            ++ev_off;
+        }
+        if (tid == 0) s_nev = nev_total;
+        __syncthreads();
+        // ---- 5. close records: event e closes the record opened at event e-1
+        const uint32_t nev = s_nev;
+        for (uint32_t base = 0; base < (nev + CUT_THREADS - 1) / CUT_THREADS * CUT_THREADS; base += CUT_THREADS) {
+            const uint32_t e = base + tid;
+            bool emit = false;
+            uint64_t st = 0, mh = 0;
+            uint32_t mlo = 0, nk = 0, mp = 0;
+            if (e < nev) {
+                const uint64_t pos = t0 + (s_ev[e].x >> 2);
+                if (e == 0) {
+                    if (s_open >= 0) {
+                        emit = true;
+                        st = (uint64_t)s_open;
+                        mlo = s_open_mlo;
+                        if (EXPORT) { mh = s_open_hash; mp = s_open_mp; }
+                    }
+                } else if (s_ev[e - 1].x & EV_OWNED) {
+                    emit = true;
+                    st = t0 + (s_ev[e - 1].x >> 2);
+                    mlo = s_ev[e - 1].y;
+                    if (EXPORT) { mh = s_evm[2 * (e - 1)]; mp = (uint32_t)s_evm[2 * (e - 1) + 1]; }
+                }
+                nk = (uint32_t)(pos - st);
+            }
+            uint32_t ntot;
+            const uint32_t di = BlockScan<CUT_THREADS>::excl_sum(emit ? 1u : 0u, s_scan32, ntot);
+            if (emit) {
+                const uint32_t idx = s_ndesc + di;
+                if (idx < P.desc_cap) {
+                    P.desc[(uint64_t)c * P.desc_cap + idx] =
+                        (uint64_t)(uint32_t)(st - cstart) | ((uint64_t)nk << 32) | ((uint64_t)mlo << 40);
+                    if (EXPORT) {
+                        uint64_t* x = P.xdesc + ((uint64_t)c * P.desc_cap + idx) * 3;
+                        x[0] = st;
+                        x[1] = mh;
+                        x[2] = ((uint64_t)mp << 32) | nk;
+                    }
+                } else {
+                    overflowed = true;
+                }
+                const uint32_t b = mlo & (p1 - 1);
+                atomicAdd(&s_hw[b], 1u + (nk + (uint32_t)k - 1 + 15) / 16);
+                atomicAdd(&s_hr[b], 1u);
+                atomicAdd(&s_hk[b], nk);
+                loc_kmers += nk;
+                loc_recs += 1;
+            }
+            __syncthreads();
+            if (tid == 0) s_ndesc += ntot;
+            __syncthreads();
+        }
+        // ---- 6. carries to the next tile
+        if (tid == 0) {
+            if (nev > 0) {
+                const uint2 le = s_ev[nev - 1];
+                if (le.x & EV_OWNED) {
+                    s_open = (int64_t)(t0 + (le.x >> 2));
+                    s_open_mlo = le.y;
+                    if (EXPORT) { s_open_hash = s_evm[2 * (nev - 1)]; s_open_mp = (uint32_t)s_evm[2 * (nev - 1) + 1]; }
+                } else {
+                    s_open = -1;
+                }
+            }
+        }
+        // the tile's last chain start (thread with the highest position wins)
+        if (tid == CUT_THREADS - 1) s_cs_carry = max(s_cs_carry, cs);
+        __syncthreads();
+    }
+    // ---- flush histograms and counters
+    for (uint32_t i = tid; i < p1; i += CUT_THREADS) {
+        P.hist[(uint64_t)i * P.n_cta + c] = s_hw[i];
+        P.hist[(uint64_t)p1 * P.n_cta + (uint64_t)i * P.n_cta + c] = s_hr[i];
+        if (s_hk[i]) atomicAdd(reinterpret_cast<unsigned long long*>(P.hist + 2ull * p1 * P.n_cta) + i,
+                               (unsigned long long)s_hk[i]);
+    }
+    if (tid == 0) P.n_desc[c] = s_ndesc;
+    if (overflowed) atomicExch(P.overflow, 1u);
+    // block-reduce the counters
+    for (int o = 16; o > 0; o >>= 1) {
+        loc_kmers += __shfl_down_sync(0xffffffffu, loc_kmers, o);
+        loc_recs += __shfl_down_sync(0xffffffffu, loc_recs, o);
+        loc_runs += __shfl_down_sync(0xffffffffu, loc_runs, o);
+    }
+    if ((tid & 31) == 0) {
+        if (loc_kmers) atomicAdd(&P.stats[0], loc_kmers);
+        if (loc_recs) atomicAdd(&P.stats[1], loc_recs);
+        if (loc_runs) atomicAdd(&P.stats[2], loc_runs);
+    }
+}
+
+// ---------------------------------------------------------------- offsets
+// Exclusive scan of two u32 arrays of length n into u64 outputs, one CTA per
+// SCAN_ITEMS items, then a fix-up with the scanned block sums.
+constexpr int SCAN_T = 1024, SCAN_ITEMS = 8192;
+
+__global__ void k_scan_blocks(const uint32_t* __restrict__ in, uint64_t n, unsigned long long* __restrict__ out,
+                              unsigned long long* __restrict__ block_sums) {
+    __shared__ unsigned long long s[SCAN_T];
+    const uint64_t b0 = (uint64_t)blockIdx.x * SCAN_ITEMS;
+    constexpr int PER = SCAN_ITEMS / SCAN_T;
+    unsigned long long v[PER], acc = 0;
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const uint64_t idx = b0 + (uint64_t)threadIdx.x * PER + i;
+        v[i] = idx < n ? in[idx] : 0;
+        acc += v[i];
+    }
+    s[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = 1; o < SCAN_T; o <<= 1) {
+        const unsigned long long y = threadIdx.x >= o ? s[threadIdx.x - o] : 0;
+        __syncthreads();
+        s[threadIdx.x] += y;
+        __syncthreads();
+    }
+    unsigned long long run = s[threadIdx.x] - acc;
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const uint64_t idx = b0 + (uint64_t)threadIdx.x * PER + i;
+        if (idx < n) out[idx] = run;
+        run += v[i];
+    }
+    if (threadIdx.x == SCAN_T - 1) block_sums[blockIdx.x] = s[SCAN_T - 1];
+}
+
+__global__ void k_scan_sums(unsigned long long* __restrict__ sums, uint32_t nb, unsigned long long* __restrict__ total) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        unsigned long long acc = 0;
+        for (uint32_t i = 0; i < nb; ++i) {
+            const unsigned long long v = sums[i];
+            sums[i] = acc;
+            acc += v;
+        }
+        *total = acc;
+    }
+}
+
+__global__ void k_scan_add(unsigned long long* __restrict__ out, uint64_t n, const unsigned long long* __restrict__ sums) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] += sums[i / SCAN_ITEMS];
+}
+
+// ---------------------------------------------------------------- scatter
+// One CTA per Phase-1 chunk: its descriptors become bucket records
+// [hdr = nk | fine << 8][packed words], and their offsets go to the index.
+constexpr int SCAT_THREADS = 256;
+
+__global__ void __launch_bounds__(SCAT_THREADS)
+k_scatter(ScatterParams P) {
+    extern __shared__ __align__(16) uint32_t cur[];  // [2][p1]
+    const uint32_t p1 = 1u << P.p1_bits;
+    uint32_t* cw = cur;
+    uint32_t* cr = cur + p1;
+    for (uint32_t i = threadIdx.x; i < p1; i += SCAT_THREADS) { cw[i] = 0; cr[i] = 0; }
+    __syncthreads();
+    const uint32_t c = blockIdx.x;
+    const uint32_t nd = min((uint64_t)P.n_desc[c], P.desc_cap);
+    const uint64_t cstart = (uint64_t)c * P.chunk;
+    const int k = P.k;
+    for (uint32_t i = threadIdx.x; i < nd; i += SCAT_THREADS) {
+        const uint64_t d = P.desc[(uint64_t)c * P.desc_cap + i];
+        const uint64_t st = cstart + (uint32_t)d;
+        const uint32_t nk = (uint32_t)(d >> 32) & 0xFFu;
+        const uint32_t mlo = (uint32_t)(d >> 40);
+        const uint32_t b = mlo & (p1 - 1);
+        const uint32_t fine = mlo >> P.p1_bits;
+        const uint32_t len = nk + (uint32_t)k - 1;
+        const uint32_t nw = (len + 15) / 16;
+        const uint32_t wo = atomicAdd(&cw[b], 1u + nw);
+        const uint32_t ro = atomicAdd(&cr[b], 1u);
+        const uint64_t bucket0 = P.off_w[(uint64_t)b * P.n_cta];
+        const uint64_t wabs = P.off_w[(uint64_t)b * P.n_cta + c] + wo;
+        const uint64_t rabs = P.off_r[(uint64_t)b * P.n_cta + c] + ro;
+        uint32_t* rec = P.records + wabs;
+        rec[0] = nk | (fine << 8);
+        const uint64_t a = st + TG_PAD;
+        const uint64_t w0 = a >> 4;
+        const uint32_t o = (uint32_t)(a & 15);
+        for (uint32_t j = 0; j < nw; ++j) {
+            uint32_t v = P.packed[w0 + j];
+            if (o) v = (v << (2 * o)) | (P.packed[w0 + j + 1] >> (32 - 2 * o));
+            const uint32_t left = len - 16 * j;  // bases of this word still in the record
+            if (left < 16) v &= ~0u << (32 - 2 * left);
+            rec[1 + j] = v;
+        }
+        P.index[rabs] = (uint32_t)(wabs - bucket0);
+    }
+}
+
+// ---------------------------------------------------------------- launchers
+size_t cut_smem_bytes(int w, uint32_t p1, bool exp) {
+    CutSmem L;
+    L.layout(w, p1, exp);
+    return L.total;
+}
+
+cudaError_t launch_pack(const uint8_t* seq, uint64_t n, uint32_t* packed, uint32_t* valid, uint64_t n_words,
+                        unsigned long long* n_bases, cudaStream_t st) {
+    const uint64_t nw = (n_words + 1) & ~uint64_t(1);  // even: lane pairs share a validity word
+    const uint32_t threads = 256;
+    const uint64_t blocks = (nw + threads - 1) / threads;
+    k_pack<<<(unsigned)blocks, threads, 0, st>>>(seq, n, packed, valid, nw, n_bases);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cut(const CutParams& P, const HashTables* gT, bool exp, cudaStream_t st) {
+    const size_t sm = cut_smem_bytes(P.w, 1u << P.p1_bits, exp);
+    cudaError_t e;
+    if (exp) {
+        e = cudaFuncSetAttribute(k_cut<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        k_cut<true><<<P.n_cta, CUT_THREADS, sm, st>>>(P, gT);
+    } else {
+        e = cudaFuncSetAttribute(k_cut<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        k_cut<false><<<P.n_cta, CUT_THREADS, sm, st>>>(P, gT);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scan(const uint32_t* in, uint64_t n, unsigned long long* out, unsigned long long* sums,
+                        unsigned long long* total, cudaStream_t st, int* launches) {
+    const uint32_t nb = (uint32_t)((n + SCAN_ITEMS - 1) / SCAN_ITEMS);
+    k_scan_blocks<<<nb, SCAN_T, 0, st>>>(in, n, out, sums);
+    k_scan_sums<<<1, 32, 0, st>>>(sums, nb, total);
+    k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, n, sums);
+    *launches += 3;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter(const ScatterParams& P, cudaStream_t st) {
+    const size_t sm = 2 * 4 * (size_t)(1u << P.p1_bits);
+    cudaError_t e = cudaFuncSetAttribute(k_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    k_scatter<<<P.n_cta, SCAT_THREADS, sm, st>>>(P);
+    return cudaGetLastError();
+}
+
+}  // namespace tg
