@@ -118,6 +118,9 @@ typedef int (*tg_sink_fn)(const void* data, size_t bytes, uint64_t n_kmers, void
 tg_status tg_ctx_create(const tg_ctx_opts* opts, tg_ctx** out);
 tg_status tg_ctx_destroy(tg_ctx* ctx);
 const char* tg_last_error(const tg_ctx* ctx);
+/* The cudaStream_t (as void*) on which the context launches all its work, so a
+ * caller can order its own work and time with CUDA events on the same stream. */
+void* tg_ctx_stream(const tg_ctx* ctx);
 /* Library version string and whether a CUDA device is usable. */
 const char* tg_version(void);
 int tg_device_count(void);

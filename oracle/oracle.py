@@ -51,7 +51,7 @@ def lib():
         L.tor_parse_fastx.restype = i32
         L.tor_nthash_canonical.argtypes = [vp, i32]
         L.tor_nthash_canonical.restype = u64
-        for fn in (L.tor_count_stream, L.tor_count_fastx):
+        for fn in (L.tor_count_stream, L.tor_count_fastx, L.tor_count_stream_unsorted):
             fn.argtypes = [vp, ctypes.c_size_t, i32, i32, u64, u64, u64, i32, ctypes.POINTER(_Stats)]
             fn.restype = vp
         L.tor_result_words.argtypes = [vp]
@@ -151,6 +151,16 @@ def count_stream(seq, k: int, m: int, n_parts: int = 16, ci: int = 1,
     st = _Stats()
     p = lib().tor_count_stream(buf.ctypes.data if buf.size else None, buf.size, k, m,
                                n_parts, ci, cx, threads, ctypes.byref(st))
+    return _take(p, k, st)
+
+
+def count_stream_unsorted(seq, k: int, m: int, n_parts: int = 16, ci: int = 1,
+                          cx: int = (1 << 64) - 1, threads: int = 1) -> Result:
+    """count_stream without the final sort (what the CPU baseline times)."""
+    buf = _as_u8(seq)
+    st = _Stats()
+    p = lib().tor_count_stream_unsorted(buf.ctypes.data if buf.size else None, buf.size, k, m,
+                                        n_parts, ci, cx, threads, ctypes.byref(st))
     return _take(p, k, st)
 
 

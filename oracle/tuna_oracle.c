@@ -719,9 +719,25 @@ static void free_phase1(p1_job* jobs, int threads, uint64_t n_parts) {
     free(jobs);
 }
 
+static tor_result* count_stream_impl(const uint8_t* seq, size_t len, int k, int m,
+                                     uint64_t n_parts, uint64_t ci, uint64_t cx,
+                                     int threads, tor_stats* st, int sort_output);
+
 tor_result* tor_count_stream(const uint8_t* seq, size_t len, int k, int m,
                              uint64_t n_parts, uint64_t ci, uint64_t cx,
                              int threads, tor_stats* st) {
+    return count_stream_impl(seq, len, k, m, n_parts, ci, cx, threads, st, 1);
+}
+
+tor_result* tor_count_stream_unsorted(const uint8_t* seq, size_t len, int k, int m,
+                                      uint64_t n_parts, uint64_t ci, uint64_t cx,
+                                      int threads, tor_stats* st) {
+    return count_stream_impl(seq, len, k, m, n_parts, ci, cx, threads, st, 0);
+}
+
+static tor_result* count_stream_impl(const uint8_t* seq, size_t len, int k, int m,
+                                     uint64_t n_parts, uint64_t ci, uint64_t cx,
+                                     int threads, tor_stats* st, int sort_output) {
     if (k < 2 || k > 256 || m < 1 || m > 32 || m >= k) return NULL;
     if (n_parts == 0 || (n_parts & (n_parts - 1))) return NULL;
     threads = clamp_threads(threads);
@@ -765,7 +781,7 @@ tor_result* tor_count_stream(const uint8_t* seq, size_t len, int k, int m,
         st->n_out = n_out;
     }
     free_phase1(jobs, threads, n_parts);
-    sort_result(r);
+    if (sort_output) sort_result(r);
     return r;
 }
 

@@ -63,6 +63,11 @@ typedef struct tor_result tor_result;
 tor_result* tor_count_stream(const uint8_t* seq, size_t len, int k, int m,
                              uint64_t n_parts, uint64_t ci, uint64_t cx,
                              int threads, tor_stats* st);
+/* Same without the final sort (the reference's own output is unsorted); the
+ * CPU baseline times this one. */
+tor_result* tor_count_stream_unsorted(const uint8_t* seq, size_t len, int k, int m,
+                                      uint64_t n_parts, uint64_t ci, uint64_t cx,
+                                      int threads, tor_stats* st);
 /* Same, but parses FASTA/FASTQ bytes first (helicase semantics). */
 tor_result* tor_count_fastx(const uint8_t* data, size_t len, int k, int m,
                             uint64_t n_parts, uint64_t ci, uint64_t cx,

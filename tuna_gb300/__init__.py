@@ -70,7 +70,7 @@ _SINK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.
 _lib = None
 
 # Every symbol of include/tuna_gpu.h; tests check the library exports them all.
-ABI_SYMBOLS = ["tg_ctx_create", "tg_ctx_destroy", "tg_last_error", "tg_version", "tg_device_count",
+ABI_SYMBOLS = ["tg_ctx_create", "tg_ctx_destroy", "tg_last_error", "tg_ctx_stream", "tg_version", "tg_device_count",
                "tg_job_begin", "tg_job_feed_seq", "tg_job_feed_seq_device", "tg_job_feed_fastx",
                "tg_job_feed_file", "tg_job_run", "tg_job_stats", "tg_job_result_size", "tg_job_key_words",
                "tg_job_result_copy", "tg_job_drain", "tg_job_write", "tg_job_export_partitions", "tg_job_end",
@@ -93,6 +93,8 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
     L.tg_ctx_destroy.argtypes = [vp]
     L.tg_last_error.argtypes = [vp]
     L.tg_last_error.restype = ctypes.c_char_p
+    L.tg_ctx_stream.argtypes = [vp]
+    L.tg_ctx_stream.restype = vp
     L.tg_version.restype = ctypes.c_char_p
     L.tg_device_count.restype = i32
     L.tg_job_begin.argtypes = [vp, ctypes.POINTER(_JobOpts), ctypes.POINTER(vp)]
@@ -202,6 +204,11 @@ class Context:
 
     def __exit__(self, *a):
         self.close()
+
+    @property
+    def stream_ptr(self) -> int:
+        """cudaStream_t of this context (all library work runs on it)."""
+        return int(self._L.tg_ctx_stream(self.h) or 0)
 
     def check(self, rc: int) -> None:
         if rc != 0:

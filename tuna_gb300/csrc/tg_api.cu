@@ -237,6 +237,8 @@ tg_status tg_ctx_destroy(tg_ctx* ctx) {
 
 const char* tg_last_error(const tg_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
+void* tg_ctx_stream(const tg_ctx* ctx) { return ctx ? (void*)ctx->st : nullptr; }
+
 tg_status tg_job_begin(tg_ctx* ctx, const tg_job_opts* opts, tg_job** out) {
     if (!ctx || !opts || !out) return TG_ERR_ARG;
     *out = nullptr;
