@@ -23,34 +23,10 @@
 
 #include "host/tg_host.h"
 #include "tg_internal.cuh"
+#include "tg_launch.h"
 #include "tuna_gpu.h"
 
 namespace tg {
-size_t cut_smem_bytes(int w, uint32_t p1, bool exp);
-cudaError_t launch_pack(const uint8_t* seq, uint64_t n, uint32_t* packed, uint32_t* valid, uint64_t n_words,
-                        unsigned long long* n_bases, cudaStream_t st);
-cudaError_t launch_cut(const CutParams& P, const HashTables* gT, bool exp, cudaStream_t st);
-cudaError_t launch_scan(const uint32_t* in, uint64_t n, unsigned long long* out, unsigned long long* sums,
-                        unsigned long long* total, cudaStream_t st, int* launches);
-cudaError_t launch_scatter(const ScatterParams& P, cudaStream_t st);
-size_t count_smem_bytes(int W, uint32_t slots);
-size_t key_bytes(int W);
-cudaError_t launch_count(int W, const Phase2Params& P, uint32_t grid, cudaStream_t st);
-struct FallbackParams {
-    const uint32_t* records;
-    const uint32_t* index;
-    uint64_t wb;
-    uint64_t r0, nrec;
-    uint32_t group, F;
-    int k;
-    void* keys;
-    uint32_t* cnt;
-    uint32_t mask;
-    uint32_t* fail;
-};
-cudaError_t launch_fallback(int W, const FallbackParams& F, uint64_t S, const Phase2Params& P, uint32_t grid,
-                            cudaStream_t st, int* launches);
-
 // per-bucket record / word / k-mer totals from the scanned offsets
 __global__ void k_sizes(const unsigned long long* off_r, const unsigned long long* off_w, uint32_t n_buckets,
                         uint32_t C, unsigned long long* out_recs, unsigned long long* out_words) {
@@ -71,7 +47,9 @@ constexpr uint64_t FWD_SEED[4] = {0x3c8bfbb395c60474ULL, 0x3193c18562a02b4cULL, 
 inline uint64_t hrol(uint64_t x, int s) { s &= 63; return s ? (x << s) | (x >> (64 - s)) : x; }
 inline uint64_t hror(uint64_t x, int s) { s &= 63; return s ? (x >> s) | (x << (64 - s)) : x; }
 
-HashTables make_tables(int m) {
+}  // namespace
+
+HashTables tg::make_hash_tables(int m) {
     HashTables T;
     for (int b = 0; b < 4; ++b) {
         const int nt = b ^ (b >> 1);  // kache A0 C1 G2 T3 -> nt A0 C1 T2 G3
@@ -95,6 +73,8 @@ HashTables make_tables(int m) {
     }
     return T;
 }
+
+namespace {
 
 struct DevBuf {
     void* p = nullptr;
@@ -406,7 +386,7 @@ tg_status tg_job_run(tg_job* j) {
     // hash tables for m
     CK(ctx->ensure(ctx->tables, sizeof(HashTables)), "alloc tables");
     if (ctx->prepared_m != j->o.m) {
-        const HashTables T = make_tables(j->o.m);
+        const HashTables T = make_hash_tables(j->o.m);
         CK(cudaMemcpy(ctx->tables.p, &T, sizeof T, cudaMemcpyHostToDevice), "upload tables");
         ctx->prepared_m = j->o.m;
     }

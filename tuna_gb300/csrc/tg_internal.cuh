@@ -97,6 +97,20 @@ struct Phase2Params {
     uint32_t smem_slots;               // table capacity in shared memory
 };
 
+// A group that did not fit in shared memory, counted in a global table.
+struct FallbackParams {
+    const uint32_t* records;
+    const uint32_t* index;
+    uint64_t wb;          // bucket start word
+    uint64_t r0, nrec;    // bucket record range in the index
+    uint32_t group, F;
+    int k;
+    void* keys;           // S slots
+    uint32_t* cnt;
+    uint32_t mask;
+    uint32_t* fail;
+};
+
 // ---------------------------------------------------------------- bit helpers
 __device__ __forceinline__ uint64_t rol64(uint64_t x, int s) {
     s &= 63;

@@ -350,18 +350,6 @@ k_count(Phase2Params P) {
 // A group that overflowed its shared-memory table is counted in a global
 // table of S slots (power of two >= 2 x its k-mer instances): every CTA walks a
 // slice of the bucket's records and adds the k-mers of the group's records.
-struct FallbackParams {
-    const uint32_t* records;
-    const uint32_t* index;
-    uint64_t wb;          // bucket start word
-    uint64_t r0, nrec;    // bucket record range in the index
-    uint32_t group, F;
-    int k;
-    void* keys;           // S slots
-    uint32_t* cnt;
-    uint32_t mask;
-    uint32_t* fail;
-};
 
 template <int W>
 __global__ void k_fb_insert(FallbackParams P) {
