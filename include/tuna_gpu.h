@@ -166,6 +166,39 @@ tg_status tg_count_seq(tg_ctx* ctx, const tg_job_opts* opts, const uint8_t* seq,
                        uint64_t* keys, uint32_t* counts, uint64_t cap, uint64_t* n_out,
                        tg_stats* stats);
 
+/* ---- counting without device allocation --------------------------------
+ * No counterpart in the reference: tuna allocates its partition buffers and
+ * tables as it goes. This entry point is for callers that must not allocate
+ * device memory when they call in: a plugin or inference-server enqueue that is
+ * given a stream and its buffers, a process whose device memory belongs to
+ * another allocator, or a loop where an allocation would stall the device.
+ *
+ * It counts a sequence stream already in device memory (d_seq, len bytes, the
+ * convention of tg_job_feed_seq) and writes the pairs that pass ci/cx to the
+ * caller's device buffers d_keys (cap * key words u64, see tg_job_key_words)
+ * and d_counts (cap u32); *n_out receives the number of pairs. All work is
+ * ordered on `stream` (a cudaStream_t; NULL = the legacy default stream) and
+ * the call returns when the result is complete. No cudaMalloc / cudaFree (or
+ * any allocating library routine) is called: every intermediate array lives in
+ * one device array of TG_NOALLOC_SCRATCH_BYTES in the library, which each GPU
+ * that loads the library keeps reserved until the process exits.
+ *   - len above TG_NOALLOC_MAX_LEN, or an input whose intermediate arrays do not
+ *     fit in the scratch array, fails with TG_ERR_ARG and a message in errbuf
+ *     (errbuf / errlen may be NULL / 0); k must be <= 63.
+ *   - The first call on a device looks up the scratch array's device address
+ *     (with that device current); make that first call before any stream
+ *     capture on the device.
+ *   - All calls share the one scratch array, so calls whose work overlaps on the
+ *     GPU (two host threads, or two streams without ordering) race; serialise
+ *     them. Each call re-initialises the parts that must start at zero.
+ *   - Output capacity too small: TG_ERR_ARG with *n_out set to the needed size.
+ */
+#define TG_NOALLOC_MAX_LEN (1u << 19)
+#define TG_NOALLOC_SCRATCH_BYTES (64u << 20)
+tg_status tg_count_seq_device_noalloc(const tg_job_opts* opts, const uint8_t* d_seq, size_t len,
+                                      uint64_t* d_keys, uint32_t* d_counts, uint64_t cap,
+                                      uint64_t* n_out, void* stream, char* errbuf, size_t errlen);
+
 #ifdef __cplusplus
 }
 #endif

@@ -74,7 +74,7 @@ ABI_SYMBOLS = ["tg_ctx_create", "tg_ctx_destroy", "tg_last_error", "tg_ctx_strea
                "tg_job_begin", "tg_job_feed_seq", "tg_job_feed_seq_device", "tg_job_feed_fastx",
                "tg_job_feed_file", "tg_job_run", "tg_job_stats", "tg_job_result_size", "tg_job_key_words",
                "tg_job_result_copy", "tg_job_drain", "tg_job_write", "tg_job_export_partitions", "tg_job_end",
-               "tg_count_seq"]
+               "tg_count_seq", "tg_count_seq_device_noalloc"]
 
 
 def library(build_if_missing: bool = True) -> ctypes.CDLL:
@@ -115,6 +115,9 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
     L.tg_job_end.argtypes = [vp]
     L.tg_count_seq.argtypes = [vp, ctypes.POINTER(_JobOpts), vp, sz, vp, vp, u64, ctypes.POINTER(u64),
                                ctypes.POINTER(_Stats)]
+    L.tg_count_seq_device_noalloc.argtypes = [ctypes.POINTER(_JobOpts), vp, sz, vp, vp, u64,
+                                              ctypes.POINTER(u64), vp, ctypes.c_char_p, sz]
+    L.tg_count_seq_device_noalloc.restype = i32
     for fn in ("tg_ctx_create", "tg_ctx_destroy", "tg_job_begin", "tg_job_feed_seq", "tg_job_feed_seq_device",
                "tg_job_feed_fastx", "tg_job_feed_file", "tg_job_run", "tg_job_stats", "tg_job_result_copy",
                "tg_job_drain", "tg_job_write", "tg_job_export_partitions", "tg_job_end", "tg_count_seq"):

@@ -1,0 +1,263 @@
+// tg_noalloc.cu — counting without any device allocation, for callers that
+// must not allocate.
+//
+// Who needs it: code that runs where a cudaMalloc/cudaFree is not allowed or
+// not wanted at call time — an inference-server or plugin `enqueue` that is
+// handed its buffers and a stream and may not allocate, a process whose device
+// memory is owned by another allocator (a framework's caching allocator, a
+// pre-reserved pool), or a latency-critical loop where an allocation would
+// synchronise the device. tg_count_seq_device_noalloc takes the input and the
+// output buffers from the caller and keeps every intermediate array (packed
+// bases, superkmer descriptors, histograms, bucket offsets, bucket records,
+// index, per-CTA lists, fallback table) in one file-scope device array of
+// TG_NOALLOC_SCRATCH_BYTES that the CUDA runtime reserves when the library is
+// loaded on a device and that stays reserved until the process exits.
+//
+// It runs the same kernels as tg_job_run on the same parameters, so its output
+// is the same set of (k-mer, count) pairs. Inputs longer than
+// TG_NOALLOC_MAX_LEN bytes are rejected; so is an input whose intermediate
+// arrays would not fit in the scratch array.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "tg_internal.cuh"
+#include "tg_launch.h"
+#include "tuna_gpu.h"
+
+using namespace tg;
+
+// All scratch of the entry point. In host code this name is only a handle for
+// cudaGetSymbolAddress: its device address is looked up per device at first use.
+static __device__ __align__(256) uint8_t tg_noalloc_scratch[TG_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+std::mutex g_mu;
+constexpr int MAX_DEV = 64;
+uint8_t* g_scratch_addr[MAX_DEV] = {};
+
+void set_err(char* buf, size_t len, const std::string& msg) {
+    if (buf && len) {
+        const size_t n = std::min(len - 1, msg.size());
+        memcpy(buf, msg.data(), n);
+        buf[n] = 0;
+    }
+}
+
+// Device address of the scratch array on the current device (looked up once per
+// device, with that device current).
+cudaError_t scratch_address(int dev, uint8_t** out) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_scratch_addr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, tg_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_scratch_addr[dev] = static_cast<uint8_t*>(p);
+    }
+    *out = g_scratch_addr[dev];
+    return cudaSuccess;
+}
+
+// Bump allocator over the scratch array (256-byte aligned pieces).
+struct Carve {
+    uint8_t* base;
+    size_t off = 0, cap;
+    bool ok = true;
+    template <typename T>
+    T* take(size_t count) {
+        const size_t bytes = (count * sizeof(T) + 255) & ~size_t(255);
+        if (!ok || off + bytes > cap) { ok = false; return nullptr; }
+        T* p = reinterpret_cast<T*>(base + off);
+        off += bytes;
+        return p;
+    }
+};
+
+}  // namespace
+
+extern "C" tg_status tg_count_seq_device_noalloc(const tg_job_opts* opts, const uint8_t* d_seq, size_t len,
+                                                 uint64_t* d_keys, uint32_t* d_counts, uint64_t cap,
+                                                 uint64_t* n_out, void* stream, char* errbuf, size_t errlen) {
+    if (!opts || !n_out || (!d_seq && len)) { set_err(errbuf, errlen, "null argument"); return TG_ERR_ARG; }
+    *n_out = 0;
+    const tg_job_opts& o = *opts;
+    if (o.k < 2 || o.k > 63 || o.m < 1 || o.m > 32 || o.m >= o.k) {
+        set_err(errbuf, errlen, "k must be in [2, 63] and m in [1, min(k-1, 32)]");
+        return o.k > 63 ? TG_ERR_UNSUPPORTED : TG_ERR_ARG;
+    }
+    if (len > TG_NOALLOC_MAX_LEN) {
+        set_err(errbuf, errlen, "input of " + std::to_string(len) + " bytes exceeds the no-allocation limit of " +
+                                    std::to_string(TG_NOALLOC_MAX_LEN) + " bytes");
+        return TG_ERR_ARG;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= MAX_DEV) { set_err(errbuf, errlen, "no current CUDA device"); return TG_ERR_CUDA; }
+    uint8_t* base = nullptr;
+    e = scratch_address(dev, &base);
+    if (e != cudaSuccess) { set_err(errbuf, errlen, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e)); return TG_ERR_CUDA; }
+    int n_sm = 0;
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+#define NA_CK(call, what)                                                                          \
+    do {                                                                                           \
+        const cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) { set_err(errbuf, errlen, std::string(what) + ": " + cudaGetErrorString(e_)); return TG_ERR_CUDA; } \
+    } while (0)
+    const int k = o.k, m = o.m, w = k - m, W = k <= 31 ? 1 : 2;
+    const uint32_t hdr_max = (2u * k - m <= 255u) ? 255u : 65535u;
+    const uint32_t L = hdr_max + 1 - k;
+    const uint64_t n = len;
+    Carve cv{base, 0, (size_t)TG_NOALLOC_SCRATCH_BYTES};
+    // ---- fixed pieces
+    HashTables* tables = cv.take<HashTables>(1);
+    unsigned long long* misc = cv.take<unsigned long long>(32);  // counters, see below
+    uint64_t pw = (TG_PAD + n + CUT_TILE + 2 * MAX_W + 640) / 16 + 16;
+    pw = (pw + 1) & ~uint64_t(1);
+    uint32_t* packed = cv.take<uint32_t>(pw);
+    uint32_t* valid = cv.take<uint32_t>(pw / 2 + 16);
+    // phase-1 layout: as tg_job_run, with room for one record per k-mer start
+    uint32_t p1 = o.gpu_parts ? o.gpu_parts : std::min<uint32_t>(P1_MAX, std::max<uint32_t>(16, (uint32_t)(n / 32768)));
+    uint32_t p1_bits = 0;
+    while ((1u << p1_bits) < p1) ++p1_bits;
+    p1 = 1u << p1_bits;
+    const size_t smem = cut_smem_bytes(w, p1, false);
+    const uint32_t per_sm = std::max<uint32_t>(1, std::min<uint32_t>(2, (uint32_t)(228u * 1024u / (smem + 1024))));
+    uint32_t C = (uint32_t)n_sm * per_sm;
+    uint64_t chunk = (n + C - 1) / C;
+    chunk = std::max<uint64_t>(CUT_TILE, (chunk + CUT_TILE - 1) / CUT_TILE * CUT_TILE);
+    C = (uint32_t)std::max<uint64_t>(1, (n + chunk - 1) / chunk);
+    const uint64_t desc_cap = chunk + 2ull * CUT_TILE + L + 64;
+    uint64_t* desc = cv.take<uint64_t>((size_t)C * desc_cap);
+    uint32_t* n_desc = cv.take<uint32_t>(C);
+    const uint64_t nhist = (uint64_t)p1 * C;
+    uint32_t* hist = cv.take<uint32_t>(2 * nhist + 2 * (size_t)p1);  // + u64 per-bucket k-mers
+    unsigned long long* bucket_kmers = reinterpret_cast<unsigned long long*>(hist + 2 * nhist);
+    unsigned long long* offw = cv.take<unsigned long long>(nhist + 1);
+    unsigned long long* offr = cv.take<unsigned long long>(nhist + 1);
+    const uint64_t nsum = (nhist + 8191) / 8192 + 1;
+    unsigned long long* sums = cv.take<unsigned long long>(2 * nsum + 2);
+    unsigned long long* sizes = cv.take<unsigned long long>(2 * (size_t)p1);
+    uint32_t* order = cv.take<uint32_t>(p1);
+    uint32_t* fallback = cv.take<uint32_t>(3 * 4096);
+    if (!cv.ok) { set_err(errbuf, errlen, "input too large for the no-allocation scratch"); return TG_ERR_ARG; }
+    // counters in misc (u64 indices): [0..2] k-mers/records/runs, [3] bases,
+    // [4] overflow (u32), [8..10] out/distinct/fallback, [12] work (u32), [13] fail (u32)
+    uint32_t* overflow = reinterpret_cast<uint32_t*>(misc + 4);
+    unsigned long long* out_n = misc + 8;
+    uint32_t* work = reinterpret_cast<uint32_t*>(misc + 12);
+    uint32_t* fail = reinterpret_cast<uint32_t*>(misc + 13);
+
+    const HashTables T = make_hash_tables(m);
+    NA_CK(cudaMemcpyAsync(tables, &T, sizeof T, cudaMemcpyHostToDevice, st), "upload tables");
+    NA_CK(cudaMemsetAsync(misc, 0, 32 * 8, st), "memset");
+    NA_CK(cudaMemsetAsync(bucket_kmers, 0, (size_t)p1 * 8, st), "memset");
+    // ---- phase 1
+    NA_CK(launch_pack(d_seq, n, packed, valid, pw, misc + 3, st), "k_pack");
+    CutParams P{};
+    P.packed = packed; P.valid = valid; P.n = n;
+    P.k = k; P.m = m; P.w = w; P.L = L;
+    P.p1_bits = p1_bits; P.n_cta = C; P.chunk = chunk;
+    P.desc = desc; P.desc_cap = desc_cap; P.n_desc = n_desc;
+    P.hist = hist; P.stats = misc; P.overflow = overflow; P.xdesc = nullptr;
+    NA_CK(launch_cut(P, tables, false, st), "k_cut");
+    int launches = 0;
+    NA_CK(launch_scan(hist, nhist, offw, sums, offw + nhist, st, &launches), "scan");
+    NA_CK(launch_scan(hist + nhist, nhist, offr, sums + nsum, offr + nhist, st, &launches), "scan");
+    k_sizes<<<(p1 + 255) / 256, 256, 0, st>>>(offr, offw, p1, C, sizes, sizes + p1);
+    NA_CK(cudaGetLastError(), "k_sizes");
+    std::vector<unsigned long long> hsz(2 * (size_t)p1), hk(p1);
+    unsigned long long tot_w = 0, tot_r = 0, cstats[3] = {0, 0, 0};
+    uint32_t ovf = 0;
+    NA_CK(cudaMemcpyAsync(hsz.data(), sizes, (size_t)p1 * 16, cudaMemcpyDeviceToHost, st), "d2h");
+    NA_CK(cudaMemcpyAsync(hk.data(), bucket_kmers, (size_t)p1 * 8, cudaMemcpyDeviceToHost, st), "d2h");
+    NA_CK(cudaMemcpyAsync(&tot_w, offw + nhist, 8, cudaMemcpyDeviceToHost, st), "d2h");
+    NA_CK(cudaMemcpyAsync(&tot_r, offr + nhist, 8, cudaMemcpyDeviceToHost, st), "d2h");
+    NA_CK(cudaMemcpyAsync(cstats, misc, 24, cudaMemcpyDeviceToHost, st), "d2h");
+    NA_CK(cudaMemcpyAsync(&ovf, overflow, 4, cudaMemcpyDeviceToHost, st), "d2h");
+    NA_CK(cudaStreamSynchronize(st), "phase 1");
+    if (ovf) { set_err(errbuf, errlen, "descriptor capacity exceeded"); return TG_ERR_DEVICE; }
+    // ---- records, index, per-CTA lists from what is left
+    uint32_t* records = cv.take<uint32_t>(tot_w + 16);
+    uint32_t* index = cv.take<uint32_t>(tot_r + 16);
+    uint64_t max_recs = 0;
+    for (uint32_t b = 0; b < p1; ++b) max_recs = std::max<uint64_t>(max_recs, hsz[b]);
+    const uint32_t slots = W == 1 ? 8192 : 4096;
+    const size_t smem2 = count_smem_bytes(W, slots);
+    const uint32_t per_sm2 = std::max<uint32_t>(1, std::min<uint32_t>(2, (uint32_t)(228u * 1024u / (smem2 + 1024))));
+    const size_t left = cv.cap > cv.off ? cv.cap - cv.off : 0;
+    const size_t per_cta = ((max_recs + 1) * 4 + 255) & ~size_t(255);
+    uint32_t grid2 = (uint32_t)std::min<size_t>((size_t)n_sm * per_sm2, per_cta ? left / (per_cta + 256) : 1);
+    if (grid2 == 0) grid2 = 1;
+    uint32_t* scratch = cv.take<uint32_t>((size_t)grid2 * (max_recs + 1));
+    if (!cv.ok) { set_err(errbuf, errlen, "input too large for the no-allocation scratch"); return TG_ERR_ARG; }
+    std::vector<uint32_t> ord(p1);
+    std::iota(ord.begin(), ord.end(), 0u);
+    std::stable_sort(ord.begin(), ord.end(), [&](uint32_t a, uint32_t b) { return hk[a] > hk[b]; });
+    NA_CK(cudaMemcpyAsync(order, ord.data(), (size_t)p1 * 4, cudaMemcpyHostToDevice, st), "h2d");
+    ScatterParams SP{};
+    SP.packed = packed; SP.k = k; SP.p1_bits = p1_bits; SP.n_cta = C; SP.chunk = chunk;
+    SP.desc = desc; SP.desc_cap = desc_cap; SP.n_desc = n_desc;
+    SP.off_w = offw; SP.off_r = offr; SP.records = records; SP.index = index;
+    NA_CK(launch_scatter(SP, st), "k_scatter");
+    // ---- phase 2 straight into the caller's buffers
+    Phase2Params QP{};
+    QP.records = records; QP.index = index; QP.off_w = offw; QP.off_r = offr;
+    QP.n_cta1 = C; QP.n_buckets = p1; QP.order = order; QP.k = k;
+    QP.fine_bits = 24 - p1_bits; QP.target = slots / 2;
+    QP.ci = o.ci; QP.cx = o.cx; QP.work = work;
+    QP.scratch = scratch; QP.scratch_cap = max_recs + 1;
+    QP.out_keys = d_keys; QP.out_counts = d_counts; QP.out_n = out_n; QP.out_cap = cap;
+    QP.fallback = fallback; QP.fallback_cap = 4096; QP.bucket_kmers = bucket_kmers; QP.smem_slots = slots;
+    NA_CK(launch_count(W, QP, grid2, st), "k_count");
+    unsigned long long on[3] = {0, 0, 0};
+    NA_CK(cudaMemcpyAsync(on, out_n, 24, cudaMemcpyDeviceToHost, st), "d2h");
+    NA_CK(cudaStreamSynchronize(st), "phase 2");
+    if (on[2] > 0) {
+        if (on[2] > 4096) { set_err(errbuf, errlen, "too many overflowing groups"); return TG_ERR_TABLE; }
+        std::vector<uint32_t> fl(3 * on[2]);
+        NA_CK(cudaMemcpyAsync(fl.data(), fallback, fl.size() * 4, cudaMemcpyDeviceToHost, st), "d2h");
+        std::vector<unsigned long long> ho(2 * (nhist + 1));
+        NA_CK(cudaMemcpyAsync(ho.data(), offr, (nhist + 1) * 8, cudaMemcpyDeviceToHost, st), "d2h");
+        NA_CK(cudaMemcpyAsync(ho.data() + nhist + 1, offw, (nhist + 1) * 8, cudaMemcpyDeviceToHost, st), "d2h");
+        NA_CK(cudaStreamSynchronize(st), "d2h");
+        const size_t fb_base = cv.off;
+        for (unsigned long long i = 0; i < on[2]; ++i) {
+            const uint32_t b = fl[3 * i], g = fl[3 * i + 1], F = fl[3 * i + 2];
+            uint64_t S = 1024;
+            while (S < 2 * hk[b] + 2) S <<= 1;
+            cv.off = fb_base;  // groups run one after another on the stream; reuse the space
+            cv.ok = true;
+            void* keys = cv.take<uint8_t>((size_t)S * key_bytes(W));
+            uint32_t* cnt = cv.take<uint32_t>(S);
+            if (!cv.ok) { set_err(errbuf, errlen, "an overflowing group does not fit in the no-allocation scratch"); return TG_ERR_TABLE; }
+            FallbackParams FP{};
+            FP.records = records; FP.index = index;
+            FP.wb = ho[nhist + 1 + (uint64_t)b * C];
+            FP.r0 = ho[(uint64_t)b * C];
+            FP.nrec = ho[(uint64_t)(b + 1) * C] - FP.r0;
+            FP.group = g; FP.F = F; FP.k = k; FP.keys = keys; FP.cnt = cnt;
+            FP.mask = (uint32_t)(S - 1); FP.fail = fail;
+            NA_CK(launch_fallback(W, FP, S, QP, (uint32_t)n_sm * 2, st, &launches), "fallback");
+        }
+        uint32_t failed = 0;
+        NA_CK(cudaMemcpyAsync(&failed, fail, 4, cudaMemcpyDeviceToHost, st), "d2h");
+        NA_CK(cudaMemcpyAsync(on, out_n, 16, cudaMemcpyDeviceToHost, st), "d2h");
+        NA_CK(cudaStreamSynchronize(st), "fallback");
+        if (failed) { set_err(errbuf, errlen, "fallback table overflow"); return TG_ERR_TABLE; }
+    }
+    *n_out = on[0];
+    if (on[0] > cap) {
+        set_err(errbuf, errlen, "output capacity too small: " + std::to_string(on[0]) + " k-mers");
+        return TG_ERR_ARG;
+    }
+#undef NA_CK
+    return TG_OK;
+}
