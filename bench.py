@@ -229,7 +229,7 @@ def main():
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(ext)
     launches = 0
-    kern = {"pack": [], "cut": [], "scatter": [], "count": [], "phase1": []}
+    kern = {"pack": [], "cut": [], "scatter": [], "count": [], "phase1": [], "count_kernel": []}
     for _ in range(args.steps):
         st = step()
         launches += int(st["gpu_launches"])
@@ -238,6 +238,7 @@ def main():
         kern["scatter"].append(st["phase1_scatter_ms"])
         kern["count"].append(st["phase2_ms"])
         kern["phase1"].append(st["phase1_ms"])
+        kern["count_kernel"].append(st["phase2_count_ms"])
     e1.record(ext)
     e1.synchronize()
     torch.cuda.synchronize()
@@ -251,14 +252,16 @@ def main():
     avg = {k2: statistics.mean(v) for k2, v in kern.items()}
     recs = st["superkmers"]
     n_stream = int(dev.numel())
+    rec_bases = st["kmers"] + recs * (K - 1)
     alg = {
         "cut": n_stream / 4 + n_stream / 8 + 8 * recs,            # packed + validity in, descriptors out
-        "scatter": 8 * recs + st["record_bytes"] / 2 + st["record_bytes"] + 4 * recs,  # desc + bases in, records + index out
-        "count": st["record_bytes"] + 4 * recs + st["out"] * 12,  # records + index in, (key, count) out
+        "scatter": 16 * recs,                                     # descriptors in, bucket-ordered descriptors out
+        "count": 8 * recs + rec_bases / 4 + st["out"] * 12,       # descriptors + record bases in, (key, count) out
         "pack": n_stream + n_stream / 4 + n_stream / 8,           # ASCII in, packed + validity out
     }
     dom = max(("cut", "scatter", "count", "pack"), key=lambda x: avg[x])
     achieved = alg[dom] / (avg[dom] / 1e3) / 1e9
+    kernel_names = {"cut": "k_cut", "scatter": "k_bucket", "count": "k_count", "pack": "k_pack"}
     # phase 1 against the reference's algorithmic bytes B1 = N/4 + record bytes (~1.82 B/base)
     ref_record_bytes = 2 * recs + (st["kmers"] + recs * (K - 1)) / 4
     b1 = bases / 4 + ref_record_bytes
@@ -329,9 +332,8 @@ def main():
                        "parallelism": f"replicas x{world}"},
             "stats": {"kmers": int(st["kmers"]), "superkmers": int(st["superkmers"]),
                       "distinct": int(st["distinct"]), "fallback_groups": int(st["fallback_groups"])},
-            "kernels_ms": {k2: round(v, 4) for k2, v in avg.items()},
-            "roofline": {"bound": "hbm", "kernel": {"cut": "k_cut", "scatter": "k_scatter", "count": "k_count",
-                                                    "pack": "k_pack"}[dom],
+            "kernels_ms": {kernel_names.get(k2, k2): round(v, 4) for k2, v in avg.items()},
+            "roofline": {"bound": "hbm", "kernel": kernel_names[dom],
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                          else "fallback 6.8 TB/s",

@@ -101,6 +101,7 @@ typedef struct {
     double phase1_scatter_ms; /* part of phase1_ms: the bucket scatter kernel */
     uint64_t record_bytes;    /* bytes of bucket records written */
     uint64_t gpu_launches;    /* kernels launched by the last tg_job_run */
+    double phase2_count_ms;   /* part of phase2_ms: the shared-memory counting kernel */
 } tg_stats;
 
 /* Output formats of tg_job_drain. */

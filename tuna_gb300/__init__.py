@@ -57,7 +57,8 @@ class _Stats(ctypes.Structure):
                 ("fallback_groups", ctypes.c_uint64), ("h2d_ms", ctypes.c_double), ("pack_ms", ctypes.c_double),
                 ("phase1_ms", ctypes.c_double), ("phase2_ms", ctypes.c_double), ("d2h_ms", ctypes.c_double),
                 ("phase1_cut_ms", ctypes.c_double), ("phase1_scatter_ms", ctypes.c_double),
-                ("record_bytes", ctypes.c_uint64), ("gpu_launches", ctypes.c_uint64)]
+                ("record_bytes", ctypes.c_uint64), ("gpu_launches", ctypes.c_uint64),
+                ("phase2_count_ms", ctypes.c_double)]
 
     def as_dict(self) -> Dict[str, float]:
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -5,11 +5,11 @@
 //   k_pack      ASCII stream -> 2-bit codes + validity bits
 //   k_cut       minimizers, chain starts, forced splits -> record descriptors
 //               and per (bucket, CTA) histograms
-//   k_scan_*    exclusive scans of the histograms -> bucket offsets
-//   k_sizes     per-bucket record counts (sizing; one host sync here)
-//   k_scatter   descriptors -> bucket records + record index
-//   k_count     per bucket: fine split, shared-memory counting, ci/cx, compaction
-//   k_fb_*      (rare) groups that overflowed shared memory, global tables
+//   k_scan_*    exclusive scan of the histogram -> bucket offsets
+//   k_sizes     per-bucket descriptor counts (sizing; one host sync here)
+//   k_bucket    descriptors -> bucket-major order
+//   k_count     per bucket: bin split, shared-memory counting, ci/cx, compaction
+//   k_fb_*      (rare) bins that overflowed shared memory, global tables
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -27,13 +27,12 @@
 #include "tuna_gpu.h"
 
 namespace tg {
-// per-bucket record / word / k-mer totals from the scanned offsets
-__global__ void k_sizes(const unsigned long long* off_r, const unsigned long long* off_w, uint32_t n_buckets,
-                        uint32_t C, unsigned long long* out_recs, unsigned long long* out_words) {
+// per-bucket descriptor counts from the scanned offsets
+__global__ void k_sizes(const unsigned long long* off_r, uint32_t n_buckets, uint32_t C,
+                        unsigned long long* out_recs) {
     const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= n_buckets) return;
     out_recs[b] = off_r[(uint64_t)(b + 1) * C] - off_r[(uint64_t)b * C];
-    out_words[b] = off_w[(uint64_t)(b + 1) * C] - off_w[(uint64_t)b * C];
 }
 }  // namespace tg
 
@@ -111,7 +110,7 @@ struct tg_ctx {
     size_t smem_optin = 0;
     unsigned host_threads = 1;
     std::string err;
-    DevBuf seq, packed, valid, desc, xdesc, hist, offw, offr, sums, sizes, records, index, scratch, okeys, ocnt,
+    DevBuf seq, packed, valid, desc, xdesc, hist, offr, sums, sizes, records, scratch, okeys, ocnt,
         misc, fallback, fbtab, order, tables;
     cudaEvent_t ev[12] = {};
     tg_job* active = nullptr;
@@ -202,8 +201,8 @@ tg_status tg_ctx_destroy(tg_ctx* ctx) {
     if (!ctx) return TG_ERR_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->st) cudaStreamSynchronize(ctx->st);
-    DevBuf* bufs[] = {&ctx->seq, &ctx->packed, &ctx->valid, &ctx->desc, &ctx->xdesc, &ctx->hist, &ctx->offw,
-                      &ctx->offr, &ctx->sums, &ctx->sizes, &ctx->records, &ctx->index, &ctx->scratch,
+    DevBuf* bufs[] = {&ctx->seq, &ctx->packed, &ctx->valid, &ctx->desc, &ctx->xdesc, &ctx->hist,
+                      &ctx->offr, &ctx->sums, &ctx->sizes, &ctx->records, &ctx->scratch,
                       &ctx->okeys, &ctx->ocnt, &ctx->misc, &ctx->fallback, &ctx->fbtab, &ctx->order,
                       &ctx->tables};
     for (DevBuf* b : bufs)
@@ -340,9 +339,9 @@ static tg_status run_cut(tg_job* j, bool exp, uint32_t p1_bits, int* launches) {
         j->desc_cap = cap;
         CK(ctx->ensure(ctx->desc, (size_t)C * cap * 8), "alloc descriptors");
         if (exp) CK(ctx->ensure(ctx->xdesc, (size_t)C * cap * 24), "alloc export descriptors");
-        const size_t hist_bytes = (size_t)2 * p1 * C * 4 + (size_t)p1 * 8;
-        CK(ctx->ensure(ctx->hist, hist_bytes), "alloc histograms");
-        CK(cudaMemsetAsync(ctx->hist.as<uint8_t>() + (size_t)2 * p1 * C * 4, 0, (size_t)p1 * 8, ctx->st), "memset");
+        const size_t kmers_off = 4 * (size_t)hist_kmers_offset(p1, C);
+        CK(ctx->ensure(ctx->hist, kmers_off + (size_t)p1 * 8), "alloc histograms");
+        CK(cudaMemsetAsync(ctx->hist.as<uint8_t>() + kmers_off, 0, (size_t)p1 * 8, ctx->st), "memset");
         CK(cudaMemsetAsync(ctx->misc.as<uint8_t>() + MISC_CUT_STATS, 0, 24, ctx->st), "memset");
         CK(cudaMemsetAsync(ctx->misc.as<uint8_t>() + MISC_OVERFLOW, 0, 4, ctx->st), "memset");
         CutParams P{};
@@ -383,6 +382,7 @@ tg_status tg_job_run(tg_job* j) {
     const int k = j->o.k;
     const int W = j->W;
     j->ran = true;
+    if (n >= (1ull << DESC_START_BITS)) return ctx->fail(TG_ERR_ARG, "input stream longer than 2^36 bytes");
     // hash tables for m
     CK(ctx->ensure(ctx->tables, sizeof(HashTables)), "alloc tables");
     if (ctx->prepared_m != j->o.m) {
@@ -407,7 +407,7 @@ tg_status tg_job_run(tg_job* j) {
     CK(cudaMemcpyAsync(&n_bases, ctx->misc.as<uint8_t>() + MISC_BASES, 8, cudaMemcpyDeviceToHost, ctx->st), "d2h");
     // ---- phase 1: cut
     uint32_t p1 = j->o.gpu_parts;
-    if (!p1) p1 = std::min<uint32_t>(P1_MAX, std::max<uint32_t>(16, next_pow2_u32(n / 32768)));
+    if (!p1) p1 = std::min<uint32_t>(1024, std::max<uint32_t>(16, next_pow2_u32(n / 32768)));
     uint32_t p1_bits = 0;
     while ((1u << p1_bits) < p1) ++p1_bits;
     tg_status s = run_cut(j, false, p1_bits, &launches);
@@ -416,42 +416,34 @@ tg_status tg_job_run(tg_job* j) {
     CK(cudaMemcpyAsync(cstats, ctx->misc.as<uint8_t>() + MISC_CUT_STATS, 24, cudaMemcpyDeviceToHost, ctx->st), "d2h");
     const uint32_t C = j->n_cta;
     const uint64_t nhist = (uint64_t)p1 * C;
-    // ---- scans: offsets over [bucket][cta] of words and records
-    CK(ctx->ensure(ctx->offw, (nhist + 1) * 8), "alloc offsets");
+    // ---- scan: descriptor offsets over [bucket][cta]
     CK(ctx->ensure(ctx->offr, (nhist + 1) * 8), "alloc offsets");
-    CK(ctx->ensure(ctx->sums, ((nhist + 8191) / 8192 + 2) * 8 * 2), "alloc sums");
-    unsigned long long* sums = ctx->sums.as<unsigned long long>();
-    const uint64_t nsum = (nhist + 8191) / 8192 + 1;
+    CK(ctx->ensure(ctx->sums, ((nhist + 8191) / 8192 + 2) * 8), "alloc sums");
     CK(cudaEventRecord(ctx->ev[4], ctx->st), "event");
-    CK(launch_scan(ctx->hist.as<uint32_t>(), nhist, ctx->offw.as<unsigned long long>(), sums,
-                   ctx->offw.as<unsigned long long>() + nhist, ctx->st, &launches), "scan");
-    CK(launch_scan(ctx->hist.as<uint32_t>() + nhist, nhist, ctx->offr.as<unsigned long long>(), sums + nsum,
-                   ctx->offr.as<unsigned long long>() + nhist, ctx->st, &launches), "scan");
-    CK(ctx->ensure(ctx->sizes, (size_t)p1 * 16), "alloc sizes");
-    k_sizes<<<(p1 + 255) / 256, 256, 0, ctx->st>>>(ctx->offr.as<unsigned long long>(), ctx->offw.as<unsigned long long>(),
-                                                   p1, C, ctx->sizes.as<unsigned long long>(),
-                                                   ctx->sizes.as<unsigned long long>() + p1);
+    CK(launch_scan(ctx->hist.as<uint32_t>(), nhist, ctx->offr.as<unsigned long long>(),
+                   ctx->sums.as<unsigned long long>(), ctx->offr.as<unsigned long long>() + nhist, ctx->st,
+                   &launches), "scan");
+    CK(ctx->ensure(ctx->sizes, (size_t)p1 * 8), "alloc sizes");
+    k_sizes<<<(p1 + 255) / 256, 256, 0, ctx->st>>>(ctx->offr.as<unsigned long long>(), p1, C,
+                                                   ctx->sizes.as<unsigned long long>());
     ++launches;
     CK(cudaGetLastError(), "k_sizes");
-    std::vector<unsigned long long> hsz(2 * (size_t)p1), hk(p1);
-    unsigned long long tot_w = 0, tot_r = 0;
-    CK(cudaMemcpyAsync(hsz.data(), ctx->sizes.p, (size_t)p1 * 16, cudaMemcpyDeviceToHost, ctx->st), "d2h");
-    CK(cudaMemcpyAsync(hk.data(), ctx->hist.as<uint8_t>() + (size_t)2 * nhist * 4, (size_t)p1 * 8,
-                       cudaMemcpyDeviceToHost, ctx->st), "d2h");
-    CK(cudaMemcpyAsync(&tot_w, ctx->offw.as<unsigned long long>() + nhist, 8, cudaMemcpyDeviceToHost, ctx->st), "d2h");
+    std::vector<unsigned long long> hsz(p1), hk(p1);
+    unsigned long long tot_r = 0;
+    CK(cudaMemcpyAsync(hsz.data(), ctx->sizes.p, (size_t)p1 * 8, cudaMemcpyDeviceToHost, ctx->st), "d2h");
+    const unsigned long long* bucket_kmers =
+        reinterpret_cast<const unsigned long long*>(ctx->hist.as<uint32_t>() + hist_kmers_offset(p1, C));
+    CK(cudaMemcpyAsync(hk.data(), bucket_kmers, (size_t)p1 * 8, cudaMemcpyDeviceToHost, ctx->st), "d2h");
     CK(cudaMemcpyAsync(&tot_r, ctx->offr.as<unsigned long long>() + nhist, 8, cudaMemcpyDeviceToHost, ctx->st), "d2h");
     CK(cudaStreamSynchronize(ctx->st), "phase 1");
-    // ---- buffers for records, index, scratch, output
+    // ---- buffers: bucketed descriptors, per-CTA bin lists, output
     uint64_t max_recs = 0;
     for (uint32_t b = 0; b < p1; ++b) max_recs = std::max<uint64_t>(max_recs, hsz[b]);
     const uint64_t n_kmers = cstats[0];
-    CK(ctx->ensure(ctx->records, tot_w * 4 + 64), "alloc records");
-    CK(ctx->ensure(ctx->index, tot_r * 4 + 64), "alloc index");
+    CK(ctx->ensure(ctx->records, tot_r * 8 + 64), "alloc bucket descriptors");
     const uint32_t slots = W == 1 ? 8192 : 4096;
-    const size_t smem2 = count_smem_bytes(W, slots);
-    const uint32_t per_sm2 = std::max<uint32_t>(1, std::min<uint32_t>(2, (uint32_t)(228u * 1024u / (smem2 + 1024))));
-    const uint32_t grid2 = (uint32_t)ctx->n_sm * per_sm2;
-    CK(ctx->ensure(ctx->scratch, (size_t)grid2 * (max_recs + 1) * 4), "alloc scratch");
+    const uint32_t grid2 = (uint32_t)ctx->n_sm;  // k_count runs one 512-thread CTA per SM
+    CK(ctx->ensure(ctx->scratch, (size_t)grid2 * (max_recs + 1) * 8), "alloc scratch");
     const uint64_t out_cap = std::max<uint64_t>(n_kmers, 1);
     CK(ctx->ensure(ctx->okeys, out_cap * key_bytes(W)), "alloc output keys");
     CK(ctx->ensure(ctx->ocnt, out_cap * 4), "alloc output counts");
@@ -462,22 +454,17 @@ tg_status tg_job_run(tg_job* j) {
     std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return hk[a] > hk[b]; });
     CK(ctx->ensure(ctx->order, (size_t)p1 * 4), "alloc order");
     CK(cudaMemcpyAsync(ctx->order.p, order.data(), (size_t)p1 * 4, cudaMemcpyHostToDevice, ctx->st), "h2d");
-    // ---- scatter
-    ScatterParams SP{};
-    SP.packed = ctx->packed.as<uint32_t>();
-    SP.k = k;
-    SP.p1_bits = p1_bits;
-    SP.n_cta = C;
-    SP.chunk = j->chunk;
-    SP.desc = ctx->desc.as<uint64_t>();
-    SP.desc_cap = j->desc_cap;
-    SP.n_desc = reinterpret_cast<const uint32_t*>(ctx->misc.as<uint8_t>() + MISC_NDESC);
-    SP.off_w = ctx->offw.as<unsigned long long>();
-    SP.off_r = ctx->offr.as<unsigned long long>();
-    SP.records = ctx->records.as<uint32_t>();
-    SP.index = ctx->index.as<uint32_t>();
+    // ---- descriptors into bucket order
+    BucketParams BP{};
+    BP.p1_bits = p1_bits;
+    BP.n_cta = C;
+    BP.desc = ctx->desc.as<uint64_t>();
+    BP.desc_cap = j->desc_cap;
+    BP.n_desc = reinterpret_cast<const uint32_t*>(ctx->misc.as<uint8_t>() + MISC_NDESC);
+    BP.off_r = ctx->offr.as<unsigned long long>();
+    BP.bdesc = ctx->records.as<uint64_t>();
     CK(cudaEventRecord(ctx->ev[5], ctx->st), "event");
-    CK(launch_scatter(SP, ctx->st), "k_scatter");
+    CK(launch_bucket(BP, ctx->st), "k_bucket");
     ++launches;
     CK(cudaEventRecord(ctx->ev[6], ctx->st), "event");
     // ---- phase 2
@@ -486,20 +473,19 @@ tg_status tg_job_run(tg_job* j) {
     CK(cudaMemsetAsync(out_n, 0, 24, ctx->st), "memset");
     CK(cudaMemsetAsync(work, 0, 4, ctx->st), "memset");
     Phase2Params QP{};
-    QP.records = ctx->records.as<uint32_t>();
-    QP.index = ctx->index.as<uint32_t>();
-    QP.off_w = ctx->offw.as<unsigned long long>();
+    QP.packed = ctx->packed.as<uint32_t>();
+    QP.bdesc = ctx->records.as<uint64_t>();
     QP.off_r = ctx->offr.as<unsigned long long>();
     QP.n_cta1 = C;
     QP.n_buckets = p1;
+    QP.p1_bits = p1_bits;
     QP.order = ctx->order.as<uint32_t>();
     QP.k = k;
-    QP.fine_bits = 24 - p1_bits;
-    QP.target = slots / 2;
+    QP.target = slots - slots * 3 / 10;
     QP.ci = j->o.ci;
     QP.cx = j->o.cx;
     QP.work = work;
-    QP.scratch = ctx->scratch.as<uint32_t>();
+    QP.scratch = ctx->scratch.as<uint64_t>();
     QP.scratch_cap = max_recs + 1;
     QP.out_keys = ctx->okeys.p;
     QP.out_counts = ctx->ocnt.as<uint32_t>();
@@ -507,7 +493,7 @@ tg_status tg_job_run(tg_job* j) {
     QP.out_cap = out_cap;
     QP.fallback = ctx->fallback.as<uint32_t>();
     QP.fallback_cap = 4096;
-    QP.bucket_kmers = reinterpret_cast<const unsigned long long*>(ctx->hist.as<uint8_t>() + (size_t)2 * nhist * 4);
+    QP.bucket_kmers = bucket_kmers;
     QP.smem_slots = slots;
     CK(launch_count(W, QP, grid2, ctx->st), "k_count");
     ++launches;
@@ -515,36 +501,34 @@ tg_status tg_job_run(tg_job* j) {
     unsigned long long on[3] = {0, 0, 0};
     CK(cudaMemcpyAsync(on, out_n, 24, cudaMemcpyDeviceToHost, ctx->st), "d2h");
     CK(cudaStreamSynchronize(ctx->st), "phase 2");
-    // ---- groups that did not fit in shared memory
+    // ---- bins that did not fit in shared memory
     if (on[2] > 0) {
         if (on[2] > 4096) return ctx->fail(TG_ERR_TABLE, "too many overflowing groups");
         std::vector<uint32_t> fl(3 * on[2]);
         CK(cudaMemcpy(fl.data(), ctx->fallback.p, fl.size() * 4, cudaMemcpyDeviceToHost), "d2h");
-        std::vector<unsigned long long> offr_h(2), offw_h(1);
         for (unsigned long long i = 0; i < on[2]; ++i) {
-            const uint32_t b = fl[3 * i], g = fl[3 * i + 1], F = fl[3 * i + 2];
-            unsigned long long r01[2], wb;
+            const uint32_t b = fl[3 * i], bin = fl[3 * i + 1], nbins = fl[3 * i + 2];
+            unsigned long long r01[2];
             CK(cudaMemcpy(&r01[0], ctx->offr.as<unsigned long long>() + (uint64_t)b * C, 8, cudaMemcpyDeviceToHost), "d2h");
             CK(cudaMemcpy(&r01[1], ctx->offr.as<unsigned long long>() + (uint64_t)(b + 1) * C, 8, cudaMemcpyDeviceToHost), "d2h");
-            CK(cudaMemcpy(&wb, ctx->offw.as<unsigned long long>() + (uint64_t)b * C, 8, cudaMemcpyDeviceToHost), "d2h");
             uint64_t S = 1024;
             while (S < 2 * hk[b] + 2) S <<= 1;
+            if (S > (1ull << 32)) return ctx->fail(TG_ERR_TABLE, "fallback table too large");
             const size_t kbytes = (size_t)S * key_bytes(W);
             CK(ctx->ensure(ctx->fbtab, kbytes + (size_t)S * 4 + 16), "alloc fallback table");
             FallbackParams FP{};
-            FP.records = ctx->records.as<uint32_t>();
-            FP.index = ctx->index.as<uint32_t>();
-            FP.wb = wb;
+            FP.packed = ctx->packed.as<uint32_t>();
+            FP.bdesc = ctx->records.as<uint64_t>();
             FP.r0 = r01[0];
             FP.nrec = r01[1] - r01[0];
-            FP.group = g;
-            FP.F = F;
+            FP.bin = bin;
+            FP.nbins = nbins;
+            FP.p1_bits = p1_bits;
             FP.k = k;
             FP.keys = ctx->fbtab.p;
             FP.cnt = reinterpret_cast<uint32_t*>(ctx->fbtab.as<uint8_t>() + kbytes);
             FP.mask = (uint32_t)(S - 1);
             FP.fail = reinterpret_cast<uint32_t*>(ctx->misc.as<uint8_t>() + MISC_FAIL);
-            if (S > (1ull << 32)) return ctx->fail(TG_ERR_TABLE, "fallback table too large");
             CK(cudaMemsetAsync(FP.fail, 0, 4, ctx->st), "memset");
             CK(launch_fallback(W, FP, S, QP, (uint32_t)ctx->n_sm * 4, ctx->st, &launches), "fallback");
             uint32_t failed = 0;
@@ -570,7 +554,7 @@ tg_status tg_job_run(tg_job* j) {
     S.out = on[0];
     S.gpu_parts = p1;
     S.fallback_groups = on[2];
-    S.record_bytes = tot_w * 4;
+    S.record_bytes = tot_r * 8;
     cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]); S.pack_ms = ms;
     cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]); S.phase1_cut_ms = ms;
     float scan_ms = 0;
@@ -578,14 +562,11 @@ tg_status tg_job_run(tg_job* j) {
     cudaEventElapsedTime(&ms, ctx->ev[5], ctx->ev[6]); S.phase1_scatter_ms = ms;
     S.phase1_ms = S.phase1_cut_ms + scan_ms + S.phase1_scatter_ms;
     cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[8]); S.phase2_ms = ms;
+    cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]); S.phase2_count_ms = ms;
     S.gpu_launches = (uint64_t)launches;
-    uint32_t fmax = 1;
-    for (uint32_t b = 0; b < p1; ++b) {
-        uint32_t F = 1;
-        while ((uint64_t)F * (slots / 2) < hk[b] && F < 1024 && F < (1u << (24 - p1_bits))) F <<= 1;
-        fmax = std::max(fmax, F);
-    }
-    S.fine_groups_max = fmax;
+    uint64_t kmax = 0;
+    for (uint32_t b = 0; b < p1; ++b) kmax = std::max<uint64_t>(kmax, hk[b]);
+    S.fine_groups_max = (uint32_t)((kmax + QP.target - 1) / QP.target);
     return TG_OK;
 }
 

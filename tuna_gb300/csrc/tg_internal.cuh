@@ -8,11 +8,10 @@
 //                            index g + TG_PAD, the TG_PAD leading bases are 0
 //   valid   u32[]            1 bit per base, LSB-first, same TG_PAD offset
 //   desc    u64[C][cap]      per Phase-1 CTA: one descriptor per superkmer record
-//                            (start relative to the CTA chunk, k-mer count, the low
-//                            24 bits of its minimizer hash)
-//   hist    u32[2][P][C]     record words / record count per (bucket, CTA)
-//   records u32[]            bucket-major: [hdr][ceil(len/16) packed words] ...
-//   index   u32[]            bucket-major: word offset of each record in its bucket
+//                            (start position, k-mer count, low 20 bits of its
+//                            minimizer hash; see desc_pack)
+//   hist    u32[P][C]        records per (bucket, CTA), then u64[P] k-mers per bucket
+//   bdesc   u64[]            the descriptors again, bucket-major (phase 2 input)
 //   out     keys + u32 counts of the distinct k-mers that pass ci/cx
 #pragma once
 #include <cstdint>
@@ -24,7 +23,7 @@ constexpr int TG_PAD = 32;          // leading invalid bases in packed/valid
 constexpr int CUT_TILE = 1024;      // k-mer start positions per Phase-1 tile
 constexpr int CUT_THREADS = 256;
 constexpr int MAX_W = 255;          // w = k - m
-constexpr int P1_MAX = 4096;        // max internal buckets (smem histogram)
+constexpr int P1_MAX = 4096;        // max internal buckets (smem histogram, >= 8 bin bits)
 constexpr uint32_t NONE32 = 0xFFFFFFFFu;
 
 // Event types of the Phase-1 tile event list.
@@ -38,6 +37,25 @@ struct HashTables {
     uint64_t GF[256], GR[256];   // 4-base group terms for initialisation
 };
 
+// Superkmer record descriptor (u64): the record covers the k-mers starting at
+// positions [start, start + nk) of the stream; its bases are read from
+// `packed` when it is counted. mlo = low 20 bits of the minimizer hash: the
+// low log2(P) bits pick the bucket, the rest the bin inside the bucket.
+constexpr int DESC_START_BITS = 36;
+__host__ __device__ __forceinline__ uint64_t desc_pack(uint64_t start, uint32_t nk, uint32_t mlo) {
+    return start | ((uint64_t)nk << DESC_START_BITS) | ((uint64_t)(mlo & 0xFFFFFu) << 44);
+}
+__host__ __device__ __forceinline__ uint64_t desc_start(uint64_t d) { return d & ((1ull << DESC_START_BITS) - 1); }
+__host__ __device__ __forceinline__ uint32_t desc_nk(uint64_t d) { return (uint32_t)(d >> DESC_START_BITS) & 0xFFu; }
+__host__ __device__ __forceinline__ uint32_t desc_mlo(uint64_t d) { return (uint32_t)(d >> 44); }
+
+// Offset (in u32 units) of the u64 per-bucket k-mer counters that follow the
+// u32 [P][C] record histogram: rounded up so the u64 array is 8-byte aligned
+// whatever P * C is.
+__host__ __device__ __forceinline__ uint64_t hist_kmers_offset(uint64_t p1, uint64_t n_cta) {
+    return (p1 * n_cta + 1) & ~uint64_t(1);
+}
+
 struct CutParams {
     const uint32_t* packed;
     const uint32_t* valid;
@@ -47,63 +65,57 @@ struct CutParams {
     uint32_t p1_bits;        // log2 internal bucket count
     uint32_t n_cta;
     uint64_t chunk;          // k-mer start positions per CTA (multiple of CUT_TILE)
-    uint64_t* desc;          // [n_cta][desc_cap]
+    uint64_t* desc;          // [n_cta][desc_cap] record descriptors
     uint64_t desc_cap;
     uint32_t* n_desc;        // [n_cta]
-    uint32_t* hist;          // [2][P][n_cta] words, records
+    uint32_t* hist;          // u32 [P][n_cta] records, then u64 [P] k-mers per bucket
     unsigned long long* stats;  // [0] kmers, [1] records, [2] runs
     uint32_t* overflow;      // set when a CTA's descriptor list is full
     // export mode: full descriptors (start, minimizer hash, min_pos, nk)
     uint64_t* xdesc;         // [n_cta][desc_cap][3] or null
 };
 
-struct ScatterParams {
-    const uint32_t* packed;
-    int k;
+struct BucketParams {
     uint32_t p1_bits;
     uint32_t n_cta;
-    uint64_t chunk;
     const uint64_t* desc;
     uint64_t desc_cap;
     const uint32_t* n_desc;
-    const unsigned long long* off_w;   // exclusive scan over [P][C] of words
     const unsigned long long* off_r;   // exclusive scan over [P][C] of records
-    uint32_t* records;
-    uint32_t* index;
+    uint64_t* bdesc;                   // descriptors in bucket order
 };
 
 struct Phase2Params {
-    const uint32_t* records;
-    const uint32_t* index;
-    const unsigned long long* off_w;   // [P][C] (bucket start = off_w[p*C])
-    const unsigned long long* off_r;
+    const uint32_t* packed;
+    const uint64_t* bdesc;             // descriptors in bucket order
+    const unsigned long long* off_r;   // [P][C] + total (bucket start = off_r[p*C])
     uint32_t n_cta1;                   // C of phase 1
     uint32_t n_buckets;
+    uint32_t p1_bits;
     const uint32_t* order;             // bucket processing order
     int k;
-    uint32_t fine_bits;                // bits available for fine groups
-    uint32_t target;                   // k-mer instances per fine group
+    uint32_t target;                   // k-mer instances per group
     uint64_t ci, cx;
     uint32_t* work;                    // [0] next bucket
-    uint32_t* scratch;                 // [n_cta2][scratch_cap]
+    uint64_t* scratch;                 // [n_cta2][scratch_cap] descriptors sorted by bin
     uint64_t scratch_cap;
     void* out_keys;                    // u64 x W per k-mer
     uint32_t* out_counts;
     unsigned long long* out_n;         // [0] out cursor, [1] distinct, [2] fallback groups
     uint64_t out_cap;
-    uint32_t* fallback;                // [cap][3]: bucket, group, F
+    uint32_t* fallback;                // [cap][3]: bucket, bin, bins
     uint32_t fallback_cap;
     const unsigned long long* bucket_kmers;  // per bucket k-mer instances
     uint32_t smem_slots;               // table capacity in shared memory
 };
 
-// A group that did not fit in shared memory, counted in a global table.
+// A bin that did not fit in shared memory, counted in a global table.
 struct FallbackParams {
-    const uint32_t* records;
-    const uint32_t* index;
-    uint64_t wb;          // bucket start word
-    uint64_t r0, nrec;    // bucket record range in the index
-    uint32_t group, F;
+    const uint32_t* packed;
+    const uint64_t* bdesc;
+    uint64_t r0, nrec;    // the bucket's descriptor range
+    uint32_t bin, nbins;  // bin of the overflowing group, bins of its bucket
+    uint32_t p1_bits;
     int k;
     void* keys;           // S slots
     uint32_t* cnt;

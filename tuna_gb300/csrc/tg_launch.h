@@ -12,7 +12,7 @@ cudaError_t launch_pack(const uint8_t* seq, uint64_t n, uint32_t* packed, uint32
 cudaError_t launch_cut(const CutParams& P, const HashTables* gT, bool exp, cudaStream_t st);
 cudaError_t launch_scan(const uint32_t* in, uint64_t n, unsigned long long* out, unsigned long long* sums,
                         unsigned long long* total, cudaStream_t st, int* launches);
-cudaError_t launch_scatter(const ScatterParams& P, cudaStream_t st);
+cudaError_t launch_bucket(const BucketParams& P, cudaStream_t st);
 size_t count_smem_bytes(int W, uint32_t slots);
 size_t key_bytes(int W);
 cudaError_t launch_count(int W, const Phase2Params& P, uint32_t grid, cudaStream_t st);
@@ -22,6 +22,6 @@ cudaError_t launch_fallback(int W, const FallbackParams& F, uint64_t S, const Ph
 // ntHash roll / init tables for minimizer length m (host side).
 HashTables make_hash_tables(int m);
 
-__global__ void k_sizes(const unsigned long long* off_r, const unsigned long long* off_w, uint32_t n_buckets,
-                        uint32_t C, unsigned long long* out_recs, unsigned long long* out_words);
+__global__ void k_sizes(const unsigned long long* off_r, uint32_t n_buckets, uint32_t C,
+                        unsigned long long* out_recs);
 }  // namespace tg

@@ -8,8 +8,8 @@
 // pre-reserved pool), or a latency-critical loop where an allocation would
 // synchronise the device. tg_count_seq_device_noalloc takes the input and the
 // output buffers from the caller and keeps every intermediate array (packed
-// bases, superkmer descriptors, histograms, bucket offsets, bucket records,
-// index, per-CTA lists, fallback table) in one file-scope device array of
+// bases, superkmer descriptors, histograms, bucket offsets, bucketed
+// descriptors, per-CTA bin lists, fallback table) in one file-scope device array of
 // TG_NOALLOC_SCRATCH_BYTES that the CUDA runtime reserves when the library is
 // loaded on a device and that stays reserved until the process exits.
 //
@@ -124,7 +124,7 @@ extern "C" tg_status tg_count_seq_device_noalloc(const tg_job_opts* opts, const 
     uint32_t* packed = cv.take<uint32_t>(pw);
     uint32_t* valid = cv.take<uint32_t>(pw / 2 + 16);
     // phase-1 layout: as tg_job_run, with room for one record per k-mer start
-    uint32_t p1 = o.gpu_parts ? o.gpu_parts : std::min<uint32_t>(P1_MAX, std::max<uint32_t>(16, (uint32_t)(n / 32768)));
+    uint32_t p1 = o.gpu_parts ? o.gpu_parts : std::min<uint32_t>(1024, std::max<uint32_t>(16, (uint32_t)(n / 32768)));
     uint32_t p1_bits = 0;
     while ((1u << p1_bits) < p1) ++p1_bits;
     p1 = 1u << p1_bits;
@@ -138,13 +138,12 @@ extern "C" tg_status tg_count_seq_device_noalloc(const tg_job_opts* opts, const 
     uint64_t* desc = cv.take<uint64_t>((size_t)C * desc_cap);
     uint32_t* n_desc = cv.take<uint32_t>(C);
     const uint64_t nhist = (uint64_t)p1 * C;
-    uint32_t* hist = cv.take<uint32_t>(2 * nhist + 2 * (size_t)p1);  // + u64 per-bucket k-mers
-    unsigned long long* bucket_kmers = reinterpret_cast<unsigned long long*>(hist + 2 * nhist);
-    unsigned long long* offw = cv.take<unsigned long long>(nhist + 1);
+    uint32_t* hist = cv.take<uint32_t>(hist_kmers_offset(p1, C) + 2 * (size_t)p1);  // + u64 per-bucket k-mers
+    unsigned long long* bucket_kmers = reinterpret_cast<unsigned long long*>(hist + hist_kmers_offset(p1, C));
     unsigned long long* offr = cv.take<unsigned long long>(nhist + 1);
     const uint64_t nsum = (nhist + 8191) / 8192 + 1;
-    unsigned long long* sums = cv.take<unsigned long long>(2 * nsum + 2);
-    unsigned long long* sizes = cv.take<unsigned long long>(2 * (size_t)p1);
+    unsigned long long* sums = cv.take<unsigned long long>(nsum + 2);
+    unsigned long long* sizes = cv.take<unsigned long long>(p1);
     uint32_t* order = cv.take<uint32_t>(p1);
     uint32_t* fallback = cv.take<uint32_t>(3 * 4096);
     if (!cv.ok) { set_err(errbuf, errlen, "input too large for the no-allocation scratch"); return TG_ERR_ARG; }
@@ -169,49 +168,43 @@ extern "C" tg_status tg_count_seq_device_noalloc(const tg_job_opts* opts, const 
     P.hist = hist; P.stats = misc; P.overflow = overflow; P.xdesc = nullptr;
     NA_CK(launch_cut(P, tables, false, st), "k_cut");
     int launches = 0;
-    NA_CK(launch_scan(hist, nhist, offw, sums, offw + nhist, st, &launches), "scan");
-    NA_CK(launch_scan(hist + nhist, nhist, offr, sums + nsum, offr + nhist, st, &launches), "scan");
-    k_sizes<<<(p1 + 255) / 256, 256, 0, st>>>(offr, offw, p1, C, sizes, sizes + p1);
+    NA_CK(launch_scan(hist, nhist, offr, sums, offr + nhist, st, &launches), "scan");
+    k_sizes<<<(p1 + 255) / 256, 256, 0, st>>>(offr, p1, C, sizes);
     NA_CK(cudaGetLastError(), "k_sizes");
-    std::vector<unsigned long long> hsz(2 * (size_t)p1), hk(p1);
-    unsigned long long tot_w = 0, tot_r = 0, cstats[3] = {0, 0, 0};
+    std::vector<unsigned long long> hsz(p1), hk(p1);
+    unsigned long long tot_r = 0, cstats[3] = {0, 0, 0};
     uint32_t ovf = 0;
-    NA_CK(cudaMemcpyAsync(hsz.data(), sizes, (size_t)p1 * 16, cudaMemcpyDeviceToHost, st), "d2h");
+    NA_CK(cudaMemcpyAsync(hsz.data(), sizes, (size_t)p1 * 8, cudaMemcpyDeviceToHost, st), "d2h");
     NA_CK(cudaMemcpyAsync(hk.data(), bucket_kmers, (size_t)p1 * 8, cudaMemcpyDeviceToHost, st), "d2h");
-    NA_CK(cudaMemcpyAsync(&tot_w, offw + nhist, 8, cudaMemcpyDeviceToHost, st), "d2h");
     NA_CK(cudaMemcpyAsync(&tot_r, offr + nhist, 8, cudaMemcpyDeviceToHost, st), "d2h");
     NA_CK(cudaMemcpyAsync(cstats, misc, 24, cudaMemcpyDeviceToHost, st), "d2h");
     NA_CK(cudaMemcpyAsync(&ovf, overflow, 4, cudaMemcpyDeviceToHost, st), "d2h");
     NA_CK(cudaStreamSynchronize(st), "phase 1");
     if (ovf) { set_err(errbuf, errlen, "descriptor capacity exceeded"); return TG_ERR_DEVICE; }
-    // ---- records, index, per-CTA lists from what is left
-    uint32_t* records = cv.take<uint32_t>(tot_w + 16);
-    uint32_t* index = cv.take<uint32_t>(tot_r + 16);
+    // ---- bucketed descriptors and per-CTA bin lists from what is left
+    uint64_t* bdesc = cv.take<uint64_t>(tot_r + 8);
     uint64_t max_recs = 0;
     for (uint32_t b = 0; b < p1; ++b) max_recs = std::max<uint64_t>(max_recs, hsz[b]);
     const uint32_t slots = W == 1 ? 8192 : 4096;
-    const size_t smem2 = count_smem_bytes(W, slots);
-    const uint32_t per_sm2 = std::max<uint32_t>(1, std::min<uint32_t>(2, (uint32_t)(228u * 1024u / (smem2 + 1024))));
     const size_t left = cv.cap > cv.off ? cv.cap - cv.off : 0;
-    const size_t per_cta = ((max_recs + 1) * 4 + 255) & ~size_t(255);
-    uint32_t grid2 = (uint32_t)std::min<size_t>((size_t)n_sm * per_sm2, per_cta ? left / (per_cta + 256) : 1);
+    const size_t per_cta = ((max_recs + 1) * 8 + 255) & ~size_t(255);
+    uint32_t grid2 = (uint32_t)std::min<size_t>((size_t)n_sm, per_cta ? left / (per_cta + 256) : 1);
     if (grid2 == 0) grid2 = 1;
-    uint32_t* scratch = cv.take<uint32_t>((size_t)grid2 * (max_recs + 1));
+    uint64_t* scratch = cv.take<uint64_t>((size_t)grid2 * (max_recs + 1));
     if (!cv.ok) { set_err(errbuf, errlen, "input too large for the no-allocation scratch"); return TG_ERR_ARG; }
     std::vector<uint32_t> ord(p1);
     std::iota(ord.begin(), ord.end(), 0u);
     std::stable_sort(ord.begin(), ord.end(), [&](uint32_t a, uint32_t b) { return hk[a] > hk[b]; });
     NA_CK(cudaMemcpyAsync(order, ord.data(), (size_t)p1 * 4, cudaMemcpyHostToDevice, st), "h2d");
-    ScatterParams SP{};
-    SP.packed = packed; SP.k = k; SP.p1_bits = p1_bits; SP.n_cta = C; SP.chunk = chunk;
-    SP.desc = desc; SP.desc_cap = desc_cap; SP.n_desc = n_desc;
-    SP.off_w = offw; SP.off_r = offr; SP.records = records; SP.index = index;
-    NA_CK(launch_scatter(SP, st), "k_scatter");
+    BucketParams BP{};
+    BP.p1_bits = p1_bits; BP.n_cta = C; BP.desc = desc; BP.desc_cap = desc_cap; BP.n_desc = n_desc;
+    BP.off_r = offr; BP.bdesc = bdesc;
+    NA_CK(launch_bucket(BP, st), "k_bucket");
     // ---- phase 2 straight into the caller's buffers
     Phase2Params QP{};
-    QP.records = records; QP.index = index; QP.off_w = offw; QP.off_r = offr;
-    QP.n_cta1 = C; QP.n_buckets = p1; QP.order = order; QP.k = k;
-    QP.fine_bits = 24 - p1_bits; QP.target = slots / 2;
+    QP.packed = packed; QP.bdesc = bdesc; QP.off_r = offr;
+    QP.n_cta1 = C; QP.n_buckets = p1; QP.p1_bits = p1_bits; QP.order = order; QP.k = k;
+    QP.target = slots - slots * 3 / 10;
     QP.ci = o.ci; QP.cx = o.cx; QP.work = work;
     QP.scratch = scratch; QP.scratch_cap = max_recs + 1;
     QP.out_keys = d_keys; QP.out_counts = d_counts; QP.out_n = out_n; QP.out_cap = cap;
@@ -224,26 +217,24 @@ extern "C" tg_status tg_count_seq_device_noalloc(const tg_job_opts* opts, const 
         if (on[2] > 4096) { set_err(errbuf, errlen, "too many overflowing groups"); return TG_ERR_TABLE; }
         std::vector<uint32_t> fl(3 * on[2]);
         NA_CK(cudaMemcpyAsync(fl.data(), fallback, fl.size() * 4, cudaMemcpyDeviceToHost, st), "d2h");
-        std::vector<unsigned long long> ho(2 * (nhist + 1));
+        std::vector<unsigned long long> ho(nhist + 1);
         NA_CK(cudaMemcpyAsync(ho.data(), offr, (nhist + 1) * 8, cudaMemcpyDeviceToHost, st), "d2h");
-        NA_CK(cudaMemcpyAsync(ho.data() + nhist + 1, offw, (nhist + 1) * 8, cudaMemcpyDeviceToHost, st), "d2h");
         NA_CK(cudaStreamSynchronize(st), "d2h");
         const size_t fb_base = cv.off;
         for (unsigned long long i = 0; i < on[2]; ++i) {
-            const uint32_t b = fl[3 * i], g = fl[3 * i + 1], F = fl[3 * i + 2];
+            const uint32_t b = fl[3 * i], bin = fl[3 * i + 1], nbins = fl[3 * i + 2];
             uint64_t S = 1024;
             while (S < 2 * hk[b] + 2) S <<= 1;
-            cv.off = fb_base;  // groups run one after another on the stream; reuse the space
+            cv.off = fb_base;  // bins run one after another on the stream; reuse the space
             cv.ok = true;
             void* keys = cv.take<uint8_t>((size_t)S * key_bytes(W));
             uint32_t* cnt = cv.take<uint32_t>(S);
             if (!cv.ok) { set_err(errbuf, errlen, "an overflowing group does not fit in the no-allocation scratch"); return TG_ERR_TABLE; }
             FallbackParams FP{};
-            FP.records = records; FP.index = index;
-            FP.wb = ho[nhist + 1 + (uint64_t)b * C];
+            FP.packed = packed; FP.bdesc = bdesc;
             FP.r0 = ho[(uint64_t)b * C];
             FP.nrec = ho[(uint64_t)(b + 1) * C] - FP.r0;
-            FP.group = g; FP.F = F; FP.k = k; FP.keys = keys; FP.cnt = cnt;
+            FP.bin = bin; FP.nbins = nbins; FP.p1_bits = p1_bits; FP.k = k; FP.keys = keys; FP.cnt = cnt;
             FP.mask = (uint32_t)(S - 1); FP.fail = fail;
             NA_CK(launch_fallback(W, FP, S, QP, (uint32_t)n_sm * 2, st, &launches), "fallback");
         }

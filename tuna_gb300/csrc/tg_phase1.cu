@@ -1,5 +1,5 @@
 // tg_phase1.cu — Phase 1 on the GPU: 2-bit packing, superkmer cutting and the
-// scatter of superkmer records into HBM buckets.
+// bucketing of superkmer record descriptors in HBM.
 //
 // Reference behaviour (paths relative to the reference project root):
 //   ASCII -> kache 2-bit          src/partition_hash.hpp:68-70
@@ -125,14 +125,13 @@ struct BlockScan {
 
 // Shared-memory layout of k_cut, sized at launch from w and the bucket count.
 struct CutSmem {
-    size_t tables, hist_w, hist_r, hist_k, h, a, b, ev, evm, pk, vb, scan, total;
+    size_t tables, hist_r, hist_k, h, a, b, ev, evm, pk, vb, scan, total;
     int hn;
     __host__ __device__ static size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
     __host__ __device__ void layout(int w, uint32_t p1, bool exp) {
         hn = CUT_TILE + w + 2;
         size_t o = 0;
         tables = o; o = align16(o + sizeof(HashTables));
-        hist_w = o; o = align16(o + 4 * (size_t)p1);
         hist_r = o; o = align16(o + 4 * (size_t)p1);
         hist_k = o; o = align16(o + 4 * (size_t)p1);
         h = o; o = align16(o + 8 * (size_t)hn);
@@ -185,7 +184,6 @@ k_cut(CutParams P, const HashTables* __restrict__ gT) {
     CutSmem L;
     L.layout(P.w, 1u << P.p1_bits, EXPORT);
     HashTables& T = *reinterpret_cast<HashTables*>(smem + L.tables);
-    uint32_t* s_hw = reinterpret_cast<uint32_t*>(smem + L.hist_w);
     uint32_t* s_hr = reinterpret_cast<uint32_t*>(smem + L.hist_r);
     uint32_t* s_hk = reinterpret_cast<uint32_t*>(smem + L.hist_k);
     uint64_t* s_h = reinterpret_cast<uint64_t*>(smem + L.h);
@@ -213,7 +211,7 @@ k_cut(CutParams P, const HashTables* __restrict__ gT) {
         const uint64_t* src = reinterpret_cast<const uint64_t*>(gT);
         uint64_t* dst = reinterpret_cast<uint64_t*>(&T);
         for (int i = tid; i < (int)(sizeof(HashTables) / 8); i += CUT_THREADS) dst[i] = src[i];
-        for (uint32_t i = tid; i < p1; i += CUT_THREADS) { s_hw[i] = 0; s_hr[i] = 0; s_hk[i] = 0; }
+        for (uint32_t i = tid; i < p1; i += CUT_THREADS) { s_hr[i] = 0; s_hk[i] = 0; }
         if (tid == 0) { s_cs_carry = -1; s_open = -1; s_ndesc = 0; }
     }
     __syncthreads();
@@ -394,8 +392,7 @@ k_cut(CutParams P, const HashTables* __restrict__ gT) {
             if (emit) {
                 const uint32_t idx = s_ndesc + di;
                 if (idx < P.desc_cap) {
-                    P.desc[(uint64_t)c * P.desc_cap + idx] =
-                        (uint64_t)(uint32_t)(st - cstart) | ((uint64_t)nk << 32) | ((uint64_t)mlo << 40);
+                    P.desc[(uint64_t)c * P.desc_cap + idx] = desc_pack(st, nk, mlo);
                     if (EXPORT) {
                         uint64_t* x = P.xdesc + ((uint64_t)c * P.desc_cap + idx) * 3;
                         x[0] = st;
@@ -406,7 +403,6 @@ k_cut(CutParams P, const HashTables* __restrict__ gT) {
                     overflowed = true;
                 }
                 const uint32_t b = mlo & (p1 - 1);
-                atomicAdd(&s_hw[b], 1u + (nk + (uint32_t)k - 1 + 15) / 16);
                 atomicAdd(&s_hr[b], 1u);
                 atomicAdd(&s_hk[b], nk);
                 loc_kmers += nk;
@@ -435,9 +431,8 @@ k_cut(CutParams P, const HashTables* __restrict__ gT) {
     }
     // ---- flush histograms and counters
     for (uint32_t i = tid; i < p1; i += CUT_THREADS) {
-        P.hist[(uint64_t)i * P.n_cta + c] = s_hw[i];
-        P.hist[(uint64_t)p1 * P.n_cta + (uint64_t)i * P.n_cta + c] = s_hr[i];
-        if (s_hk[i]) atomicAdd(reinterpret_cast<unsigned long long*>(P.hist + 2ull * p1 * P.n_cta) + i,
+        P.hist[(uint64_t)i * P.n_cta + c] = s_hr[i];
+        if (s_hk[i]) atomicAdd(reinterpret_cast<unsigned long long*>(P.hist + hist_kmers_offset(p1, P.n_cta)) + i,
                                (unsigned long long)s_hk[i]);
     }
     if (tid == 0) P.n_desc[c] = s_ndesc;
@@ -507,50 +502,25 @@ __global__ void k_scan_add(unsigned long long* __restrict__ out, uint64_t n, con
     if (i < n) out[i] += sums[i / SCAN_ITEMS];
 }
 
-// ---------------------------------------------------------------- scatter
-// One CTA per Phase-1 chunk: its descriptors become bucket records
-// [hdr = nk | fine << 8][packed words], and their offsets go to the index.
-constexpr int SCAT_THREADS = 256;
+// ---------------------------------------------------------------- buckets
+// One CTA per Phase-1 chunk: its descriptors go to their bucket's range of
+// the bucket-major array (one 8-byte store each).
+constexpr int BUCKET_THREADS = 1024;
 
-__global__ void __launch_bounds__(SCAT_THREADS)
-k_scatter(ScatterParams P) {
-    extern __shared__ __align__(16) uint32_t cur[];  // [2][p1]
+__global__ void __launch_bounds__(BUCKET_THREADS)
+k_bucket(BucketParams P) {
+    extern __shared__ __align__(16) uint32_t cur[];  // [p1]
     const uint32_t p1 = 1u << P.p1_bits;
-    uint32_t* cw = cur;
-    uint32_t* cr = cur + p1;
-    for (uint32_t i = threadIdx.x; i < p1; i += SCAT_THREADS) { cw[i] = 0; cr[i] = 0; }
+    for (uint32_t i = threadIdx.x; i < p1; i += BUCKET_THREADS) cur[i] = 0;
     __syncthreads();
     const uint32_t c = blockIdx.x;
-    const uint32_t nd = min((uint64_t)P.n_desc[c], P.desc_cap);
-    const uint64_t cstart = (uint64_t)c * P.chunk;
-    const int k = P.k;
-    for (uint32_t i = threadIdx.x; i < nd; i += SCAT_THREADS) {
-        const uint64_t d = P.desc[(uint64_t)c * P.desc_cap + i];
-        const uint64_t st = cstart + (uint32_t)d;
-        const uint32_t nk = (uint32_t)(d >> 32) & 0xFFu;
-        const uint32_t mlo = (uint32_t)(d >> 40);
-        const uint32_t b = mlo & (p1 - 1);
-        const uint32_t fine = mlo >> P.p1_bits;
-        const uint32_t len = nk + (uint32_t)k - 1;
-        const uint32_t nw = (len + 15) / 16;
-        const uint32_t wo = atomicAdd(&cw[b], 1u + nw);
-        const uint32_t ro = atomicAdd(&cr[b], 1u);
-        const uint64_t bucket0 = P.off_w[(uint64_t)b * P.n_cta];
-        const uint64_t wabs = P.off_w[(uint64_t)b * P.n_cta + c] + wo;
-        const uint64_t rabs = P.off_r[(uint64_t)b * P.n_cta + c] + ro;
-        uint32_t* rec = P.records + wabs;
-        rec[0] = nk | (fine << 8);
-        const uint64_t a = st + TG_PAD;
-        const uint64_t w0 = a >> 4;
-        const uint32_t o = (uint32_t)(a & 15);
-        for (uint32_t j = 0; j < nw; ++j) {
-            uint32_t v = P.packed[w0 + j];
-            if (o) v = (v << (2 * o)) | (P.packed[w0 + j + 1] >> (32 - 2 * o));
-            const uint32_t left = len - 16 * j;  // bases of this word still in the record
-            if (left < 16) v &= ~0u << (32 - 2 * left);
-            rec[1 + j] = v;
-        }
-        P.index[rabs] = (uint32_t)(wabs - bucket0);
+    const uint32_t nd = (uint32_t)min((uint64_t)P.n_desc[c], P.desc_cap);
+    const uint64_t* src = P.desc + (uint64_t)c * P.desc_cap;
+    for (uint32_t i = threadIdx.x; i < nd; i += BUCKET_THREADS) {
+        const uint64_t d = __ldcs(src + i);
+        const uint32_t b = desc_mlo(d) & (p1 - 1);
+        const uint32_t o = atomicAdd(&cur[b], 1u);
+        P.bdesc[P.off_r[(uint64_t)b * P.n_cta + c] + o] = d;
     }
 }
 
@@ -595,11 +565,11 @@ cudaError_t launch_scan(const uint32_t* in, uint64_t n, unsigned long long* out,
     return cudaGetLastError();
 }
 
-cudaError_t launch_scatter(const ScatterParams& P, cudaStream_t st) {
-    const size_t sm = 2 * 4 * (size_t)(1u << P.p1_bits);
-    cudaError_t e = cudaFuncSetAttribute(k_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+cudaError_t launch_bucket(const BucketParams& P, cudaStream_t st) {
+    const size_t sm = 4 * (size_t)(1u << P.p1_bits);
+    cudaError_t e = cudaFuncSetAttribute(k_bucket, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    k_scatter<<<P.n_cta, SCAT_THREADS, sm, st>>>(P);
+    k_bucket<<<P.n_cta, BUCKET_THREADS, sm, st>>>(P);
     return cudaGetLastError();
 }
 
