@@ -90,8 +90,8 @@ typedef struct {
     uint64_t distinct;        /* distinct canonical k-mers before ci/cx */
     uint64_t out;             /* k-mers after ci/cx (reference's unique_kmers:) */
     uint32_t gpu_parts;       /* internal bucket count used */
-    uint32_t fine_groups_max; /* largest fine split of one bucket */
-    uint64_t fallback_groups; /* groups counted in a global-memory table */
+    uint32_t heavy_groups;    /* phase-2 groups larger than one table's target */
+    uint64_t fallback_groups; /* key ranges counted in a global-memory table */
     double h2d_ms;            /* host->device copy time of the input */
     double pack_ms;           /* device time: 2-bit packing */
     double phase1_ms;         /* device time: minimizers, superkmers, buckets */
@@ -101,7 +101,9 @@ typedef struct {
     double phase1_scatter_ms; /* part of phase1_ms: the bucket scatter kernel */
     uint64_t record_bytes;    /* bytes of bucket records written */
     uint64_t gpu_launches;    /* kernels launched by the last tg_job_run */
-    double phase2_count_ms;   /* part of phase2_ms: the shared-memory counting kernel */
+    double phase2_count_ms;   /* part of phase2_ms: the shared-memory counting kernel(s) */
+    double phase2_keys_ms;    /* part of phase2_ms: bin histogram, group plan, key array */
+    uint64_t groups;          /* phase-2 groups (runs of minimizer bins counted in one table) */
 } tg_stats;
 
 /* Output formats of tg_job_drain. */

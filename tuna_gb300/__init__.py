@@ -53,12 +53,13 @@ class _JobOpts(ctypes.Structure):
 class _Stats(ctypes.Structure):
     _fields_ = [("input_bytes", ctypes.c_uint64), ("bases", ctypes.c_uint64), ("runs", ctypes.c_uint64),
                 ("kmers", ctypes.c_uint64), ("superkmers", ctypes.c_uint64), ("distinct", ctypes.c_uint64),
-                ("out", ctypes.c_uint64), ("gpu_parts", ctypes.c_uint32), ("fine_groups_max", ctypes.c_uint32),
+                ("out", ctypes.c_uint64), ("gpu_parts", ctypes.c_uint32), ("heavy_groups", ctypes.c_uint32),
                 ("fallback_groups", ctypes.c_uint64), ("h2d_ms", ctypes.c_double), ("pack_ms", ctypes.c_double),
                 ("phase1_ms", ctypes.c_double), ("phase2_ms", ctypes.c_double), ("d2h_ms", ctypes.c_double),
                 ("phase1_cut_ms", ctypes.c_double), ("phase1_scatter_ms", ctypes.c_double),
                 ("record_bytes", ctypes.c_uint64), ("gpu_launches", ctypes.c_uint64),
-                ("phase2_count_ms", ctypes.c_double)]
+                ("phase2_count_ms", ctypes.c_double), ("phase2_keys_ms", ctypes.c_double),
+                ("groups", ctypes.c_uint64)]
 
     def as_dict(self) -> Dict[str, float]:
         return {f: getattr(self, f) for f, _ in self._fields_}

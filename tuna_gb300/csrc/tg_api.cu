@@ -8,8 +8,12 @@
 //   k_scan_*    exclusive scan of the histogram -> bucket offsets
 //   k_sizes     per-bucket descriptor counts (sizing; one host sync here)
 //   k_bucket    descriptors -> bucket-major order
-//   k_count     per bucket: bin split, shared-memory counting, ci/cx, compaction
-//   k_fb_*      (rare) bins that overflowed shared memory, global tables
+//   k_binhist   k-mer instances per minimizer bin of each slice of a bucket
+//   k_binscan   key offsets per (slice, bin); groups of whole bins
+//   k_keys      every canonical k-mer key, bin-major
+//   k_count     per group: keys streamed by bulk copies into a shared-memory
+//               table, ci/cx, compaction (again for groups split by key hash)
+//   k_fb_*      (rare) key ranges that overflowed shared memory, global tables
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -91,9 +95,6 @@ uint32_t next_pow2_u32(uint64_t v) {
 constexpr size_t MISC_CUT_STATS = 0;    // u64[3]: k-mers, records, runs (k_cut)
 constexpr size_t MISC_BASES = 24;       // u64: ACGT bases (k_pack)
 constexpr size_t MISC_OVERFLOW = 32;    // u32: descriptor list overflow (k_cut)
-constexpr size_t MISC_OUT = 64;         // u64[3]: output cursor, distinct, fallback groups (k_count)
-constexpr size_t MISC_WORK = 96;        // u32: bucket queue head (k_count)
-constexpr size_t MISC_FAIL = 100;       // u32: fallback table overflow
 constexpr size_t MISC_NDESC = 256;      // u32[C]: descriptors per Phase-1 CTA
 constexpr size_t MISC_BYTES = MISC_NDESC + 4 * 65536;
 
@@ -111,7 +112,7 @@ struct tg_ctx {
     unsigned host_threads = 1;
     std::string err;
     DevBuf seq, packed, valid, desc, xdesc, hist, offr, sums, sizes, records, scratch, okeys, ocnt,
-        misc, fallback, fbtab, order, tables;
+        misc, fbtab, tables;
     cudaEvent_t ev[12] = {};
     tg_job* active = nullptr;
     int prepared_m = -1;
@@ -203,8 +204,7 @@ tg_status tg_ctx_destroy(tg_ctx* ctx) {
     if (ctx->st) cudaStreamSynchronize(ctx->st);
     DevBuf* bufs[] = {&ctx->seq, &ctx->packed, &ctx->valid, &ctx->desc, &ctx->xdesc, &ctx->hist,
                       &ctx->offr, &ctx->sums, &ctx->sizes, &ctx->records, &ctx->scratch,
-                      &ctx->okeys, &ctx->ocnt, &ctx->misc, &ctx->fallback, &ctx->fbtab, &ctx->order,
-                      &ctx->tables};
+                      &ctx->okeys, &ctx->ocnt, &ctx->misc, &ctx->fbtab, &ctx->tables};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
     for (auto& e : ctx->ev)
@@ -436,24 +436,26 @@ tg_status tg_job_run(tg_job* j) {
     CK(cudaMemcpyAsync(hk.data(), bucket_kmers, (size_t)p1 * 8, cudaMemcpyDeviceToHost, ctx->st), "d2h");
     CK(cudaMemcpyAsync(&tot_r, ctx->offr.as<unsigned long long>() + nhist, 8, cudaMemcpyDeviceToHost, ctx->st), "d2h");
     CK(cudaStreamSynchronize(ctx->st), "phase 1");
-    // ---- buffers: bucketed descriptors, per-CTA bin lists, output
-    uint64_t max_recs = 0;
-    for (uint32_t b = 0; b < p1; ++b) max_recs = std::max<uint64_t>(max_recs, hsz[b]);
+    // ---- buffers: bucketed descriptors, phase-2 scratch (keys included), output
     const uint64_t n_kmers = cstats[0];
     CK(ctx->ensure(ctx->records, tot_r * 8 + 64), "alloc bucket descriptors");
-    const uint32_t slots = W == 1 ? 8192 : 4096;
-    const uint32_t grid2 = (uint32_t)ctx->n_sm;  // k_count runs one 512-thread CTA per SM
-    CK(ctx->ensure(ctx->scratch, (size_t)grid2 * (max_recs + 1) * 8), "alloc scratch");
     const uint64_t out_cap = std::max<uint64_t>(n_kmers, 1);
     CK(ctx->ensure(ctx->okeys, out_cap * key_bytes(W)), "alloc output keys");
     CK(ctx->ensure(ctx->ocnt, out_cap * 4), "alloc output counts");
-    CK(ctx->ensure(ctx->fallback, 4096 * 12), "alloc fallback list");
-    // bucket order: most k-mers first
-    std::vector<uint32_t> order(p1);
-    std::iota(order.begin(), order.end(), 0u);
-    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return hk[a] > hk[b]; });
-    CK(ctx->ensure(ctx->order, (size_t)p1 * 4), "alloc order");
-    CK(cudaMemcpyAsync(ctx->order.p, order.data(), (size_t)p1 * 4, cudaMemcpyHostToDevice, ctx->st), "h2d");
+    P2Input in{};
+    in.W = W;
+    in.k = k;
+    in.p1 = p1;
+    in.p1_bits = p1_bits;
+    in.n_sm = (uint32_t)ctx->n_sm;
+    in.packed = ctx->packed.as<uint32_t>();
+    in.bdesc = ctx->records.as<uint64_t>();
+    in.recs = hsz.data();
+    in.kmers = hk.data();
+    in.ci = j->o.ci;
+    in.cx = j->o.cx;
+    const size_t p2_bytes = phase2_scratch_bytes(in);
+    CK(ctx->ensure(ctx->scratch, p2_bytes), "alloc phase-2 scratch");
     // ---- descriptors into bucket order
     BucketParams BP{};
     BP.p1_bits = p1_bits;
@@ -468,81 +470,20 @@ tg_status tg_job_run(tg_job* j) {
     ++launches;
     CK(cudaEventRecord(ctx->ev[6], ctx->st), "event");
     // ---- phase 2
-    unsigned long long* out_n = reinterpret_cast<unsigned long long*>(ctx->misc.as<uint8_t>() + MISC_OUT);
-    uint32_t* work = reinterpret_cast<uint32_t*>(ctx->misc.as<uint8_t>() + MISC_WORK);
-    CK(cudaMemsetAsync(out_n, 0, 24, ctx->st), "memset");
-    CK(cudaMemsetAsync(work, 0, 4, ctx->st), "memset");
-    Phase2Params QP{};
-    QP.packed = ctx->packed.as<uint32_t>();
-    QP.bdesc = ctx->records.as<uint64_t>();
-    QP.off_r = ctx->offr.as<unsigned long long>();
-    QP.n_cta1 = C;
-    QP.n_buckets = p1;
-    QP.p1_bits = p1_bits;
-    QP.order = ctx->order.as<uint32_t>();
-    QP.k = k;
-    QP.target = slots - slots * 3 / 10;
-    QP.ci = j->o.ci;
-    QP.cx = j->o.cx;
-    QP.work = work;
-    QP.scratch = ctx->scratch.as<uint64_t>();
-    QP.scratch_cap = max_recs + 1;
-    QP.out_keys = ctx->okeys.p;
-    QP.out_counts = ctx->ocnt.as<uint32_t>();
-    QP.out_n = out_n;
-    QP.out_cap = out_cap;
-    QP.fallback = ctx->fallback.as<uint32_t>();
-    QP.fallback_cap = 4096;
-    QP.bucket_kmers = bucket_kmers;
-    QP.smem_slots = slots;
-    CK(launch_count(W, QP, grid2, ctx->st), "k_count");
-    ++launches;
-    CK(cudaEventRecord(ctx->ev[7], ctx->st), "event");
-    unsigned long long on[3] = {0, 0, 0};
-    CK(cudaMemcpyAsync(on, out_n, 24, cudaMemcpyDeviceToHost, ctx->st), "d2h");
-    CK(cudaStreamSynchronize(ctx->st), "phase 2");
-    // ---- bins that did not fit in shared memory
-    if (on[2] > 0) {
-        if (on[2] > 4096) return ctx->fail(TG_ERR_TABLE, "too many overflowing groups");
-        std::vector<uint32_t> fl(3 * on[2]);
-        CK(cudaMemcpy(fl.data(), ctx->fallback.p, fl.size() * 4, cudaMemcpyDeviceToHost), "d2h");
-        for (unsigned long long i = 0; i < on[2]; ++i) {
-            const uint32_t b = fl[3 * i], bin = fl[3 * i + 1], nbins = fl[3 * i + 2];
-            unsigned long long r01[2];
-            CK(cudaMemcpy(&r01[0], ctx->offr.as<unsigned long long>() + (uint64_t)b * C, 8, cudaMemcpyDeviceToHost), "d2h");
-            CK(cudaMemcpy(&r01[1], ctx->offr.as<unsigned long long>() + (uint64_t)(b + 1) * C, 8, cudaMemcpyDeviceToHost), "d2h");
-            uint64_t S = 1024;
-            while (S < 2 * hk[b] + 2) S <<= 1;
-            if (S > (1ull << 32)) return ctx->fail(TG_ERR_TABLE, "fallback table too large");
-            const size_t kbytes = (size_t)S * key_bytes(W);
-            CK(ctx->ensure(ctx->fbtab, kbytes + (size_t)S * 4 + 16), "alloc fallback table");
-            FallbackParams FP{};
-            FP.packed = ctx->packed.as<uint32_t>();
-            FP.bdesc = ctx->records.as<uint64_t>();
-            FP.r0 = r01[0];
-            FP.nrec = r01[1] - r01[0];
-            FP.bin = bin;
-            FP.nbins = nbins;
-            FP.p1_bits = p1_bits;
-            FP.k = k;
-            FP.keys = ctx->fbtab.p;
-            FP.cnt = reinterpret_cast<uint32_t*>(ctx->fbtab.as<uint8_t>() + kbytes);
-            FP.mask = (uint32_t)(S - 1);
-            FP.fail = reinterpret_cast<uint32_t*>(ctx->misc.as<uint8_t>() + MISC_FAIL);
-            CK(cudaMemsetAsync(FP.fail, 0, 4, ctx->st), "memset");
-            CK(launch_fallback(W, FP, S, QP, (uint32_t)ctx->n_sm * 4, ctx->st, &launches), "fallback");
-            uint32_t failed = 0;
-            CK(cudaMemcpyAsync(&failed, FP.fail, 4, cudaMemcpyDeviceToHost, ctx->st), "d2h");
-            CK(cudaStreamSynchronize(ctx->st), "fallback");
-            if (failed) return ctx->fail(TG_ERR_TABLE, "fallback table overflow");
-        }
-        CK(cudaMemcpyAsync(on, out_n, 16, cudaMemcpyDeviceToHost, ctx->st), "d2h");
-        CK(cudaStreamSynchronize(ctx->st), "fallback");
-    }
+    P2Output out{};
+    out.keys = ctx->okeys.p;
+    out.counts = ctx->ocnt.as<uint32_t>();
+    out.cap = out_cap;
+    std::string msg;
+    auto fallback_table = [&](size_t bytes) -> void* {
+        return ctx->ensure(ctx->fbtab, bytes) == cudaSuccess ? ctx->fbtab.p : nullptr;
+    };
+    const tg_status ps = phase2_run(in, ctx->scratch.p, p2_bytes, out, fallback_table, ctx->st, ctx->ev[7],
+                                    &launches, msg);
+    if (ps != TG_OK) return ctx->fail(ps, msg);
     CK(cudaEventRecord(ctx->ev[8], ctx->st), "event");
     CK(cudaEventSynchronize(ctx->ev[8]), "sync");
-    if (on[0] > out_cap) return ctx->fail(TG_ERR_TABLE, "output capacity exceeded");
-    j->n_out = on[0];
+    j->n_out = out.n_out;
     // ---- stats
     float ms = 0;
     tg_stats& S = j->st;
@@ -550,10 +491,12 @@ tg_status tg_job_run(tg_job* j) {
     S.runs = cstats[2];
     S.kmers = cstats[0];
     S.superkmers = cstats[1];
-    S.distinct = on[1];
-    S.out = on[0];
+    S.distinct = out.distinct;
+    S.out = out.n_out;
     S.gpu_parts = p1;
-    S.fallback_groups = on[2];
+    S.fallback_groups = out.fallback_groups;
+    S.groups = out.groups;
+    S.heavy_groups = (uint32_t)out.heavy_groups;
     S.record_bytes = tot_r * 8;
     cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]); S.pack_ms = ms;
     cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]); S.phase1_cut_ms = ms;
@@ -562,11 +505,9 @@ tg_status tg_job_run(tg_job* j) {
     cudaEventElapsedTime(&ms, ctx->ev[5], ctx->ev[6]); S.phase1_scatter_ms = ms;
     S.phase1_ms = S.phase1_cut_ms + scan_ms + S.phase1_scatter_ms;
     cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[8]); S.phase2_ms = ms;
-    cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]); S.phase2_count_ms = ms;
+    cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]); S.phase2_keys_ms = ms;
+    cudaEventElapsedTime(&ms, ctx->ev[7], ctx->ev[8]); S.phase2_count_ms = ms;
     S.gpu_launches = (uint64_t)launches;
-    uint64_t kmax = 0;
-    for (uint32_t b = 0; b < p1; ++b) kmax = std::max<uint64_t>(kmax, hk[b]);
-    S.fine_groups_max = (uint32_t)((kmax + QP.target - 1) / QP.target);
     return TG_OK;
 }
 

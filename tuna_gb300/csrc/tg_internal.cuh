@@ -12,6 +12,8 @@
 //                            minimizer hash; see desc_pack)
 //   hist    u32[P][C]        records per (bucket, CTA), then u64[P] k-mers per bucket
 //   bdesc   u64[]            the descriptors again, bucket-major (phase 2 input)
+//   keys    u64 x W [K]      every canonical k-mer instance, bucket-major and, inside
+//                            a bucket, grouped by minimizer bin (W = 1 for k <= 31)
 //   out     keys + u32 counts of the distinct k-mers that pass ci/cx
 #pragma once
 #include <cstdint>
@@ -85,40 +87,72 @@ struct BucketParams {
     uint64_t* bdesc;                   // descriptors in bucket order
 };
 
-struct Phase2Params {
+// Phase 2 works on slices of the bucket-major descriptors (one slice never
+// spans two buckets) and on groups: runs of whole minimizer bins of one bucket
+// whose keys are contiguous in the key array.
+struct Slice {
+    uint64_t r_lo, r_hi;  // descriptor range in bdesc
+    uint32_t bucket, pad;
+};
+
+struct Group {
+    unsigned long long lo, hi;  // key range [lo, hi)
+    uint32_t parts, part;       // count only the keys whose hash part is `part` of `parts`
+    uint32_t pad[2];
+};
+
+// Counters of one Phase-2 run (device, u64 each).
+enum P2Counter : int {
+    P2C_NORMAL = 0,   // groups of at most `target` k-mers
+    P2C_HEAVY,        // groups larger than `target`
+    P2C_WORK,         // next group of the current k_count launch
+    P2C_RETRY,        // groups pushed back for another pass with more parts
+    P2C_FALLBACK,     // key ranges left to the global-memory table
+    P2C_OUT,          // output cursor
+    P2C_DISTINCT,     // distinct keys seen
+    P2C_COUNT
+};
+
+struct KeysParams {
     const uint32_t* packed;
-    const uint64_t* bdesc;             // descriptors in bucket order
-    const unsigned long long* off_r;   // [P][C] + total (bucket start = off_r[p*C])
-    uint32_t n_cta1;                   // C of phase 1
-    uint32_t n_buckets;
-    uint32_t p1_bits;
-    const uint32_t* order;             // bucket processing order
-    int k;
+    const uint64_t* bdesc;
+    const Slice* slices;
+    const uint32_t* slice_first;       // [P + 1] first slice of each bucket
+    const unsigned long long* kbase;   // [P + 1] first key of each bucket
+    uint32_t* shist;                   // [n_slices][nb]: k-mers per bin, then key offsets
+    uint32_t p1_bits, nb;              // nb = bins per bucket
     uint32_t target;                   // k-mer instances per group
+    int k;
+    void* keys;                        // u64 x W per k-mer instance, bin-major per bucket
+    Group* groups[2];                  // [0] normal, [1] heavy
+    uint64_t groups_cap;
+    unsigned long long* ctr;           // P2Counter
+};
+
+struct CountParams {
+    const void* keys;
+    const Group* list[2];              // processed in order: list[1] first, then list[0]
+    const unsigned long long* n_list;  // [0] entries of list[0], [1] of list[1]
+    Group* retry;                      // failed groups, split in two
+    unsigned long long* n_retry;
+    uint64_t retry_cap;
+    Group* fallback;
+    uint64_t fallback_cap;
     uint64_t ci, cx;
-    uint32_t* work;                    // [0] next bucket
-    uint64_t* scratch;                 // [n_cta2][scratch_cap] descriptors sorted by bin
-    uint64_t scratch_cap;
-    void* out_keys;                    // u64 x W per k-mer
+    void* out_keys;                    // u64 x W per distinct k-mer
     uint32_t* out_counts;
-    unsigned long long* out_n;         // [0] out cursor, [1] distinct, [2] fallback groups
     uint64_t out_cap;
-    uint32_t* fallback;                // [cap][3]: bucket, bin, bins
-    uint32_t fallback_cap;
-    const unsigned long long* bucket_kmers;  // per bucket k-mer instances
+    unsigned long long* ctr;           // P2Counter
     uint32_t smem_slots;               // table capacity in shared memory
 };
 
-// A bin that did not fit in shared memory, counted in a global table.
+// A key range that did not fit in shared memory, counted in a global table.
 struct FallbackParams {
-    const uint32_t* packed;
-    const uint64_t* bdesc;
-    uint64_t r0, nrec;    // the bucket's descriptor range
-    uint32_t bin, nbins;  // bin of the overflowing group, bins of its bucket
-    uint32_t p1_bits;
-    int k;
-    void* keys;           // S slots
-    uint32_t* cnt;
+    const void* keys;
+    unsigned long long lo, hi;
+    uint32_t parts, part;
+    void* tkeys;          // S slots
+    uint32_t* tcnt;
     uint32_t mask;
     uint32_t* fail;
 };
@@ -189,13 +223,10 @@ __device__ __forceinline__ void nt_roll(const HashTables& T, uint32_t out, uint3
 // ---------------------------------------------------------------- k-mer keys
 // Reverse complement of a k-mer held in the low 2k bits (k <= 32).
 __device__ __forceinline__ uint64_t revcomp64(uint64_t x, int k) {
-    x = ~x;
-    // reverse the order of 2-bit groups
-    x = ((x >> 2) & 0x3333333333333333ull) | ((x & 0x3333333333333333ull) << 2);
-    x = ((x >> 4) & 0x0F0F0F0F0F0F0F0Full) | ((x & 0x0F0F0F0F0F0F0F0Full) << 4);
-    x = ((x >> 8) & 0x00FF00FF00FF00FFull) | ((x & 0x00FF00FF00FF00FFull) << 8);
-    x = ((x >> 16) & 0x0000FFFF0000FFFFull) | ((x & 0x0000FFFF0000FFFFull) << 16);
-    x = (x >> 32) | (x << 32);
+    // complement = ~code; a full bit reversal reverses the 2-bit groups and
+    // swaps the two bits inside each group, which the last step swaps back
+    x = __brevll(~x);
+    x = ((x >> 1) & 0x5555555555555555ull) | ((x & 0x5555555555555555ull) << 1);
     return x >> (64 - 2 * k);
 }
 

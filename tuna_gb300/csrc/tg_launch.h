@@ -3,6 +3,11 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <functional>
+#include <string>
+
+#include "tuna_gpu.h"
+
 #include "tg_internal.cuh"
 
 namespace tg {
@@ -13,11 +18,35 @@ cudaError_t launch_cut(const CutParams& P, const HashTables* gT, bool exp, cudaS
 cudaError_t launch_scan(const uint32_t* in, uint64_t n, unsigned long long* out, unsigned long long* sums,
                         unsigned long long* total, cudaStream_t st, int* launches);
 cudaError_t launch_bucket(const BucketParams& P, cudaStream_t st);
-size_t count_smem_bytes(int W, uint32_t slots);
 size_t key_bytes(int W);
-cudaError_t launch_count(int W, const Phase2Params& P, uint32_t grid, cudaStream_t st);
-cudaError_t launch_fallback(int W, const FallbackParams& F, uint64_t S, const Phase2Params& P, uint32_t grid,
-                            cudaStream_t st, int* launches);
+uint32_t count_slots(int W);
+
+// Phase 2 of one job, shared by the entry points: bucket-major descriptors in,
+// distinct keys and counts out.
+struct P2Input {
+    int W, k;                          // key words, k
+    uint32_t p1, p1_bits;              // buckets
+    uint32_t n_sm;
+    const uint32_t* packed;
+    const uint64_t* bdesc;
+    const unsigned long long* recs;    // [p1] descriptors per bucket (host)
+    const unsigned long long* kmers;   // [p1] k-mer instances per bucket (host)
+    uint64_t ci, cx;
+};
+struct P2Output {
+    void* keys;                        // u64 x W per distinct k-mer
+    uint32_t* counts;
+    uint64_t cap;
+    uint64_t n_out, distinct, groups, heavy_groups, fallback_groups;
+};
+// Device scratch one run needs (key array included).
+size_t phase2_scratch_bytes(const P2Input& in);
+// Runs phase 2 on `st` and waits for it. fallback_table(bytes) returns device
+// memory for a global table (or null); ev_keys (optional) is recorded once the
+// keys are written.
+tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Output& out,
+                     const std::function<void*(size_t)>& fallback_table, cudaStream_t st, cudaEvent_t ev_keys,
+                     int* launches, std::string& err);
 
 // ntHash roll / init tables for minimizer length m (host side).
 HashTables make_hash_tables(int m);

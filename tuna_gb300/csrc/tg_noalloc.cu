@@ -9,7 +9,7 @@
 // synchronise the device. tg_count_seq_device_noalloc takes the input and the
 // output buffers from the caller and keeps every intermediate array (packed
 // bases, superkmer descriptors, histograms, bucket offsets, bucketed
-// descriptors, per-CTA bin lists, fallback table) in one file-scope device array of
+// descriptors, k-mer keys, group lists, fallback table) in one file-scope device array of
 // TG_NOALLOC_SCRATCH_BYTES that the CUDA runtime reserves when the library is
 // loaded on a device and that stays reserved until the process exits.
 //
@@ -144,15 +144,9 @@ extern "C" tg_status tg_count_seq_device_noalloc(const tg_job_opts* opts, const 
     const uint64_t nsum = (nhist + 8191) / 8192 + 1;
     unsigned long long* sums = cv.take<unsigned long long>(nsum + 2);
     unsigned long long* sizes = cv.take<unsigned long long>(p1);
-    uint32_t* order = cv.take<uint32_t>(p1);
-    uint32_t* fallback = cv.take<uint32_t>(3 * 4096);
     if (!cv.ok) { set_err(errbuf, errlen, "input too large for the no-allocation scratch"); return TG_ERR_ARG; }
-    // counters in misc (u64 indices): [0..2] k-mers/records/runs, [3] bases,
-    // [4] overflow (u32), [8..10] out/distinct/fallback, [12] work (u32), [13] fail (u32)
+    // counters in misc (u64 indices): [0..2] k-mers/records/runs, [3] bases, [4] overflow (u32)
     uint32_t* overflow = reinterpret_cast<uint32_t*>(misc + 4);
-    unsigned long long* out_n = misc + 8;
-    uint32_t* work = reinterpret_cast<uint32_t*>(misc + 12);
-    uint32_t* fail = reinterpret_cast<uint32_t*>(misc + 13);
 
     const HashTables T = make_hash_tables(m);
     NA_CK(cudaMemcpyAsync(tables, &T, sizeof T, cudaMemcpyHostToDevice, st), "upload tables");
@@ -181,73 +175,41 @@ extern "C" tg_status tg_count_seq_device_noalloc(const tg_job_opts* opts, const 
     NA_CK(cudaMemcpyAsync(&ovf, overflow, 4, cudaMemcpyDeviceToHost, st), "d2h");
     NA_CK(cudaStreamSynchronize(st), "phase 1");
     if (ovf) { set_err(errbuf, errlen, "descriptor capacity exceeded"); return TG_ERR_DEVICE; }
-    // ---- bucketed descriptors and per-CTA bin lists from what is left
+    // ---- bucketed descriptors, then phase 2 in what is left
     uint64_t* bdesc = cv.take<uint64_t>(tot_r + 8);
-    uint64_t max_recs = 0;
-    for (uint32_t b = 0; b < p1; ++b) max_recs = std::max<uint64_t>(max_recs, hsz[b]);
-    const uint32_t slots = W == 1 ? 8192 : 4096;
-    const size_t left = cv.cap > cv.off ? cv.cap - cv.off : 0;
-    const size_t per_cta = ((max_recs + 1) * 8 + 255) & ~size_t(255);
-    uint32_t grid2 = (uint32_t)std::min<size_t>((size_t)n_sm, per_cta ? left / (per_cta + 256) : 1);
-    if (grid2 == 0) grid2 = 1;
-    uint64_t* scratch = cv.take<uint64_t>((size_t)grid2 * (max_recs + 1));
     if (!cv.ok) { set_err(errbuf, errlen, "input too large for the no-allocation scratch"); return TG_ERR_ARG; }
-    std::vector<uint32_t> ord(p1);
-    std::iota(ord.begin(), ord.end(), 0u);
-    std::stable_sort(ord.begin(), ord.end(), [&](uint32_t a, uint32_t b) { return hk[a] > hk[b]; });
-    NA_CK(cudaMemcpyAsync(order, ord.data(), (size_t)p1 * 4, cudaMemcpyHostToDevice, st), "h2d");
     BucketParams BP{};
     BP.p1_bits = p1_bits; BP.n_cta = C; BP.desc = desc; BP.desc_cap = desc_cap; BP.n_desc = n_desc;
     BP.off_r = offr; BP.bdesc = bdesc;
     NA_CK(launch_bucket(BP, st), "k_bucket");
-    // ---- phase 2 straight into the caller's buffers
-    Phase2Params QP{};
-    QP.packed = packed; QP.bdesc = bdesc; QP.off_r = offr;
-    QP.n_cta1 = C; QP.n_buckets = p1; QP.p1_bits = p1_bits; QP.order = order; QP.k = k;
-    QP.target = slots - slots * 3 / 10;
-    QP.ci = o.ci; QP.cx = o.cx; QP.work = work;
-    QP.scratch = scratch; QP.scratch_cap = max_recs + 1;
-    QP.out_keys = d_keys; QP.out_counts = d_counts; QP.out_n = out_n; QP.out_cap = cap;
-    QP.fallback = fallback; QP.fallback_cap = 4096; QP.bucket_kmers = bucket_kmers; QP.smem_slots = slots;
-    NA_CK(launch_count(W, QP, grid2, st), "k_count");
-    unsigned long long on[3] = {0, 0, 0};
-    NA_CK(cudaMemcpyAsync(on, out_n, 24, cudaMemcpyDeviceToHost, st), "d2h");
-    NA_CK(cudaStreamSynchronize(st), "phase 2");
-    if (on[2] > 0) {
-        if (on[2] > 4096) { set_err(errbuf, errlen, "too many overflowing groups"); return TG_ERR_TABLE; }
-        std::vector<uint32_t> fl(3 * on[2]);
-        NA_CK(cudaMemcpyAsync(fl.data(), fallback, fl.size() * 4, cudaMemcpyDeviceToHost, st), "d2h");
-        std::vector<unsigned long long> ho(nhist + 1);
-        NA_CK(cudaMemcpyAsync(ho.data(), offr, (nhist + 1) * 8, cudaMemcpyDeviceToHost, st), "d2h");
-        NA_CK(cudaStreamSynchronize(st), "d2h");
-        const size_t fb_base = cv.off;
-        for (unsigned long long i = 0; i < on[2]; ++i) {
-            const uint32_t b = fl[3 * i], bin = fl[3 * i + 1], nbins = fl[3 * i + 2];
-            uint64_t S = 1024;
-            while (S < 2 * hk[b] + 2) S <<= 1;
-            cv.off = fb_base;  // bins run one after another on the stream; reuse the space
-            cv.ok = true;
-            void* keys = cv.take<uint8_t>((size_t)S * key_bytes(W));
-            uint32_t* cnt = cv.take<uint32_t>(S);
-            if (!cv.ok) { set_err(errbuf, errlen, "an overflowing group does not fit in the no-allocation scratch"); return TG_ERR_TABLE; }
-            FallbackParams FP{};
-            FP.packed = packed; FP.bdesc = bdesc;
-            FP.r0 = ho[(uint64_t)b * C];
-            FP.nrec = ho[(uint64_t)(b + 1) * C] - FP.r0;
-            FP.bin = bin; FP.nbins = nbins; FP.p1_bits = p1_bits; FP.k = k; FP.keys = keys; FP.cnt = cnt;
-            FP.mask = (uint32_t)(S - 1); FP.fail = fail;
-            NA_CK(launch_fallback(W, FP, S, QP, (uint32_t)n_sm * 2, st, &launches), "fallback");
+    P2Input in{};
+    in.W = W; in.k = k; in.p1 = p1; in.p1_bits = p1_bits; in.n_sm = (uint32_t)n_sm;
+    in.packed = packed; in.bdesc = bdesc; in.recs = hsz.data(); in.kmers = hk.data();
+    in.ci = o.ci; in.cx = o.cx;
+    const size_t p2_bytes = phase2_scratch_bytes(in);
+    uint8_t* p2_scratch = cv.take<uint8_t>(p2_bytes);
+    if (!cv.ok) { set_err(errbuf, errlen, "input too large for the no-allocation scratch"); return TG_ERR_ARG; }
+    // a global table for a group that overflows shared memory: the space after
+    // the phase-2 scratch, reused by each such group in turn
+    const size_t fb_base = cv.off;
+    auto fallback_table = [&](size_t bytes) -> void* {
+        cv.off = fb_base;
+        cv.ok = true;
+        return cv.take<uint8_t>(bytes);
+    };
+    P2Output out{};
+    out.keys = d_keys; out.counts = d_counts; out.cap = cap;
+    std::string msg;
+    // straight into the caller's buffers
+    const tg_status ps = phase2_run(in, p2_scratch, p2_bytes, out, fallback_table, st, nullptr, &launches, msg);
+    *n_out = out.n_out;
+    if (ps != TG_OK) {
+        if (out.n_out > cap) {
+            set_err(errbuf, errlen, "output capacity too small: " + std::to_string(out.n_out) + " k-mers");
+            return TG_ERR_ARG;
         }
-        uint32_t failed = 0;
-        NA_CK(cudaMemcpyAsync(&failed, fail, 4, cudaMemcpyDeviceToHost, st), "d2h");
-        NA_CK(cudaMemcpyAsync(on, out_n, 16, cudaMemcpyDeviceToHost, st), "d2h");
-        NA_CK(cudaStreamSynchronize(st), "fallback");
-        if (failed) { set_err(errbuf, errlen, "fallback table overflow"); return TG_ERR_TABLE; }
-    }
-    *n_out = on[0];
-    if (on[0] > cap) {
-        set_err(errbuf, errlen, "output capacity too small: " + std::to_string(on[0]) + " k-mers");
-        return TG_ERR_ARG;
+        set_err(errbuf, errlen, msg);
+        return ps;
     }
 #undef NA_CK
     return TG_OK;

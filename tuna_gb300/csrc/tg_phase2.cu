@@ -10,23 +10,34 @@
 //   count += 1 per instance       src/count.hpp:81, Streaming_Kmer_Hash_Table::upsert
 //   keep ci <= count <= cx        src/count.hpp:202, :250, :287
 //
-// One CTA takes one bucket at a time from a size-ordered queue. A bucket whose
-// k-mer instances exceed what one shared-memory table holds is split by further
-// bits of the minimizer hash (each descriptor's bin) into groups of contiguous
-// bins; all occurrences of a canonical k-mer share its minimizer, so they land
-// in the same group. Each group is counted in a shared-memory open-addressing
-// table (64-bit CAS insert for k <= 31, 128-bit CAS for k <= 63, u32 atomicAdd
-// counts). A group that overflows is halved; a single bin that still overflows
-// is left to the global-memory table of k_fb_insert.
-#include "tg_internal.cuh"
+// Pipeline (all instances of a canonical k-mer share its minimizer, hence its
+// bucket and its bin = further bits of the minimizer hash):
+//   k_binhist   per slice of a bucket's descriptors: k-mer instances per bin
+//   k_binscan   per bucket: key offset of every (slice, bin); greedy runs of
+//               whole bins of at most `target` k-mers become groups
+//   k_keys      per slice: every k-mer's canonical key, written bin-major, so
+//               the keys of a group are one contiguous range of the key array
+//   k_count     persistent, one CTA per SM: each group's keys are read with
+//               coalesced loads (the next round's already in flight while one
+//               is counted) into a shared-memory open-addressing table, then
+//               filtered and compacted.
+//               A group with more distinct keys than the table holds comes back
+//               as its two key-hash halves in the next launch; past MAX_PARTS
+//               parts it goes to the global-memory table (k_fb_*).
+#include <algorithm>
+#include <vector>
+
+#include "tg_launch.h"
 
 namespace tg {
 
-constexpr int P2_THREADS = 1024;
-constexpr uint32_t NBINS = 1024;         // minimizer-bit bins per bucket for the group split
+constexpr int P2_THREADS = 1024;         // threads of the phase-2 CTAs
+constexpr uint32_t NBINS = 1024;         // minimizer-bit bins per bucket (at most)
 constexpr uint32_t PROBE_LIMIT = 128;    // linear-probe steps before a group is split
-constexpr uint32_t MAX_PARTS = 4096;     // key-hash passes over one bin before the global table
-constexpr int UNROLL = 4;                // k-mers per lane per round of k_count
+constexpr uint32_t MAX_PARTS = 64;       // key-hash parts of one range before the global table
+constexpr uint32_t SLICE_DESC = 65536;   // descriptors per slice
+constexpr int KEYS_UNROLL = 4;           // k-mers per lane in flight in k_keys
+constexpr uint64_t FALLBACK_CAP = 4096;
 
 struct __align__(16) U128 {
     unsigned long long lo, hi;
@@ -45,7 +56,7 @@ struct KeyOps<1> {
     __device__ static uint64_t hash(const Key& k) { return mix_key1(k); }
     __device__ static Key load(const Key* p) { return *reinterpret_cast<const volatile Key*>(p); }
     __device__ static Key cas(Key* p, const Key& cmp, const Key& val) { return atomicCAS(p, cmp, val); }
-    __device__ static void store_out(void* out, uint64_t i, const Key& k) {
+    __device__ static void store(void* out, uint64_t i, const Key& k) {
         reinterpret_cast<unsigned long long*>(out)[i] = k;
     }
 };
@@ -63,10 +74,16 @@ struct KeyOps<2> {
         Key k; k.lo = q[0]; k.hi = q[1]; return k;
     }
     __device__ static Key cas(Key* p, const Key& cmp, const Key& val) { return atomicCAS(p, cmp, val); }
-    __device__ static void store_out(void* out, uint64_t i, const Key& k) {
+    __device__ static void store(void* out, uint64_t i, const Key& k) {
         reinterpret_cast<U128*>(out)[i] = k;
     }
 };
+
+// Key-hash part of a key (hash bits apart from the table's slot bits).
+template <int W>
+__device__ __forceinline__ uint32_t key_part(const typename KeyOps<W>::Key& key, uint32_t parts) {
+    return (uint32_t)(KeyOps<W>::hash(key) >> 8) & (parts - 1);
+}
 
 // Insert one k-mer instance: count += 1. False if `limit` slots were taken.
 // 64-bit keys are probed with a plain load and claimed with a CAS. A 128-bit
@@ -136,58 +153,10 @@ __device__ __forceinline__ U128 kmer_key<2>(const uint32_t* __restrict__ pk, uin
     return key;
 }
 
-// Add one k-mer instance. Returns 1 and the slot when the key claimed a new
-// slot (the caller appends it to the used list), 0 when the key was already
-// present, -1 when `limit` probes found no place (the group must be split).
-template <int W>
-__device__ __forceinline__ int tbl_claim(typename KeyOps<W>::Key* keys, uint32_t* cnt, uint32_t mask,
-                                         const typename KeyOps<W>::Key& key, uint32_t limit, uint32_t& slot) {
-    using O = KeyOps<W>;
-    uint32_t h = (uint32_t)(O::hash(key) >> 32) & mask;
-    for (uint32_t p = 0; p < limit; ++p) {
-        if constexpr (W == 1) {
-            const typename O::Key cur = O::load(&keys[h]);
-            if (O::eq(cur, key)) { atomicAdd(&cnt[h], 1u); return 0; }
-            if (O::is_empty(cur)) {
-                const typename O::Key prev = O::cas(&keys[h], O::empty(), key);
-                if (O::is_empty(prev)) { atomicAdd(&cnt[h], 1u); slot = h; return 1; }
-                if (O::eq(prev, key)) { atomicAdd(&cnt[h], 1u); return 0; }
-            }
-        } else {
-            const typename O::Key prev = O::cas(&keys[h], O::empty(), key);
-            if (O::is_empty(prev)) { atomicAdd(&cnt[h], 1u); slot = h; return 1; }
-            if (O::eq(prev, key)) { atomicAdd(&cnt[h], 1u); return 0; }
-        }
-        h = (h + 1) & mask;
-    }
-    return -1;
-}
-
-template <int W>
-struct P2Smem {
-    size_t keys, cnt, used, brec, bkm, boff, pre, total;
-    __host__ __device__ void layout(uint32_t slots) {
-        size_t o = 0;
-        keys = o; o += KeyOps<W>::BYTES * (size_t)slots;
-        cnt = o; o += 4 * (size_t)slots;
-        used = o; o += 2 * (size_t)slots;
-        o = (o + 15) & ~size_t(15);
-        brec = o; o += 4 * (size_t)NBINS;
-        bkm = o; o += 4 * (size_t)NBINS;
-        boff = o; o += 4 * (size_t)(NBINS + 1);
-        o = (o + 15) & ~size_t(15);
-        pre = o; o += 4 * (size_t)(NBINS + 1);
-        total = (o + 15) & ~size_t(15);
-    }
-};
-
-// Block-wide exclusive scan of a[0..n) (n <= 2 * P2_THREADS) into out[0..n],
-// out[n] = total.
-__device__ void scan_bins(const uint32_t* a, uint32_t n, uint32_t* out, uint32_t* s_warp) {
+// Block-wide exclusive scan of one value per thread (blockDim == P2_THREADS);
+// `total` = the sum.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_warp, uint32_t& total) {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const uint32_t i0 = 2 * tid, i1 = 2 * tid + 1;
-    const uint32_t v0 = i0 < n ? a[i0] : 0, v1 = i1 < n ? a[i1] : 0;
-    const uint32_t v = v0 + v1;
     uint32_t x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -206,329 +175,455 @@ __device__ void scan_bins(const uint32_t* a, uint32_t n, uint32_t* out, uint32_t
         if (lane < P2_THREADS / 32) s_warp[lane] = t;
     }
     __syncthreads();
-    const uint32_t before = (wid ? s_warp[wid - 1] : 0) + x - v;
-    if (i0 < n) out[i0] = before;
-    if (i1 < n) out[i1] = before + v0;
-    if (tid == P2_THREADS - 1) out[n] = s_warp[P2_THREADS / 32 - 1];
-    __syncthreads();
+    total = s_warp[P2_THREADS / 32 - 1];
+    const uint32_t r = (wid ? s_warp[wid - 1] : 0) + x - v;
+    __syncthreads();  // s_warp may be reused right after
+    return r;
 }
 
-// One CTA per SM. The table is cleared once; each group adds its k-mers,
-// writes the used slots that pass ci/cx, and resets only those slots.
-//
-// A warp takes 32 descriptors at a time and spreads their k-mers over its
-// lanes: in each round lane t handles the warp's k-mer number r + t, whose
-// descriptor is found by a search over the descriptors' inclusive k-mer
-// prefix sums (five shuffles). All lanes stay busy whatever the record lengths.
-template <int W>
-__global__ void __launch_bounds__(P2_THREADS, 1)
-k_count(Phase2Params P) {
-    using O = KeyOps<W>;
-    extern __shared__ __align__(16) uint8_t smem[];
-    P2Smem<W> L;
-    L.layout(P.smem_slots);
-    typename O::Key* keys = reinterpret_cast<typename O::Key*>(smem + L.keys);
-    uint32_t* cnt = reinterpret_cast<uint32_t*>(smem + L.cnt);
-    uint16_t* used = reinterpret_cast<uint16_t*>(smem + L.used);
-    uint32_t* brec = reinterpret_cast<uint32_t*>(smem + L.brec);
-    uint32_t* bkm = reinterpret_cast<uint32_t*>(smem + L.bkm);
-    uint32_t* boff = reinterpret_cast<uint32_t*>(smem + L.boff);
-    uint32_t* pre = reinterpret_cast<uint32_t*>(smem + L.pre);
-    __shared__ uint32_t s_bucket, s_next, s_fail, s_nused, s_sp;
-    __shared__ uint32_t s_warp[P2_THREADS / 32];
-    __shared__ uint4 s_stack[64];  // {first bin, end bin, key-hash parts J, part j}
-    __shared__ unsigned long long s_obase;
-    __shared__ uint32_t s_ocur;
+__device__ __forceinline__ uint32_t bin_of(uint64_t d, uint32_t p1_bits, uint32_t nb) {
+    return (desc_mlo(d) >> p1_bits) & (nb - 1);
+}
 
-    const int tid = threadIdx.x, lane = tid & 31;
-    const uint32_t C = P.n_cta1;
-    const uint32_t S = P.smem_slots, mask = S - 1;
-    const uint32_t fill_cap = S - S / 8;  // a group is split beyond 7/8 occupancy
-    const uint32_t bin_bits = 20 - P.p1_bits;
-    const uint32_t nb = min(NBINS, 1u << bin_bits);
+// ---------------------------------------------------------------- k_binhist
+// k-mer instances per bin of one slice.
+__global__ void __launch_bounds__(P2_THREADS) k_binhist(KeysParams P) {
+    __shared__ uint32_t h[NBINS];
+    const int tid = threadIdx.x;
+    const Slice sl = P.slices[blockIdx.x];
+    for (uint32_t i = tid; i < P.nb; i += P2_THREADS) h[i] = 0;
+    __syncthreads();
+    const uint64_t* d = P.bdesc + sl.r_lo;
+    const uint32_t n = (uint32_t)(sl.r_hi - sl.r_lo);
+    for (uint32_t i0 = tid; i0 < n; i0 += 4 * P2_THREADS) {
+        uint64_t v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t i = i0 + u * P2_THREADS;
+            v[u] = i < n ? d[i] : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (desc_nk(v[u])) atomicAdd(&h[bin_of(v[u], P.p1_bits, P.nb)], desc_nk(v[u]));
+    }
+    __syncthreads();
+    for (uint32_t i = tid; i < P.nb; i += P2_THREADS) P.shist[(uint64_t)blockIdx.x * P.nb + i] = h[i];
+}
+
+// ---------------------------------------------------------------- k_binscan
+// One CTA per bucket: key offsets (from the bucket's first key) of every
+// (slice, bin), bins in order and slices in order inside a bin; then the
+// bucket's groups: greedy runs of consecutive bins of at most `target` k-mers
+// (a single larger bin is a group of its own, listed as heavy).
+__global__ void __launch_bounds__(P2_THREADS) k_binscan(KeysParams P) {
+    __shared__ uint32_t tot[NBINS];
+    __shared__ uint32_t s_warp[P2_THREADS / 32];
+    const int tid = threadIdx.x;
+    const uint32_t b = blockIdx.x, nb = P.nb;
+    const uint32_t s0 = P.slice_first[b], s1 = P.slice_first[b + 1];
+    uint32_t t = 0;
+    if ((uint32_t)tid < nb)
+        for (uint32_t s = s0; s < s1; ++s) t += P.shist[(uint64_t)s * nb + tid];
+    uint32_t total;
+    const uint32_t ex = block_excl_scan(t, s_warp, total);
+    if ((uint32_t)tid < nb) {
+        uint32_t run = ex;
+        for (uint32_t s = s0; s < s1; ++s) {
+            uint32_t* e = P.shist + (uint64_t)s * nb + tid;
+            const uint32_t v = *e;
+            *e = run;
+            run += v;
+        }
+        tot[tid] = t;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        const unsigned long long kb = P.kbase[b];
+        auto emit = [&](uint32_t lo, uint32_t hi) {
+            const int heavy = hi - lo > P.target ? 1 : 0;
+            const unsigned long long i = atomicAdd(&P.ctr[heavy ? P2C_HEAVY : P2C_NORMAL], 1ull);
+            if (i < P.groups_cap) {
+                Group g;
+                g.lo = kb + lo;
+                g.hi = kb + hi;
+                g.parts = 1;
+                g.part = 0;
+                g.pad[0] = g.pad[1] = 0;
+                P.groups[heavy][i] = g;
+            }
+        };
+        uint32_t lo = 0, cur = 0;
+        for (uint32_t i = 0; i < nb; ++i) {
+            const uint32_t ki = tot[i];
+            if (ki == 0) continue;
+            if (cur > 0 && cur + ki > P.target) {
+                emit(lo, lo + cur);
+                lo += cur;
+                cur = 0;
+            }
+            cur += ki;
+        }
+        if (cur > 0) emit(lo, lo + cur);
+    }
+}
+
+// ---------------------------------------------------------------- k_keys
+// Every k-mer of a slice: canonical key written at its bin's cursor. A warp
+// takes 32 descriptors at a time; each reserves its k-mers' places with one
+// shared-memory atomic on its bin cursor, then the warp's lanes take the
+// batch's k-mers in order (consecutive lanes, consecutive keys).
+template <int W>
+__global__ void __launch_bounds__(P2_THREADS) k_keys(KeysParams P) {
+    using O = KeyOps<W>;
+    __shared__ uint32_t cur[NBINS];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const Slice sl = P.slices[blockIdx.x];
+    for (uint32_t i = tid; i < P.nb; i += P2_THREADS) cur[i] = P.shist[(uint64_t)blockIdx.x * P.nb + i];
+    __syncthreads();
+    const unsigned long long kb = P.kbase[sl.bucket];
+    const uint64_t* d = P.bdesc + sl.r_lo;
+    const uint32_t n = (uint32_t)(sl.r_hi - sl.r_lo);
     const int k = P.k;
-    uint64_t* scratch = P.scratch + (uint64_t)blockIdx.x * P.scratch_cap;
-    unsigned long long distinct = 0;
+    for (uint32_t base = (uint32_t)wid * 32; base < n; base += P2_THREADS) {
+        const uint32_t i = base + lane;
+        const uint64_t dv = i < n ? d[i] : 0;
+        const uint32_t nk = desc_nk(dv);  // 0 past the slice; at least 1 otherwise
+        uint32_t koff = 0;
+        if (nk) koff = atomicAdd(&cur[bin_of(dv, P.p1_bits, P.nb)], nk);
+        uint32_t incl = nk;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const uint32_t excl = incl - nk;
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        // k-mer t of the batch belongs to lane o: stream position srcb_o + t,
+        // key index dstb_o + t
+        const uint64_t srcb = desc_start(dv) - excl;
+        const uint64_t dstb = kb + koff - excl;
+        for (uint32_t t0 = 0; t0 < total; t0 += 32 * KEYS_UNROLL) {
+            typename O::Key kv[KEYS_UNROLL];
+            uint64_t dst[KEYS_UNROLL];
+            bool act[KEYS_UNROLL];
+#pragma unroll
+            for (int u = 0; u < KEYS_UNROLL; ++u) {
+                const uint32_t r0 = t0 + 32 * u;  // warp-uniform
+                act[u] = false;
+                if (r0 >= total) continue;
+                // owner of k-mer r0 + l = (lanes starting before r0) + (starts in
+                // [r0, r0 + l]) - 1; starts are distinct since every nk >= 1
+                const uint32_t rel = excl - r0;
+                const unsigned starts = __reduce_or_sync(0xffffffffu, (nk && rel < 32) ? 1u << rel : 0u);
+                const unsigned before = __popc(__ballot_sync(0xffffffffu, excl < r0));
+                const uint32_t own = (before + __popc(starts & ((2u << lane) - 1u)) - 1u) & 31u;
+                const uint64_t sb = __shfl_sync(0xffffffffu, srcb, own);
+                const uint64_t db = __shfl_sync(0xffffffffu, dstb, own);
+                const uint32_t t = r0 + lane;
+                act[u] = t < total;
+                if (act[u]) {
+                    kv[u] = kmer_key<W>(P.packed, sb + t, k);
+                    dst[u] = db + t;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < KEYS_UNROLL; ++u)
+                if (act[u]) O::store(P.keys, dst[u], kv[u]);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- k_count
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// 128-bit keys: slots probed in order from the home slot h with the CAS itself
+// (a 128-bit key cannot be read in one single-copy-atomic load, and a torn
+// read could skip the slot that holds the same k-mer). Returns 1 for a new key,
+// 0 for a known one, -1 after PROBE_LIMIT slots.
+__device__ __forceinline__ int claim_cas(U128* keys, uint32_t* cnt, uint32_t mask, const U128& key, uint32_t h) {
+    using O = KeyOps<2>;
+    for (uint32_t p = 0; p < PROBE_LIMIT; ++p) {
+        const U128 prev = O::cas(&keys[h], O::empty(), key);
+        if (O::is_empty(prev)) { atomicAdd(&cnt[h], 1u); return 1; }
+        if (O::eq(prev, key)) { atomicAdd(&cnt[h], 1u); return 0; }
+        h = (h + 1) & mask;
+    }
+    return -1;
+}
+
+// The 64-bit table as buckets of 4 slots (32 bytes). A key's probe order is
+// fixed: the slots of its home bucket in order, then the next bucket's, and so
+// on, so two inserts of one key meet in the same slot. One probe reads a whole
+// bucket (two 16-byte loads; each 8-byte slot is read atomically). If the key
+// is in the bucket, it is counted there (a slot once taken keeps its key);
+// otherwise the first empty slot is claimed by CAS, and a CAS lost to another
+// key re-reads the bucket. Returns 1 for a new key, 0 for a known one, -1 after
+// PROBE_BUCKETS buckets.
+constexpr uint32_t BUCKET = 4;
+constexpr uint32_t PROBE_BUCKETS = 32;
+
+__device__ __forceinline__ void lds_bucket(const unsigned long long* p, unsigned long long (&v)[BUCKET]) {
+    const uint32_t a = smem_addr(p);
+    asm volatile("ld.volatile.shared.v2.u64 {%0, %1}, [%2];" : "=l"(v[0]), "=l"(v[1]) : "r"(a));
+    asm volatile("ld.volatile.shared.v2.u64 {%0, %1}, [%2+16];" : "=l"(v[2]), "=l"(v[3]) : "r"(a));
+}
+
+__device__ __forceinline__ int claim_bucket(unsigned long long* keys, uint32_t* cnt, uint32_t bmask,
+                                            unsigned long long key, uint32_t b) {
+    for (uint32_t p = 0; p < PROBE_BUCKETS;) {
+        unsigned long long v[BUCKET];
+        lds_bucket(keys + b * BUCKET, v);
+        int hit = -1, emp = -1;
+#pragma unroll
+        for (int j = BUCKET - 1; j >= 0; --j) {
+            if (v[j] == key) hit = j;
+            if (v[j] == ~0ull) emp = j;
+        }
+        if (hit >= 0) { atomicAdd(&cnt[b * BUCKET + hit], 1u); return 0; }
+        if (emp < 0) { b = (b + 1) & bmask; ++p; continue; }
+        const unsigned long long prev = atomicCAS(&keys[b * BUCKET + emp], ~0ull, key);
+        if (prev == ~0ull || prev == key) {
+            atomicAdd(&cnt[b * BUCKET + emp], 1u);
+            return prev == key ? 0 : 1;
+        }
+        // the slot went to another key: read the bucket again
+    }
+    return -1;
+}
+
+// Asynchronous copy (cp.async, two 16-byte pieces) of group `gi` of the
+// launch's sequence (list 1 first, then list 0) into shared memory; an index
+// past the end gives an empty group.
+__device__ __forceinline__ void copy_group(Group* dst, const CountParams& P, unsigned long long gi,
+                                           unsigned long long n1, unsigned long long ntot) {
+    if (gi >= ntot) {
+        dst->lo = dst->hi = 0;
+        dst->parts = 0;
+        return;
+    }
+    const Group* src = gi < n1 ? P.list[1] + gi : P.list[0] + (gi - n1);
+    const uint32_t d = smem_addr(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d + 16),
+                 "l"(reinterpret_cast<const uint8_t*>(src) + 16)
+                 : "memory");
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+template <int W>
+struct CountSmem {
+    size_t keys, cnt, total;
+    __host__ __device__ void layout(uint32_t slots) {
+        size_t o = 0;
+        keys = o; o += KeyOps<W>::BYTES * (size_t)slots;
+        cnt = o; o += 4 * (size_t)slots;
+        total = (o + 15) & ~size_t(15);
+    }
+};
+
+// Persistent: one CTA per SM takes groups in order (list 1, then list 0) from a
+// global counter. A group's keys are one contiguous range; they are inserted
+// in rounds of RK keys, thread t taking keys t, t + P2_THREADS, ... of a round,
+// and each thread's keys of the next round (or of the next group's first round)
+// are loaded into registers while it inserts the current ones, so there is no
+// barrier inside a group. After a group every thread scans its slots of the
+// table, writes the keys that pass ci/cx and clears the slots. A group with
+// more distinct keys than 7/8 of the table (or a probe run past the limit)
+// comes back as its two key-hash halves. Group entries are fetched two groups
+// ahead (cp.async) into a ring of three.
+template <int W>
+__global__ void __launch_bounds__(P2_THREADS, 1) k_count(CountParams P) {
+    using O = KeyOps<W>;
+    using Key = typename O::Key;
+    constexpr int U = W == 1 ? 4 : 2;                 // keys per thread per round
+    constexpr uint32_t RK = U * P2_THREADS;           // keys per round
+    constexpr uint32_t SPT = W == 1 ? 16 : 8;         // table slots per thread
+    extern __shared__ __align__(128) uint8_t smem[];
+    CountSmem<W> L;
+    L.layout(P.smem_slots);
+    Key* keys = reinterpret_cast<Key*>(smem + L.keys);
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(smem + L.cnt);
+    __shared__ __align__(16) Group s_grp[3];          // groups g, g + 1, g + 2
+    __shared__ uint32_t s_fail;
+    __shared__ uint32_t s_wnew[P2_THREADS / 32];      // new keys of the group, per warp
+    __shared__ uint32_t s_wout[P2_THREADS / 32];      // output keys per warp, then their offsets
+    __shared__ unsigned long long s_obase;
+
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const uint32_t S = P.smem_slots, mask = S - 1;    // S == SPT * P2_THREADS
+    const uint32_t fill_cap = S - S / 8;
+    // counts are at least 1 and fit in 32 bits: without ci/cx limits every key is kept
+    const bool filtered = P.ci > 1 || P.cx < 0xFFFFFFFFull;
+    const unsigned long long n1 = P.n_list[1], ntot = P.n_list[0] + n1;
+    const Key* src = static_cast<const Key*>(P.keys);
+    unsigned long long distinct = 0;                  // per warp, in lane 0
+
     for (uint32_t i = tid; i < S; i += P2_THREADS) { keys[i] = O::empty(); cnt[i] = 0; }
-    if (tid == 0) s_nused = 0;
+    if (tid < P2_THREADS / 32) s_wnew[tid] = 0;
+    unsigned long long gi_pend = ~0ull;               // thread 0: index of group g + 3
+    if (tid == 0) {
+        s_fail = 0;
+        for (int q = 0; q < 3; ++q) copy_group(&s_grp[q], P, atomicAdd(&P.ctr[P2C_WORK], 1ull), n1, ntot);
+        gi_pend = atomicAdd(&P.ctr[P2C_WORK], 1ull);
+        asm volatile("cp.async.wait_all;" ::: "memory");
+    }
     __syncthreads();
 
-    for (;;) {
-        if (tid == 0) s_bucket = atomicAdd(P.work, 1u);
-        __syncthreads();
-        const uint32_t qi = s_bucket;
-        __syncthreads();
-        if (qi >= P.n_buckets) break;
-        const uint32_t b = P.order[qi];
-        const uint64_t r0 = P.off_r[(uint64_t)b * C];
-        const uint32_t nrec = (uint32_t)(P.off_r[(uint64_t)(b + 1) * C] - r0);
-        if (nrec == 0) continue;
-        const uint64_t* bd = P.bdesc + r0;
-        const uint64_t K = P.bucket_kmers[b];
-        bool binned = false;
-
-        auto bin_of = [&](uint64_t d) -> uint32_t { return (desc_mlo(d) >> P.p1_bits) & (nb - 1); };
-        auto bin_pass = [&]() {
-            for (uint32_t i = tid; i < nb; i += P2_THREADS) { brec[i] = 0; bkm[i] = 0; }
-            __syncthreads();
-            for (uint32_t i = tid; i < nrec; i += P2_THREADS) {
-                const uint64_t d = bd[i];
-                const uint32_t bin = bin_of(d);
-                atomicAdd(&brec[bin], 1u);
-                atomicAdd(&bkm[bin], desc_nk(d));
-            }
-            __syncthreads();
-            scan_bins(brec, nb, boff, s_warp);
-            scan_bins(bkm, nb, pre, s_warp);
-            for (uint32_t i = tid; i < nb; i += P2_THREADS) brec[i] = boff[i];
-            __syncthreads();
-            for (uint32_t i = tid; i < nrec; i += P2_THREADS) {
-                const uint64_t d = bd[i];
-                scratch[atomicAdd(&brec[bin_of(d)], 1u)] = d;
-            }
-            __syncthreads();
-        };
-
-        if (K > P.target) {
-            bin_pass();
-            binned = true;
+    // keys of round r of group g into K (EMPTY past the group's end)
+    auto load_round = [&](const Group& g, uint32_t r, Key (&K)[U]) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const unsigned long long i = g.lo + (unsigned long long)r * RK + (uint32_t)u * P2_THREADS + tid;
+            K[u] = i < g.hi ? src[i] : O::empty();
         }
-        if (tid == 0) { s_stack[0] = make_uint4(0, nb, 1, 0); s_sp = 1; }
-        __syncthreads();
-        while (s_sp > 0) {
-            // ---- pop a bin range; halve it while it holds more k-mers than the target
-            __syncthreads();
-            if (tid == 0) {
-                uint4 rg = s_stack[--s_sp];
-                while (binned && rg.z == 1 && rg.y - rg.x > 1 && pre[rg.y] - pre[rg.x] > P.target && s_sp < 62) {
-                    const uint32_t half = pre[rg.x] + (pre[rg.y] - pre[rg.x]) / 2;
-                    uint32_t lo = rg.x + 1, hi = rg.y - 1;  // first bin m in (x, y) with pre[m] >= half
-                    while (lo < hi) {
-                        const uint32_t md = (lo + hi) / 2;
-                        if (pre[md] >= half) hi = md; else lo = md + 1;
-                    }
-                    s_stack[s_sp++] = make_uint4(lo, rg.y, 1, 0);
-                    rg.y = lo;
+    };
+
+    Key K[U];
+    {
+        const Group g0 = s_grp[0];
+        load_round(g0, 0, K);
+    }
+    for (uint32_t q = 0;; q = q == 2 ? 0 : q + 1) {
+        const Group g = s_grp[q];
+        if (g.hi <= g.lo) break;  // no more groups
+        const uint32_t nr = (uint32_t)((g.hi - g.lo + RK - 1) / RK);
+        uint32_t newc = 0;
+        bool bad = false;
+        for (uint32_t r = 0; r < nr; ++r) {
+            Key N[U];
+            if (r + 1 < nr) load_round(g, r + 1, N);
+            else load_round(s_grp[q == 2 ? 0 : q + 1], 0, N);
+            if (!bad) {
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    if (bad || O::is_empty(K[u])) continue;
+                    const uint64_t h = O::hash(K[u]);
+                    if (g.parts > 1 && ((uint32_t)(h >> 8) & (g.parts - 1)) != g.part) continue;
+                    int res;
+                    if constexpr (W == 1)
+                        res = claim_bucket(reinterpret_cast<unsigned long long*>(keys), cnt, mask / BUCKET, K[u],
+                                           (uint32_t)(h >> 32) & (mask / BUCKET));
+                    else
+                        res = claim_cas(reinterpret_cast<U128*>(keys), cnt, mask, K[u], (uint32_t)(h >> 32) & mask);
+                    if (res < 0) bad = true;
+                    else newc += (uint32_t)res;
                 }
-                s_stack[63] = rg;  // the range to count now
-                s_next = 0;
-                s_fail = 0;
             }
+#pragma unroll
+            for (int u = 0; u < U; ++u) K[u] = N[u];
+        }
+        newc = __reduce_add_sync(0xffffffffu, newc);
+        if (lane == 0) s_wnew[wid] = newc;
+        if (bad) s_fail = 1;
+        __syncthreads();  // inserts done; every thread has read slot q
+        if (tid == 0) {
+            // group g + 3's entry into slot q (landed before the group's last
+            // barrier), the index after it claimed
+            copy_group(&s_grp[q], P, gi_pend, n1, ntot);
+            gi_pend = atomicAdd(&P.ctr[P2C_WORK], 1ull);
+        }
+        if (wid == 0) {
+            const uint32_t t = __reduce_add_sync(0xffffffffu, s_wnew[lane]);
+            if (lane == 0 && t > fill_cap) s_fail = 1;  // more than 7/8 full: split the group
+        }
+        __syncthreads();
+        if (s_fail) {
+            // clear the table; the group comes back as two halves
+#pragma unroll
+            for (uint32_t j = 0; j < SPT; ++j) { keys[tid + j * P2_THREADS] = O::empty(); cnt[tid + j * P2_THREADS] = 0; }
+            if (tid == 0) {
+                Group f = g;
+                if (g.parts < MAX_PARTS) {
+                    const unsigned long long i = atomicAdd(P.n_retry, 2ull);
+                    f.parts = 2 * g.parts;
+                    if (i + 1 < P.retry_cap) {
+                        f.part = g.part;
+                        P.retry[i] = f;
+                        f.part = g.part + g.parts;
+                        P.retry[i + 1] = f;
+                    }
+                } else {
+                    const unsigned long long i = atomicAdd(&P.ctr[P2C_FALLBACK], 1ull);
+                    if (i < P.fallback_cap) P.fallback[i] = f;
+                }
+            }
+        } else {
+            // ---- output: thread t owns slots t + j * P2_THREADS (a warp's accesses
+            // are consecutive); per warp and round j one ballot places the kept
+            // keys contiguously
+            uint32_t keepm = 0, nocc = 0;
+#pragma unroll
+            for (uint32_t j = 0; j < SPT; ++j) {
+                const uint32_t sl = tid + j * P2_THREADS;
+                const bool occ = !O::is_empty(keys[sl]);
+                nocc += occ ? 1u : 0u;
+                bool keep = occ;
+                if (filtered && occ) {
+                    const uint32_t c = cnt[sl];
+                    keep = (uint64_t)c >= P.ci && (uint64_t)c <= P.cx;
+                }
+                keepm |= (keep ? 1u : 0u) << j;
+            }
+            uint32_t wtot = 0;
+#pragma unroll
+            for (uint32_t j = 0; j < SPT; ++j) wtot += __popc(__ballot_sync(0xffffffffu, (keepm >> j) & 1u));
+            nocc = __reduce_add_sync(0xffffffffu, nocc);
+            if (lane == 0) { s_wout[wid] = wtot; distinct += nocc; }
             __syncthreads();
-            const uint4 rg = s_stack[63];
-            const uint32_t part_mask = rg.z - 1, part = rg.w;
-            const uint64_t* list = binned ? scratch + boff[rg.x] : bd;
-            const uint32_t cnt_r = binned ? boff[rg.y] - boff[rg.x] : nrec;
-            // ---- add every k-mer of the range: batches of 32 descriptors per warp
-            for (;;) {
-                uint32_t base = 0;
-                if (lane == 0) base = atomicAdd(&s_next, 32u);
-                base = __shfl_sync(0xffffffffu, base, 0);
-                if (base >= cnt_r) break;
-                const uint32_t i = base + lane;
-                const uint64_t d = i < cnt_r ? list[i] : 0;
-                const uint32_t nk = i < cnt_r ? desc_nk(d) : 0;
-                const uint64_t st = desc_start(d);
-                uint32_t incl = nk;
+            if (wid == 0) {
+                const uint32_t v = s_wout[lane];
+                uint32_t x = v;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
-                    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o) incl += y;
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                    if (lane >= o) x += y;
                 }
-                const uint32_t excl = incl - nk;
-                const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-                bool bad = false;
-                // U k-mers per lane per round: their loads and probes overlap
-                for (uint32_t t0 = 0; t0 < total; t0 += 32 * UNROLL) {
-                    typename O::Key kv[UNROLL];
-                    bool act[UNROLL];
-#pragma unroll
-                    for (int u = 0; u < UNROLL; ++u) {
-                        const uint32_t t = t0 + 32 * u + lane;
-                        // owner = first lane whose inclusive prefix exceeds t
-                        uint32_t lo = 0;
-#pragma unroll
-                        for (uint32_t step = 16; step >= 1; step >>= 1) {
-                            const uint32_t c = lo + step - 1;
-                            const uint32_t v = __shfl_sync(0xffffffffu, incl, c);
-                            if (v <= t) lo = c + 1;
-                        }
-                        const uint32_t owner = lo & 31;
-                        const uint64_t ost = __shfl_sync(0xffffffffu, st, owner);
-                        const uint32_t opre = __shfl_sync(0xffffffffu, excl, owner);
-                        act[u] = t < total;
-                        if (act[u]) kv[u] = kmer_key<W>(P.packed, ost + (t - opre), k);
-                    }
-#pragma unroll
-                    for (int u = 0; u < UNROLL; ++u) {
-                        int r = 0;
-                        uint32_t slot = 0;
-                        // a bin split by key hash counts only its part of the keys
-                        if (act[u] && !bad && ((uint32_t)(O::hash(kv[u]) >> 8) & part_mask) == part) {
-                            r = tbl_claim<W>(keys, cnt, mask, kv[u], PROBE_LIMIT, slot);
-                            if (r < 0) bad = true;
-                        }
-                        // append the newly claimed slots to the used list, one atomic per warp
-                        const unsigned nm = __ballot_sync(0xffffffffu, r > 0);
-                        if (nm) {
-                            uint32_t ub = 0;
-                            if (lane == 0) ub = atomicAdd(&s_nused, (uint32_t)__popc(nm));
-                            ub = __shfl_sync(0xffffffffu, ub, 0);
-                            const uint32_t uu = ub + __popc(nm & ((1u << lane) - 1));
-                            if (r > 0) {
-                                used[uu] = (uint16_t)slot;      // uu < S: at most S slots can be claimed
-                                if (uu >= fill_cap) bad = true;  // the table is 7/8 full: split the group
-                            }
-                        }
-                    }
-                }
-                if (bad) *reinterpret_cast<volatile uint32_t*>(&s_fail) = 1;
-                if (__any_sync(0xffffffffu, *reinterpret_cast<volatile uint32_t*>(&s_fail) != 0)) break;
+                s_wout[lane] = x - v;
+                if (lane == 31) s_obase = x ? atomicAdd(&P.ctr[P2C_OUT], (unsigned long long)x) : 0;
             }
             __syncthreads();
-            const uint32_t nu = min(s_nused, S);
-            if (s_fail) {
-                // reset the partial table, then split the range (or hand it to the global table)
-                for (uint32_t i = tid; i < nu; i += P2_THREADS) { keys[used[i]] = O::empty(); cnt[used[i]] = 0; }
-                __syncthreads();
-                if (!binned) {
-                    bin_pass();
-                    binned = true;
-                    if (tid == 0) { s_stack[0] = make_uint4(0, nb, 1, 0); s_sp = 1; }
-                } else if (tid == 0) {
-                    if (rg.y - rg.x > 1 && s_sp < 62) {
-                        const uint32_t mid = (rg.x + rg.y) / 2;
-                        s_stack[s_sp++] = make_uint4(mid, rg.y, 1, 0);
-                        s_stack[s_sp++] = make_uint4(rg.x, mid, 1, 0);
-                    } else if (rg.z < MAX_PARTS && s_sp < 62) {
-                        // one bin with more distinct k-mers than a table: count it in
-                        // 2J passes, each over the keys whose hash bits select it
-                        s_stack[s_sp++] = make_uint4(rg.x, rg.y, 2 * rg.z, rg.w + rg.z);
-                        s_stack[s_sp++] = make_uint4(rg.x, rg.y, 2 * rg.z, rg.w);
-                    } else {
-                        for (uint32_t g = rg.x; g < rg.y; ++g) {
-                            const unsigned long long slot = atomicAdd(&P.out_n[2], 1ull);
-                            if (slot < P.fallback_cap) {
-                                P.fallback[3 * slot + 0] = b;
-                                P.fallback[3 * slot + 1] = g;
-                                P.fallback[3 * slot + 2] = nb;
-                            }
-                        }
-                    }
-                }
-                if (tid == 0) s_nused = 0;
-                __syncthreads();
-                continue;
-            }
-            // ---- output the used slots that pass ci/cx, and reset them. One
-            // global atomic per group reserves the output range; inside it each
-            // warp claims a contiguous slice per pass, so its stores coalesce.
-            uint32_t mine = 0;
-            for (uint32_t i = tid; i < nu; i += P2_THREADS) {
-                const uint32_t c = cnt[used[i]];
-                mine += ((uint64_t)c >= P.ci && (uint64_t)c <= P.cx) ? 1u : 0u;
-            }
+            unsigned long long o = s_obase + s_wout[wid];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) mine += __shfl_down_sync(0xffffffffu, mine, o);
-            if (tid == 0) s_ocur = 0;
-            if (lane == 0) s_warp[tid >> 5] = mine;
-            __syncthreads();
-            if (tid == 0) {
-                uint32_t t = 0;
-                for (int w2 = 0; w2 < P2_THREADS / 32; ++w2) t += s_warp[w2];
-                if (t) s_obase = atomicAdd(&P.out_n[0], (unsigned long long)t);
-            }
-            __syncthreads();
-            const unsigned long long obase = s_obase;
-            const uint32_t iters = (nu + P2_THREADS - 1) / P2_THREADS;
-            for (uint32_t it = 0; it < iters; ++it) {
-                const uint32_t i = it * P2_THREADS + tid;
-                bool keep = false;
-                typename O::Key key;
-                uint32_t c = 0;
-                if (i < nu) {
-                    const uint32_t sl = used[i];
-                    key = keys[sl];
-                    c = cnt[sl];
-                    keep = (uint64_t)c >= P.ci && (uint64_t)c <= P.cx;
-                    keys[sl] = O::empty();
-                    cnt[sl] = 0;
-                }
+            for (uint32_t j = 0; j < SPT; ++j) {
+                const uint32_t sl = tid + j * P2_THREADS;
+                const bool keep = (keepm >> j) & 1u;
                 const unsigned bal = __ballot_sync(0xffffffffu, keep);
-                if (bal) {
-                    uint32_t wb = 0;
-                    if (lane == 0) wb = atomicAdd(&s_ocur, (uint32_t)__popc(bal));
-                    wb = __shfl_sync(0xffffffffu, wb, 0);
-                    if (keep) {
-                        const uint64_t o = obase + wb + __popc(bal & ((1u << lane) - 1));
-                        if (o < P.out_cap) {
-                            O::store_out(P.out_keys, o, key);
-                            P.out_counts[o] = c;
-                        }
+                if (keep) {
+                    const unsigned long long i = o + __popc(bal & ((1u << lane) - 1));
+                    if (i < P.out_cap) {
+                        O::store(P.out_keys, i, keys[sl]);
+                        P.out_counts[i] = cnt[sl];
                     }
                 }
+                keys[sl] = O::empty();
+                cnt[sl] = 0;
+                o += __popc(bal);
             }
-            if (tid == 0) { distinct += nu; s_nused = 0; }
-            __syncthreads();
         }
+        if (tid == 0) {
+            s_fail = 0;
+            asm volatile("cp.async.wait_all;" ::: "memory");  // group g + 3's entry has landed
+        }
+        __syncthreads();
     }
-    if (tid == 0 && distinct) atomicAdd(&P.out_n[1], distinct);
-}
-
-// Write the occupied slots [0, S) of a global table that pass ci/cx (warp-aggregated).
-template <int W>
-__device__ void extract_all(const typename KeyOps<W>::Key* keys, const uint32_t* cnt, uint32_t S,
-                            const Phase2Params& P, unsigned long long& distinct) {
-    using O = KeyOps<W>;
-    const int lane = threadIdx.x & 31;
-    const uint32_t iters = (S + blockDim.x - 1) / blockDim.x;
-    for (uint32_t it = 0; it < iters; ++it) {
-        const uint32_t i = it * blockDim.x + threadIdx.x;
-        bool occ = false, keep = false;
-        typename O::Key key;
-        uint32_t c = 0;
-        if (i < S) {
-            key = keys[i];
-            occ = !O::is_empty(key);
-            if (occ) {
-                c = cnt[i];
-                keep = (uint64_t)c >= P.ci && (uint64_t)c <= P.cx;
-            }
-        }
-        distinct += occ ? 1 : 0;
-        const unsigned bal = __ballot_sync(0xffffffffu, keep);
-        if (!bal) continue;
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(&P.out_n[0], (unsigned long long)__popc(bal));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (keep) {
-            const uint64_t o = base + __popc(bal & ((1u << lane) - 1));
-            if (o < P.out_cap) {
-                O::store_out(P.out_keys, o, key);
-                P.out_counts[o] = c;
-            }
-        }
-    }
+    if (lane == 0 && distinct) atomicAdd(&P.ctr[P2C_DISTINCT], distinct);
 }
 
 // ---------------------------------------------------------------- fallback
-// A group that overflowed its shared-memory table is counted in a global
-// table of S slots (power of two >= 2 x its k-mer instances): every CTA walks a
-// slice of the bucket's records and adds the k-mers of the group's records.
-
+// A key range (one key-hash part of it) that did not fit in shared memory,
+// counted in a global table of S slots (power of two >= 2 x the range).
 template <int W>
-__global__ void k_fb_insert(FallbackParams P) {
+__global__ void k_fb_insert(FallbackParams F) {
     using O = KeyOps<W>;
-    auto* keys = reinterpret_cast<typename O::Key*>(P.keys);
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P.nrec;
+    auto* tk = reinterpret_cast<typename O::Key*>(F.tkeys);
+    const auto* src = reinterpret_cast<const typename O::Key*>(F.keys);
+    for (unsigned long long i = F.lo + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < F.hi;
          i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t d = P.bdesc[P.r0 + i];
-        if (((desc_mlo(d) >> P.p1_bits) & (P.nbins - 1)) != P.bin) continue;
-        const uint64_t st = desc_start(d);
-        const uint32_t nk = desc_nk(d);
-        for (uint32_t j = 0; j < nk; ++j)
-            if (!tbl_add<W>(keys, P.cnt, P.mask, kmer_key<W>(P.packed, st + j, P.k), P.mask + 1))
-                atomicExch(P.fail, 1u);
+        const typename O::Key key = src[i];
+        if (key_part<W>(key, F.parts) != F.part) continue;
+        if (!tbl_add<W>(tk, F.tcnt, F.mask, key, F.mask + 1)) atomicExch(F.fail, 1u);
     }
 }
 
@@ -542,59 +637,312 @@ __global__ void k_fb_init(void* keys, uint32_t* cnt, uint64_t S) {
     }
 }
 
+// Write the occupied slots that pass ci/cx (warp-aggregated output atomics).
 template <int W>
 __global__ void __launch_bounds__(256) k_fb_extract(const void* keys, const uint32_t* cnt, uint64_t S,
-                                                            Phase2Params P) {
+                                                    CountParams P) {
     using O = KeyOps<W>;
     const auto* kk = reinterpret_cast<const typename O::Key*>(keys);
+    const int lane = threadIdx.x & 31;
     unsigned long long distinct = 0;
-    const uint64_t chunk = (uint64_t)256 * 64;
-    for (uint64_t base = (uint64_t)blockIdx.x * chunk; base < S; base += (uint64_t)gridDim.x * chunk) {
-        const uint32_t n = (uint32_t)((S - base) < chunk ? (S - base) : chunk);
-        extract_all<W>(kk + base, cnt + base, n, P, distinct);
+    for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < S; i0 += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i = i0 + threadIdx.x;
+        bool occ = false, keep = false;
+        typename O::Key key;
+        uint32_t c = 0;
+        if (i < S) {
+            key = kk[i];
+            occ = !O::is_empty(key);
+            if (occ) {
+                c = cnt[i];
+                keep = (uint64_t)c >= P.ci && (uint64_t)c <= P.cx;
+            }
+        }
+        distinct += occ ? 1 : 0;
+        const unsigned bal = __ballot_sync(0xffffffffu, keep);
+        if (!bal) continue;
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(&P.ctr[P2C_OUT], (unsigned long long)__popc(bal));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (keep) {
+            const uint64_t o = base + __popc(bal & ((1u << lane) - 1));
+            if (o < P.out_cap) {
+                O::store(P.out_keys, o, key);
+                P.out_counts[o] = c;
+            }
+        }
     }
     for (int o = 16; o > 0; o >>= 1) distinct += __shfl_down_sync(0xffffffffu, distinct, o);
-    if ((threadIdx.x & 31) == 0 && distinct) atomicAdd(&P.out_n[1], distinct);
+    if (lane == 0 && distinct) atomicAdd(&P.ctr[P2C_DISTINCT], distinct);
 }
 
-// ---------------------------------------------------------------- launchers
-size_t count_smem_bytes(int W, uint32_t slots) {
-    if (W == 1) { P2Smem<1> L; L.layout(slots); return L.total; }
-    P2Smem<2> L;
+// ---------------------------------------------------------------- host side
+size_t key_bytes(int W) { return W == 1 ? 8 : 16; }
+
+// Table slots of a k_count CTA: the largest power of two whose keys and counts
+// fit in one SM's shared memory (large tables mean large groups, and fewer of
+// them to set up and drain).
+uint32_t count_slots(int W) { return W == 1 ? 16384 : 8192; }
+
+static size_t count_smem_bytes(int W, uint32_t slots) {
+    if (W == 1) { CountSmem<1> L; L.layout(slots); return L.total; }
+    CountSmem<2> L;
     L.layout(slots);
     return L.total;
 }
 
-size_t key_bytes(int W) { return W == 1 ? 8 : 16; }
-
-cudaError_t launch_count(int W, const Phase2Params& P, uint32_t grid, cudaStream_t st) {
-    const size_t sm = count_smem_bytes(W, P.smem_slots);
-    cudaError_t e;
-    if (W == 1) {
-        e = cudaFuncSetAttribute(k_count<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        if (e != cudaSuccess) return e;
-        k_count<1><<<grid, P2_THREADS, sm, st>>>(P);
-    } else {
-        e = cudaFuncSetAttribute(k_count<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        if (e != cudaSuccess) return e;
-        k_count<2><<<grid, P2_THREADS, sm, st>>>(P);
+namespace {
+struct Carve {
+    uint8_t* base;
+    size_t off, cap;
+    bool ok;
+    template <class T>
+    T* take(size_t n) {
+        off = (off + 255) & ~size_t(255);
+        if (off + n * sizeof(T) > cap) { ok = false; return nullptr; }
+        T* p = reinterpret_cast<T*>(base + off);
+        off += n * sizeof(T);
+        return p;
     }
-    return cudaGetLastError();
+};
+
+struct P2Plan {
+    uint64_t n_slices = 0, groups_cap = 0, retry_cap = 0, n_keys = 0, n_keys_alloc = 0;
+    uint32_t nb = 0;
+    std::vector<Slice> slices;
+    std::vector<uint32_t> slice_first;
+    std::vector<unsigned long long> kbase;
+};
+
+P2Plan make_plan(const P2Input& in) {
+    P2Plan L;
+    L.nb = std::min<uint32_t>(NBINS, 1u << (20 - in.p1_bits));
+    L.slice_first.resize(in.p1 + 1);
+    L.kbase.resize(in.p1 + 1);
+    uint64_t r = 0, kb = 0;
+    for (uint32_t b = 0; b < in.p1; ++b) {
+        L.slice_first[b] = (uint32_t)L.slices.size();
+        L.kbase[b] = kb;
+        for (uint64_t s = 0; s < in.recs[b]; s += SLICE_DESC) {
+            Slice sl;
+            sl.r_lo = r + s;
+            sl.r_hi = r + std::min<uint64_t>(in.recs[b], s + SLICE_DESC);
+            sl.bucket = b;
+            sl.pad = 0;
+            L.slices.push_back(sl);
+        }
+        r += in.recs[b];
+        kb += in.kmers[b];
+    }
+    L.slice_first[in.p1] = (uint32_t)L.slices.size();
+    L.kbase[in.p1] = kb;
+    L.n_slices = L.slices.size();
+    L.groups_cap = (uint64_t)in.p1 * L.nb;
+    L.retry_cap = std::max<uint64_t>(4096, L.groups_cap);
+    L.n_keys = kb;
+    L.n_keys_alloc = kb + 16 / key_bytes(in.W) + 1;  // a bulk copy may read to the next 16 bytes
+    return L;
 }
 
-cudaError_t launch_fallback(int W, const FallbackParams& F, uint64_t S, const Phase2Params& P, uint32_t grid,
-                            cudaStream_t st, int* launches) {
-    if (W == 1) {
-        k_fb_init<1><<<grid, 256, 0, st>>>(F.keys, F.cnt, S);
-        k_fb_insert<1><<<grid, 256, 0, st>>>(F);
-        k_fb_extract<1><<<grid, 256, 0, st>>>(F.keys, F.cnt, S, P);
-    } else {
-        k_fb_init<2><<<grid, 256, 0, st>>>(F.keys, F.cnt, S);
-        k_fb_insert<2><<<grid, 256, 0, st>>>(F);
-        k_fb_extract<2><<<grid, 256, 0, st>>>(F.keys, F.cnt, S, P);
+// The scratch regions of one run, in order (the same walk sizes and places them).
+struct P2Regions {
+    unsigned long long* ctr;
+    unsigned long long* aux;  // [0..1] retry counters, [2..3] list sizes of a retry pass
+    Slice* slices;
+    uint32_t* slice_first;
+    unsigned long long* kbase;
+    uint32_t* shist;
+    Group* normal;
+    Group* heavy;
+    Group* retry[2];
+    Group* fb;
+    uint8_t* keys;
+};
+
+P2Regions carve(Carve& c, const P2Input& in, const P2Plan& L) {
+    P2Regions R;
+    R.ctr = c.take<unsigned long long>(P2C_COUNT);
+    R.aux = c.take<unsigned long long>(4);
+    R.slices = c.take<Slice>(L.n_slices + 1);
+    R.slice_first = c.take<uint32_t>(in.p1 + 1);
+    R.kbase = c.take<unsigned long long>(in.p1 + 1);
+    R.shist = c.take<uint32_t>(L.n_slices * L.nb + 1);
+    R.normal = c.take<Group>(L.groups_cap);
+    R.heavy = c.take<Group>(L.groups_cap);
+    R.retry[0] = c.take<Group>(L.retry_cap);
+    R.retry[1] = c.take<Group>(L.retry_cap);
+    R.fb = c.take<Group>(FALLBACK_CAP);
+    R.keys = c.take<uint8_t>(L.n_keys_alloc * key_bytes(in.W));
+    return R;
+}
+}  // namespace
+
+size_t phase2_scratch_bytes(const P2Input& in) {
+    const P2Plan L = make_plan(in);
+    Carve c{nullptr, 0, ~size_t(0), true};
+    carve(c, in, L);
+    return c.off + 256;
+}
+
+#define P2_CK(call, what)                                            \
+    do {                                                             \
+        cudaError_t e_ = (call);                                     \
+        if (e_ != cudaSuccess) {                                     \
+            err = std::string(what) + ": " + cudaGetErrorString(e_); \
+            return TG_ERR_CUDA;                                      \
+        }                                                            \
+    } while (0)
+
+tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Output& out,
+                     const std::function<void*(size_t)>& fallback_table, cudaStream_t st, cudaEvent_t ev_keys,
+                     int* launches, std::string& err) {
+    const P2Plan L = make_plan(in);
+    const int W = in.W;
+    for (uint32_t b = 0; b < in.p1; ++b)
+        if (in.kmers[b] >= (1ull << 32)) {
+            err = "a bucket holds 2^32 k-mer instances or more";
+            return TG_ERR_UNSUPPORTED;
+        }
+    Carve c{static_cast<uint8_t*>(scratch), 0, scratch_cap, true};
+    const P2Regions R = carve(c, in, L);
+    if (!c.ok) { err = "phase-2 scratch too small"; return TG_ERR_OOM; }
+    const uint32_t slots = count_slots(W);
+
+    P2_CK(cudaMemsetAsync(R.ctr, 0, (P2C_COUNT + 0) * 8, st), "memset");
+    if (L.n_slices)
+        P2_CK(cudaMemcpyAsync(R.slices, L.slices.data(), L.n_slices * sizeof(Slice), cudaMemcpyHostToDevice, st),
+              "h2d");
+    P2_CK(cudaMemcpyAsync(R.slice_first, L.slice_first.data(), (in.p1 + 1) * 4, cudaMemcpyHostToDevice, st), "h2d");
+    P2_CK(cudaMemcpyAsync(R.kbase, L.kbase.data(), (in.p1 + 1) * 8, cudaMemcpyHostToDevice, st), "h2d");
+    // the bytes a bulk copy may read past the last key
+    P2_CK(cudaMemsetAsync(R.keys + L.n_keys * key_bytes(W), 0, (L.n_keys_alloc - L.n_keys) * key_bytes(W), st),
+          "memset");
+
+    KeysParams K{};
+    K.packed = in.packed;
+    K.bdesc = in.bdesc;
+    K.slices = R.slices;
+    K.slice_first = R.slice_first;
+    K.kbase = R.kbase;
+    K.shist = R.shist;
+    K.p1_bits = in.p1_bits;
+    K.nb = L.nb;
+    K.target = slots * 7 / 10;
+    K.k = in.k;
+    K.keys = R.keys;
+    K.groups[0] = R.normal;
+    K.groups[1] = R.heavy;
+    K.groups_cap = L.groups_cap;
+    K.ctr = R.ctr;
+    if (L.n_slices) {
+        k_binhist<<<(unsigned)L.n_slices, P2_THREADS, 0, st>>>(K);
+        P2_CK(cudaGetLastError(), "k_binhist");
+        k_binscan<<<in.p1, P2_THREADS, 0, st>>>(K);
+        P2_CK(cudaGetLastError(), "k_binscan");
+        if (W == 1) k_keys<1><<<(unsigned)L.n_slices, P2_THREADS, 0, st>>>(K);
+        else k_keys<2><<<(unsigned)L.n_slices, P2_THREADS, 0, st>>>(K);
+        P2_CK(cudaGetLastError(), "k_keys");
+        *launches += 3;
     }
-    *launches += 3;
-    return cudaGetLastError();
+    if (ev_keys) P2_CK(cudaEventRecord(ev_keys, st), "event");
+
+    CountParams Q{};
+    Q.keys = R.keys;
+    Q.list[0] = R.normal;
+    Q.list[1] = R.heavy;
+    Q.n_list = R.ctr + P2C_NORMAL;  // [0] normal, [1] heavy: the heavy groups go first
+    Q.fallback = R.fb;
+    Q.fallback_cap = FALLBACK_CAP;
+    Q.ci = in.ci;
+    Q.cx = in.cx;
+    Q.out_keys = out.keys;
+    Q.out_counts = out.counts;
+    Q.out_cap = out.cap;
+    Q.ctr = R.ctr;
+    Q.retry_cap = L.retry_cap;
+    Q.smem_slots = slots;
+    const size_t sm = count_smem_bytes(W, slots);
+    if (W == 1)
+        P2_CK(cudaFuncSetAttribute(k_count<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm), "smem");
+    else
+        P2_CK(cudaFuncSetAttribute(k_count<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm), "smem");
+    unsigned long long h[P2C_COUNT];
+    for (int pass = 0;; ++pass) {
+        // pass p writes its split groups to retry[p & 1]; pass p + 1 counts them
+        Q.retry = R.retry[pass & 1];
+        Q.n_retry = R.aux + (pass & 1);
+        P2_CK(cudaMemsetAsync(Q.n_retry, 0, 8, st), "memset");
+        P2_CK(cudaMemsetAsync(R.ctr + P2C_WORK, 0, 8, st), "memset");
+        if (W == 1) k_count<1><<<in.n_sm, P2_THREADS, sm, st>>>(Q);
+        else k_count<2><<<in.n_sm, P2_THREADS, sm, st>>>(Q);
+        P2_CK(cudaGetLastError(), "k_count");
+        ++*launches;
+        unsigned long long nret = 0;
+        P2_CK(cudaMemcpyAsync(&nret, Q.n_retry, 8, cudaMemcpyDeviceToHost, st), "d2h");
+        P2_CK(cudaMemcpyAsync(h, R.ctr, sizeof h, cudaMemcpyDeviceToHost, st), "d2h");
+        P2_CK(cudaStreamSynchronize(st), "phase 2");
+        if (pass == 0 && (h[P2C_NORMAL] > L.groups_cap || h[P2C_HEAVY] > L.groups_cap)) {
+            err = "group list overflow";
+            return TG_ERR_TABLE;
+        }
+        if (nret > L.retry_cap) { err = "too many groups to split"; return TG_ERR_TABLE; }
+        if (nret == 0) break;
+        const unsigned long long nl[2] = {0, nret};
+        P2_CK(cudaMemcpyAsync(R.aux + 2, nl, 16, cudaMemcpyHostToDevice, st), "h2d");
+        Q.list[0] = Q.list[1] = R.retry[pass & 1];
+        Q.n_list = R.aux + 2;
+    }
+    out.fallback_groups = h[P2C_FALLBACK];
+    // ---- key ranges that did not fit in shared memory
+    if (h[P2C_FALLBACK] > 0) {
+        if (h[P2C_FALLBACK] > FALLBACK_CAP) { err = "too many overflowing groups"; return TG_ERR_TABLE; }
+        std::vector<Group> fl(h[P2C_FALLBACK]);
+        P2_CK(cudaMemcpyAsync(fl.data(), R.fb, fl.size() * sizeof(Group), cudaMemcpyDeviceToHost, st), "d2h");
+        P2_CK(cudaStreamSynchronize(st), "d2h");
+        for (const Group& g : fl) {
+            uint64_t S = 1024;
+            while (S < 2 * (g.hi - g.lo) + 2) S <<= 1;
+            if (S > (1ull << 32)) { err = "fallback table too large"; return TG_ERR_TABLE; }
+            const size_t kbytes = (size_t)S * key_bytes(W);
+            uint8_t* tab = static_cast<uint8_t*>(fallback_table(kbytes + (size_t)S * 4 + 16));
+            if (!tab) { err = "no room for the fallback table"; return TG_ERR_OOM; }
+            FallbackParams F{};
+            F.keys = R.keys;
+            F.lo = g.lo;
+            F.hi = g.hi;
+            F.parts = g.parts;
+            F.part = g.part;
+            F.tkeys = tab;
+            F.tcnt = reinterpret_cast<uint32_t*>(tab + kbytes);
+            F.mask = (uint32_t)(S - 1);
+            F.fail = reinterpret_cast<uint32_t*>(tab + kbytes + (size_t)S * 4);
+            P2_CK(cudaMemsetAsync(F.fail, 0, 4, st), "memset");
+            const unsigned grid = (unsigned)in.n_sm * 4;
+            if (W == 1) {
+                k_fb_init<1><<<grid, 256, 0, st>>>(F.tkeys, F.tcnt, S);
+                k_fb_insert<1><<<grid, 256, 0, st>>>(F);
+                k_fb_extract<1><<<grid, 256, 0, st>>>(F.tkeys, F.tcnt, S, Q);
+            } else {
+                k_fb_init<2><<<grid, 256, 0, st>>>(F.tkeys, F.tcnt, S);
+                k_fb_insert<2><<<grid, 256, 0, st>>>(F);
+                k_fb_extract<2><<<grid, 256, 0, st>>>(F.tkeys, F.tcnt, S, Q);
+            }
+            P2_CK(cudaGetLastError(), "fallback");
+            *launches += 3;
+            uint32_t failed = 0;
+            P2_CK(cudaMemcpyAsync(&failed, F.fail, 4, cudaMemcpyDeviceToHost, st), "d2h");
+            P2_CK(cudaStreamSynchronize(st), "fallback");
+            if (failed) { err = "fallback table overflow"; return TG_ERR_TABLE; }
+        }
+        P2_CK(cudaMemcpyAsync(h, R.ctr, sizeof h, cudaMemcpyDeviceToHost, st), "d2h");
+        P2_CK(cudaStreamSynchronize(st), "fallback");
+    }
+    out.n_out = h[P2C_OUT];
+    out.distinct = h[P2C_DISTINCT];
+    out.groups = h[P2C_NORMAL] + h[P2C_HEAVY];
+    out.heavy_groups = h[P2C_HEAVY];
+    if (out.n_out > out.cap) { err = "output capacity exceeded"; return TG_ERR_TABLE; }
+    return TG_OK;
 }
 
 }  // namespace tg
