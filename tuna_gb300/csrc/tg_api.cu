@@ -322,12 +322,12 @@ static tg_status run_cut(tg_job* j, bool exp, uint32_t p1_bits, int* launches) {
     tg_ctx* ctx = j->ctx;
     const uint64_t n = j->n;
     const uint32_t p1 = 1u << p1_bits;
-    const size_t smem = cut_smem_bytes(j->w, p1, exp);
+    const size_t smem = cut_smem_bytes(j->w, j->o.k, p1, exp);
     if (smem > ctx->smem_optin) return ctx->fail(TG_ERR_UNSUPPORTED, "phase-1 tile does not fit in shared memory");
-    const uint32_t per_sm = std::max<uint32_t>(1, std::min<uint32_t>(2, (uint32_t)(228u * 1024u / (smem + 1024))));
-    uint32_t C = (uint32_t)ctx->n_sm * per_sm;
+    const uint64_t tile = cut_tile(j->w, exp);
+    uint32_t C = (uint32_t)ctx->n_sm * cut_ctas_per_sm(j->w, j->o.k, p1, exp);
     uint64_t chunk = (n + C - 1) / C;
-    chunk = std::max<uint64_t>(CUT_TILE, (chunk + CUT_TILE - 1) / CUT_TILE * CUT_TILE);
+    chunk = std::max<uint64_t>(tile, (chunk + tile - 1) / tile * tile);
     C = (uint32_t)std::max<uint64_t>(1, (n + chunk - 1) / chunk);
     j->n_cta = C;
     j->chunk = chunk;
@@ -335,7 +335,7 @@ static tg_status run_cut(tg_job* j, bool exp, uint32_t p1_bits, int* launches) {
     // descriptors: about 2/(w+2) records per k-mer for random minimizers; grow on overflow
     double factor = std::min(1.0, 3.0 / (j->w + 2));
     for (int attempt = 0; attempt < 2; ++attempt) {
-        const uint64_t cap = (uint64_t)(chunk * factor) + 2ull * CUT_TILE + j->L + 64;
+        const uint64_t cap = (uint64_t)(chunk * factor) + 2ull * tile + j->L + 64;
         j->desc_cap = cap;
         CK(ctx->ensure(ctx->desc, (size_t)C * cap * 8), "alloc descriptors");
         if (exp) CK(ctx->ensure(ctx->xdesc, (size_t)C * cap * 24), "alloc export descriptors");
@@ -392,7 +392,7 @@ tg_status tg_job_run(tg_job* j) {
     }
     CK(ctx->ensure(ctx->misc, MISC_BYTES), "alloc misc");
     // ---- pack
-    uint64_t pw = (TG_PAD + n + CUT_TILE + 2 * MAX_W + 640) / 16 + 16;
+    uint64_t pw = (TG_PAD + n + CUT_SPAN + 2 * MAX_W + 640) / 16 + 16;
     pw = (pw + 1) & ~uint64_t(1);
     j->packed_words = pw;
     CK(ctx->ensure(ctx->packed, pw * 4), "alloc packed");

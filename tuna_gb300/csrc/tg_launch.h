@@ -11,7 +11,9 @@
 #include "tg_internal.cuh"
 
 namespace tg {
-size_t cut_smem_bytes(int w, uint32_t p1, bool exp);
+size_t cut_smem_bytes(int w, int k, uint32_t p1, bool exp);
+uint64_t cut_tile(int w, bool exp);                 // k-mer start positions per tile of a cut CTA
+uint32_t cut_ctas_per_sm(int w, int k, uint32_t p1, bool exp);
 cudaError_t launch_pack(const uint8_t* seq, uint64_t n, uint32_t* packed, uint32_t* valid, uint64_t n_words,
                         unsigned long long* n_bases, cudaStream_t st);
 cudaError_t launch_cut(const CutParams& P, const HashTables* gT, bool exp, cudaStream_t st);

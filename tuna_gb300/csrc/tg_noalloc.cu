@@ -119,7 +119,7 @@ extern "C" tg_status tg_count_seq_device_noalloc(const tg_job_opts* opts, const 
     // ---- fixed pieces
     HashTables* tables = cv.take<HashTables>(1);
     unsigned long long* misc = cv.take<unsigned long long>(32);  // counters, see below
-    uint64_t pw = (TG_PAD + n + CUT_TILE + 2 * MAX_W + 640) / 16 + 16;
+    uint64_t pw = (TG_PAD + n + CUT_SPAN + 2 * MAX_W + 640) / 16 + 16;
     pw = (pw + 1) & ~uint64_t(1);
     uint32_t* packed = cv.take<uint32_t>(pw);
     uint32_t* valid = cv.take<uint32_t>(pw / 2 + 16);
@@ -128,13 +128,12 @@ extern "C" tg_status tg_count_seq_device_noalloc(const tg_job_opts* opts, const 
     uint32_t p1_bits = 0;
     while ((1u << p1_bits) < p1) ++p1_bits;
     p1 = 1u << p1_bits;
-    const size_t smem = cut_smem_bytes(w, p1, false);
-    const uint32_t per_sm = std::max<uint32_t>(1, std::min<uint32_t>(2, (uint32_t)(228u * 1024u / (smem + 1024))));
-    uint32_t C = (uint32_t)n_sm * per_sm;
+    const uint64_t tile = cut_tile(w, false);
+    uint32_t C = (uint32_t)n_sm * cut_ctas_per_sm(w, k, p1, false);
     uint64_t chunk = (n + C - 1) / C;
-    chunk = std::max<uint64_t>(CUT_TILE, (chunk + CUT_TILE - 1) / CUT_TILE * CUT_TILE);
+    chunk = std::max<uint64_t>(tile, (chunk + tile - 1) / tile * tile);
     C = (uint32_t)std::max<uint64_t>(1, (n + chunk - 1) / chunk);
-    const uint64_t desc_cap = chunk + 2ull * CUT_TILE + L + 64;
+    const uint64_t desc_cap = chunk + 2ull * tile + L + 64;
     uint64_t* desc = cv.take<uint64_t>((size_t)C * desc_cap);
     uint32_t* n_desc = cv.take<uint32_t>(C);
     const uint64_t nhist = (uint64_t)p1 * C;

@@ -17,6 +17,8 @@
 // a chain a forced split falls every L = hdr_max + 1 - k k-mers after the
 // chain start (the cap of partition_hash.hpp:81 replayed from the chain
 // start); a record ends at the next cut or at the end of the run.
+#include <algorithm>
+
 #include "tg_internal.cuh"
 
 namespace tg {
@@ -450,6 +452,299 @@ k_cut(CutParams P, const HashTables* __restrict__ gT) {
     }
 }
 
+// ---------------------------------------------------------------- sequential cut
+// The counting path's cut (no export): each thread walks SEG consecutive k-mer
+// start positions in order, as the reference walks a run, with a rolling
+// ntHash and a block minimum over the window of w+1 m-mer hashes (van Herk /
+// Gil-Werman: blocks of w+1 m-mers aligned to the thread's first m-mer; the
+// window minimum is min(suffix minimum of the previous block, prefix minimum
+// of the current one); the two per-thread buffers sit in shared memory, entry
+// q of thread t at q * NT + t). Records whose start and end fall in one
+// thread's segment are written during the walk; two block scans per tile of
+// NT * SEG positions then give each thread the chain in force at its first
+// position (for the forced split every L k-mers) and the next cut after its
+// last one, which close the records that cross segments. A record that is open
+// at the tile's end is carried to the next tile.
+constexpr int SEG = 64;
+
+struct SeqSmem {
+    size_t tables, hist_r, hist_k, pk, vb, vh, vs, sum, total;
+    uint32_t npk, nvb;
+    __host__ __device__ static size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+    __host__ __device__ void layout(int w, uint32_t p1, int nt, int k) {
+        // bases [t0 - 1, t0 + nt * SEG + k) from a 32-base boundary
+        const uint32_t span = (uint32_t)nt * SEG + (uint32_t)k + 96;
+        npk = span / 16 + 2;
+        nvb = span / 32 + 2;
+        size_t o = 0;
+        tables = o; o = align16(o + sizeof(HashTables));
+        hist_r = o; o = align16(o + 4 * (size_t)p1);
+        hist_k = o; o = align16(o + 4 * (size_t)p1);
+        pk = o; o = align16(o + 4 * (size_t)npk);
+        vb = o; o = align16(o + 4 * (size_t)nvb);
+        vh = o; o = align16(o + 8 * (size_t)(w + 1) * nt);
+        vs = o; o = align16(o + 8 * (size_t)(w + 1) * nt);
+        sum = o; o = align16(o + 20 * (size_t)nt);  // i64 chain, i64 first cut, u32 chain mlo
+        total = o;
+    }
+};
+
+// Threads of the sequential cut for window w (the block buffers hold 2(w+1)
+// hashes per thread).
+__host__ __device__ inline int seq_threads(int w) { return w <= 15 ? 256 : (w <= 31 ? 128 : 64); }
+
+// Exclusive max over lower threads of v (-1: none); `all` = inclusive max of the block.
+template <int NT>
+__device__ __forceinline__ int seq_excl_max(int v, int* s_w, int& all) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x = max(x, y);
+    }
+    int ex = __shfl_up_sync(0xffffffffu, x, 1);
+    if (lane == 0) ex = -1;
+    if (lane == 31) s_w[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int t = lane < NT / 32 ? s_w[lane] : -1;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t = max(t, y);
+        }
+        if (lane < NT / 32) s_w[lane] = t;
+    }
+    __syncthreads();
+    const int before = wid ? s_w[wid - 1] : -1;
+    all = s_w[NT / 32 - 1];
+    __syncthreads();
+    return max(before, ex);
+}
+
+// Exclusive min over higher threads of v (NT: none); `all` = min of the block.
+template <int NT>
+__device__ __forceinline__ int seq_excl_min_rev(int v, int* s_w, int& all) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    constexpr int NW = NT / 32;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_down_sync(0xffffffffu, x, o);
+        if (lane + o < 32) x = min(x, y);
+    }
+    int ex = __shfl_down_sync(0xffffffffu, x, 1);
+    if (lane == 31) ex = NT;
+    if (lane == 0) s_w[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int t = lane < NW ? s_w[lane] : NT;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_down_sync(0xffffffffu, t, o);
+            if (lane + o < 32) t = min(t, y);
+        }
+        if (lane < NW) s_w[lane] = t;
+    }
+    __syncthreads();
+    const int after = wid + 1 < NW ? s_w[wid + 1] : NT;
+    all = s_w[0];
+    __syncthreads();
+    return min(after, ex);
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT, NT == 256 ? 3 : 2)
+k_cut_seq(CutParams P, const HashTables* __restrict__ gT) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    SeqSmem L;
+    L.layout(P.w, 1u << P.p1_bits, NT, P.k);
+    HashTables& T = *reinterpret_cast<HashTables*>(smem + L.tables);
+    uint32_t* s_hr = reinterpret_cast<uint32_t*>(smem + L.hist_r);
+    uint32_t* s_hk = reinterpret_cast<uint32_t*>(smem + L.hist_k);
+    uint32_t* s_pk = reinterpret_cast<uint32_t*>(smem + L.pk);
+    uint32_t* s_vb = reinterpret_cast<uint32_t*>(smem + L.vb);
+    uint64_t* vH = reinterpret_cast<uint64_t*>(smem + L.vh);
+    uint64_t* vS = reinterpret_cast<uint64_t*>(smem + L.vs);
+    int64_t* s_cs = reinterpret_cast<int64_t*>(smem + L.sum);  // chain in force after the segment's last cut
+    int64_t* s_fe = s_cs + NT;                                  // the segment's first cut (-1: none)
+    uint32_t* s_cm = reinterpret_cast<uint32_t*>(s_fe + NT);    // mlo of s_cs
+    __shared__ int s_w[NT / 32];
+    __shared__ int64_t s_carry_cs;   // chain in force at the tile start (-1: none)
+    __shared__ uint32_t s_carry_m;
+    __shared__ int64_t s_open;       // record open at the tile start (-1: none)
+    __shared__ uint32_t s_open_m;
+    __shared__ int s_open_own;
+    __shared__ uint32_t s_ndesc;
+
+    const int tid = threadIdx.x, lane = tid & 31;
+    const uint32_t p1 = 1u << P.p1_bits;
+    const int k = P.k, m = P.m, w = P.w, B = w + 1;
+    const uint32_t c = blockIdx.x;
+    {
+        const uint64_t* src = reinterpret_cast<const uint64_t*>(gT);
+        uint64_t* dst = reinterpret_cast<uint64_t*>(&T);
+        for (int i = tid; i < (int)(sizeof(HashTables) / 8); i += NT) dst[i] = src[i];
+        for (uint32_t i = tid; i < p1; i += NT) { s_hr[i] = 0; s_hk[i] = 0; }
+        if (tid == 0) { s_carry_cs = -1; s_carry_m = 0; s_open = -1; s_open_m = 0; s_open_own = 0; s_ndesc = 0; }
+    }
+    __syncthreads();
+
+    const int64_t cstart = (int64_t)c * (int64_t)P.chunk;
+    const int64_t cend = min(cstart + (int64_t)P.chunk, (int64_t)P.n);
+    const uint64_t kmask = (1ull << k) - 1;  // k <= 63
+    const int64_t Lr = P.L;
+    unsigned long long loc_kmers = 0, loc_recs = 0, loc_runs = 0;
+    bool overflowed = false;
+    uint64_t* dlist = P.desc + (uint64_t)c * P.desc_cap;
+    auto owned = [&](int64_t cs) { return cs >= cstart && cs < cend; };
+    auto put = [&](uint32_t idx, int64_t st, uint32_t nk, uint32_t mlo) {
+        if (idx < P.desc_cap) dlist[idx] = desc_pack((uint64_t)st, nk, mlo);
+        else overflowed = true;
+        const uint32_t b = mlo & (p1 - 1);
+        atomicAdd(&s_hr[b], 1u);
+        atomicAdd(&s_hk[b], nk);
+        loc_kmers += nk;
+        loc_recs += 1;
+    };
+    // all lanes call this together; lanes with e write one record each
+    auto emit_warp = [&](bool e, int64_t st, uint32_t nk, uint32_t mlo) {
+        const unsigned bal = __ballot_sync(0xffffffffu, e);
+        if (!bal) return;
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&s_ndesc, (uint32_t)__popc(bal));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (e) put(base + __popc(bal & ((1u << lane) - 1)), st, nk, mlo);
+    };
+
+    for (int64_t t0 = cstart; t0 < (int64_t)P.n; t0 += (int64_t)NT * SEG) {
+        if (t0 >= cend && !(s_open >= 0 && s_open_own)) break;  // nothing of ours is still open
+        // ---- stage packed and validity words: array bases [A0, A0 + 16 npk)
+        const uint64_t A0 = (uint64_t)(t0 + TG_PAD - 1) & ~uint64_t(31);
+        for (uint32_t i = tid; i < L.npk; i += NT) s_pk[i] = P.packed[(A0 >> 4) + i];
+        for (uint32_t i = tid; i < L.nvb; i += NT) s_vb[i] = P.valid[(A0 >> 5) + i];
+        __syncthreads();
+
+        // ---- pass 1: walk positions [ps, ps + SEG) (m-mers from ps - 1 on)
+        const int64_t ps = t0 + (int64_t)tid * SEG;
+        const uint32_t ra = (uint32_t)((uint64_t)(ps - 1 + TG_PAD) - A0);  // staged index of m-mer ps - 1
+        uint64_t f, r;
+        nt_init(T, s_pk, ra, m, f, r);
+        int64_t inv_last;  // last invalid base among those entered so far
+        {
+            const uint64_t inval = ~valid64(s_vb, ra) & kmask;  // bases ps - 1 .. ps - 2 + k
+            inv_last = inval ? ps - 1 + (63 - __clzll((long long)inval)) : ps - 2;
+        }
+        uint64_t pmin = ~0ull, mprev = 0;
+        bool vprev = false;
+        int64_t first_ev = -1, last_ev = -1, last_cs = -1;
+        bool last_is_cs = false, open = false;
+        int64_t rs = 0;
+        uint32_t rm = 0, last_cs_m = 0;
+        int o = 0;  // offset of the m-mer in its block
+        for (int i = 0; i <= SEG + w; ++i) {
+            const uint32_t rin = ra + (uint32_t)(i + m - 1);  // base entering the m-mer (and the k-mer)
+            if (i > 0) nt_roll(T, base_at(s_pk, ra + (uint32_t)i - 1), base_at(s_pk, rin), f, r);
+            const uint64_t h = f ^ r;
+            vH[o * NT + tid] = h;
+            pmin = min(pmin, h);
+            if (i >= w) {
+                const int64_t p = ps - 1 + (i - w);  // k-mer whose window ends at this m-mer
+                const uint64_t M = o == B - 1 ? pmin : min(vS[(o + 1) * NT + tid], pmin);
+                if (i > w && !valid_base(s_vb, rin)) inv_last = p + k - 1;
+                const bool v = inv_last < p;
+                if (i > w) {
+                    const bool first = v && !vprev;
+                    const bool cs = v && (first || M != mprev);
+                    const bool cut = cs || (!v && vprev);  // a new chain, or the end of a run
+                    if (first && p >= cstart && p < cend) ++loc_runs;
+                    const bool close = cut && open && owned(rs);
+                    emit_warp(close, rs, (uint32_t)(p - rs), rm);
+                    if (cut) {
+                        if (first_ev < 0) first_ev = p;
+                        last_ev = p;
+                        last_is_cs = cs;
+                        open = cs;
+                        if (cs) { rs = p; rm = (uint32_t)(M & 0xFFFFFu); last_cs = p; last_cs_m = rm; }
+                    }
+                }
+                mprev = M;
+                vprev = v;
+            }
+            if (o == B - 1) {
+                // block end: its suffix minima, for the windows of the next block
+                uint64_t sm = ~0ull;
+                for (int q = B - 1; q >= 0; --q) {
+                    sm = min(sm, vH[q * NT + tid]);
+                    vS[q * NT + tid] = sm;
+                }
+                pmin = ~0ull;
+                o = 0;
+            } else {
+                ++o;
+            }
+        }
+        // ---- chain in force at the segment start: the last cut of a lower thread
+        s_cs[tid] = last_is_cs ? last_cs : -1;
+        s_cm[tid] = last_cs_m;
+        int last_t;
+        const int prev = seq_excl_max<NT>(last_ev >= 0 ? tid : -1, s_w, last_t);
+        int64_t cs_in = s_carry_cs;
+        uint32_t m_in = s_carry_m;
+        if (prev >= 0) { cs_in = s_cs[prev]; m_in = s_cm[prev]; }
+        // forced split of that chain inside the segment (L > SEG: at most one)
+        int64_t fc = -1;
+        if (cs_in >= 0) {
+            const int64_t d = ps - cs_in;
+            const int64_t rem = d % Lr;
+            const int64_t cand = ps + (rem ? Lr - rem : 0);
+            if (cand < ps + SEG && (first_ev < 0 || cand < first_ev)) fc = cand;
+        }
+        // a forced-split record closed by the segment's first cut
+        emit_warp(fc >= 0 && first_ev >= 0 && owned(cs_in), fc, (uint32_t)(first_ev - fc), m_in);
+        // the record open at the segment's end, if it starts in the segment
+        bool oo = false, oown = false;
+        int64_t os = 0;
+        uint32_t om = 0;
+        if (open) { oo = true; os = rs; om = rm; oown = owned(rs); }
+        else if (fc >= 0 && first_ev < 0) { oo = true; os = fc; om = m_in; oown = owned(cs_in); }
+        const int64_t fe = fc >= 0 ? fc : first_ev;
+        s_fe[tid] = fe;
+        int first_t;
+        const int nxt = seq_excl_min_rev<NT>(fe >= 0 ? tid : NT, s_w, first_t);
+        emit_warp(oo && nxt < NT && oown, os, nxt < NT ? (uint32_t)(s_fe[nxt] - os) : 0u, om);
+        // ---- tile carries: the record open at the tile start closes at the
+        // tile's first cut; the last open record and the last chain carry on
+        if (tid == 0 && first_t < NT && s_open >= 0) {
+            if (s_open_own) put(atomicAdd(&s_ndesc, 1u), s_open, (uint32_t)(s_fe[first_t] - s_open), s_open_m);
+            s_open = -1;
+        }
+        __syncthreads();
+        if (oo && nxt == NT) { s_open = os; s_open_m = om; s_open_own = oown ? 1 : 0; }
+        if (tid == 0 && last_t >= 0) { s_carry_cs = s_cs[last_t]; s_carry_m = s_cm[last_t]; }
+        __syncthreads();
+    }
+    // ---- flush histograms and counters
+    for (uint32_t i = tid; i < p1; i += NT) {
+        P.hist[(uint64_t)i * P.n_cta + c] = s_hr[i];
+        if (s_hk[i]) atomicAdd(reinterpret_cast<unsigned long long*>(P.hist + hist_kmers_offset(p1, P.n_cta)) + i,
+                               (unsigned long long)s_hk[i]);
+    }
+    if (tid == 0) P.n_desc[c] = s_ndesc;
+    if (overflowed) atomicExch(P.overflow, 1u);
+    for (int o = 16; o > 0; o >>= 1) {
+        loc_kmers += __shfl_down_sync(0xffffffffu, loc_kmers, o);
+        loc_recs += __shfl_down_sync(0xffffffffu, loc_recs, o);
+        loc_runs += __shfl_down_sync(0xffffffffu, loc_runs, o);
+    }
+    if (lane == 0) {
+        if (loc_kmers) atomicAdd(&P.stats[0], loc_kmers);
+        if (loc_recs) atomicAdd(&P.stats[1], loc_recs);
+        if (loc_runs) atomicAdd(&P.stats[2], loc_runs);
+    }
+}
+
 // ---------------------------------------------------------------- offsets
 // Exclusive scan of two u32 arrays of length n into u64 outputs, one CTA per
 // SCAN_ITEMS items, then a fix-up with the scanned block sums.
@@ -525,10 +820,23 @@ k_bucket(BucketParams P) {
 }
 
 // ---------------------------------------------------------------- launchers
-size_t cut_smem_bytes(int w, uint32_t p1, bool exp) {
-    CutSmem L;
-    L.layout(w, p1, exp);
+size_t cut_smem_bytes(int w, int k, uint32_t p1, bool exp) {
+    if (exp) {
+        CutSmem L;
+        L.layout(w, p1, exp);
+        return L.total;
+    }
+    SeqSmem L;
+    L.layout(w, p1, seq_threads(w), k);
     return L.total;
+}
+
+uint64_t cut_tile(int w, bool exp) { return exp ? (uint64_t)CUT_TILE : (uint64_t)seq_threads(w) * SEG; }
+
+uint32_t cut_ctas_per_sm(int w, int k, uint32_t p1, bool exp) {
+    const size_t sm = cut_smem_bytes(w, k, p1, exp) + 1024;
+    const uint32_t by_smem = (uint32_t)(228u * 1024u / sm);
+    return std::max<uint32_t>(1, std::min<uint32_t>(exp ? 2u : 3u, by_smem));
 }
 
 cudaError_t launch_pack(const uint8_t* seq, uint64_t n, uint32_t* packed, uint32_t* valid, uint64_t n_words,
@@ -540,19 +848,27 @@ cudaError_t launch_pack(const uint8_t* seq, uint64_t n, uint32_t* packed, uint32
     return cudaGetLastError();
 }
 
+template <int NT>
+static cudaError_t launch_cut_seq(const CutParams& P, const HashTables* gT, size_t sm, cudaStream_t st) {
+    const cudaError_t e = cudaFuncSetAttribute(k_cut_seq<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    k_cut_seq<NT><<<P.n_cta, NT, sm, st>>>(P, gT);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_cut(const CutParams& P, const HashTables* gT, bool exp, cudaStream_t st) {
-    const size_t sm = cut_smem_bytes(P.w, 1u << P.p1_bits, exp);
-    cudaError_t e;
+    const size_t sm = cut_smem_bytes(P.w, P.k, 1u << P.p1_bits, exp);
     if (exp) {
-        e = cudaFuncSetAttribute(k_cut<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        const cudaError_t e = cudaFuncSetAttribute(k_cut<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
         k_cut<true><<<P.n_cta, CUT_THREADS, sm, st>>>(P, gT);
-    } else {
-        e = cudaFuncSetAttribute(k_cut<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        if (e != cudaSuccess) return e;
-        k_cut<false><<<P.n_cta, CUT_THREADS, sm, st>>>(P, gT);
+        return cudaGetLastError();
     }
-    return cudaGetLastError();
+    switch (seq_threads(P.w)) {
+        case 256: return launch_cut_seq<256>(P, gT, sm, st);
+        case 128: return launch_cut_seq<128>(P, gT, sm, st);
+        default: return launch_cut_seq<64>(P, gT, sm, st);
+    }
 }
 
 cudaError_t launch_scan(const uint32_t* in, uint64_t n, unsigned long long* out, unsigned long long* sums,
