@@ -3,17 +3,16 @@
 //
 // A job runs, on the context's stream:
 //   k_pack      ASCII stream -> 2-bit codes + validity bits
-//   k_cut       minimizers, chain starts, forced splits -> record descriptors
-//               and per (bucket, CTA) histograms
-//   k_scan_*    exclusive scan of the histogram -> bucket offsets
-//   k_sizes     per-bucket descriptor counts (sizing; one host sync here)
-//   k_bucket    descriptors -> bucket-major order
-//   k_binhist   k-mer instances per minimizer bin of each slice of a bucket
-//   k_binscan   key offsets per (slice, bin); groups of whole bins
-//   k_keys      every canonical k-mer key, bin-major
-//   k_count     per group: keys streamed by bulk copies into a shared-memory
-//               table, ci/cx, compaction (again for groups split by key hash)
+//   k_cut_seq   minimizers, chain starts, forced splits -> record descriptors
+//               per CTA, k-mer instances per (bucket, bin) (one host sync here)
+//   k_scan_*    (bucket, bin) counts -> key offsets
+//   k_plan      groups of whole bins per bucket
+//   k_keys      every canonical k-mer key at its bin's cursor
+//   k_count     per group: keys into a shared-memory table, ci/cx, compaction
+//               (again for groups split by key hash)
 //   k_fb_*      (rare) key ranges that overflowed shared memory, global tables
+// The export of partition files runs the tile cut k_cut<true> instead, which
+// also yields each record's exact minimizer position.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -29,16 +28,6 @@
 #include "tg_internal.cuh"
 #include "tg_launch.h"
 #include "tuna_gpu.h"
-
-namespace tg {
-// per-bucket descriptor counts from the scanned offsets
-__global__ void k_sizes(const unsigned long long* off_r, uint32_t n_buckets, uint32_t C,
-                        unsigned long long* out_recs) {
-    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= n_buckets) return;
-    out_recs[b] = off_r[(uint64_t)(b + 1) * C] - off_r[(uint64_t)b * C];
-}
-}  // namespace tg
 
 using namespace tg;
 
@@ -111,7 +100,7 @@ struct tg_ctx {
     size_t smem_optin = 0;
     unsigned host_threads = 1;
     std::string err;
-    DevBuf seq, packed, valid, desc, xdesc, hist, offr, sums, sizes, records, scratch, okeys, ocnt,
+    DevBuf seq, packed, valid, desc, xdesc, hist, scratch, okeys, ocnt,
         misc, fbtab, tables;
     cudaEvent_t ev[12] = {};
     tg_job* active = nullptr;
@@ -203,7 +192,7 @@ tg_status tg_ctx_destroy(tg_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->st) cudaStreamSynchronize(ctx->st);
     DevBuf* bufs[] = {&ctx->seq, &ctx->packed, &ctx->valid, &ctx->desc, &ctx->xdesc, &ctx->hist,
-                      &ctx->offr, &ctx->sums, &ctx->sizes, &ctx->records, &ctx->scratch,
+                      &ctx->scratch,
                       &ctx->okeys, &ctx->ocnt, &ctx->misc, &ctx->fbtab, &ctx->tables};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
@@ -339,9 +328,14 @@ static tg_status run_cut(tg_job* j, bool exp, uint32_t p1_bits, int* launches) {
         j->desc_cap = cap;
         CK(ctx->ensure(ctx->desc, (size_t)C * cap * 8), "alloc descriptors");
         if (exp) CK(ctx->ensure(ctx->xdesc, (size_t)C * cap * 24), "alloc export descriptors");
-        const size_t kmers_off = 4 * (size_t)hist_kmers_offset(p1, C);
-        CK(ctx->ensure(ctx->hist, kmers_off + (size_t)p1 * 8), "alloc histograms");
-        CK(cudaMemsetAsync(ctx->hist.as<uint8_t>() + kmers_off, 0, (size_t)p1 * 8, ctx->st), "memset");
+        if (exp) {
+            const size_t kmers_off = 4 * (size_t)hist_kmers_offset(p1, C);
+            CK(ctx->ensure(ctx->hist, kmers_off + (size_t)p1 * 8), "alloc histograms");
+            CK(cudaMemsetAsync(ctx->hist.as<uint8_t>() + kmers_off, 0, (size_t)p1 * 8, ctx->st), "memset");
+        } else {
+            CK(ctx->ensure(ctx->hist, (size_t)4 << MLO_BITS), "alloc bin histogram");
+            CK(cudaMemsetAsync(ctx->hist.p, 0, (size_t)4 << MLO_BITS, ctx->st), "memset");
+        }
         CK(cudaMemsetAsync(ctx->misc.as<uint8_t>() + MISC_CUT_STATS, 0, 24, ctx->st), "memset");
         CK(cudaMemsetAsync(ctx->misc.as<uint8_t>() + MISC_OVERFLOW, 0, 4, ctx->st), "memset");
         CutParams P{};
@@ -355,7 +349,8 @@ static tg_status run_cut(tg_job* j, bool exp, uint32_t p1_bits, int* launches) {
         P.desc = ctx->desc.as<uint64_t>();
         P.desc_cap = cap;
         P.n_desc = reinterpret_cast<uint32_t*>(ctx->misc.as<uint8_t>() + MISC_NDESC);
-        P.hist = ctx->hist.as<uint32_t>();
+        P.hist = exp ? ctx->hist.as<uint32_t>() : nullptr;
+        P.binhist = exp ? nullptr : ctx->hist.as<uint32_t>();
         P.stats = reinterpret_cast<unsigned long long*>(ctx->misc.as<uint8_t>() + MISC_CUT_STATS);
         P.overflow = reinterpret_cast<uint32_t*>(ctx->misc.as<uint8_t>() + MISC_OVERFLOW);
         P.xdesc = exp ? ctx->xdesc.as<uint64_t>() : nullptr;
@@ -413,61 +408,33 @@ tg_status tg_job_run(tg_job* j) {
     tg_status s = run_cut(j, false, p1_bits, &launches);
     if (s != TG_OK) return s;
     unsigned long long cstats[3] = {0, 0, 0};
-    CK(cudaMemcpyAsync(cstats, ctx->misc.as<uint8_t>() + MISC_CUT_STATS, 24, cudaMemcpyDeviceToHost, ctx->st), "d2h");
     const uint32_t C = j->n_cta;
-    const uint64_t nhist = (uint64_t)p1 * C;
-    // ---- scan: descriptor offsets over [bucket][cta]
-    CK(ctx->ensure(ctx->offr, (nhist + 1) * 8), "alloc offsets");
-    CK(ctx->ensure(ctx->sums, ((nhist + 8191) / 8192 + 2) * 8), "alloc sums");
-    CK(cudaEventRecord(ctx->ev[4], ctx->st), "event");
-    CK(launch_scan(ctx->hist.as<uint32_t>(), nhist, ctx->offr.as<unsigned long long>(),
-                   ctx->sums.as<unsigned long long>(), ctx->offr.as<unsigned long long>() + nhist, ctx->st,
-                   &launches), "scan");
-    CK(ctx->ensure(ctx->sizes, (size_t)p1 * 8), "alloc sizes");
-    k_sizes<<<(p1 + 255) / 256, 256, 0, ctx->st>>>(ctx->offr.as<unsigned long long>(), p1, C,
-                                                   ctx->sizes.as<unsigned long long>());
-    ++launches;
-    CK(cudaGetLastError(), "k_sizes");
-    std::vector<unsigned long long> hsz(p1), hk(p1);
-    unsigned long long tot_r = 0;
-    CK(cudaMemcpyAsync(hsz.data(), ctx->sizes.p, (size_t)p1 * 8, cudaMemcpyDeviceToHost, ctx->st), "d2h");
-    const unsigned long long* bucket_kmers =
-        reinterpret_cast<const unsigned long long*>(ctx->hist.as<uint32_t>() + hist_kmers_offset(p1, C));
-    CK(cudaMemcpyAsync(hk.data(), bucket_kmers, (size_t)p1 * 8, cudaMemcpyDeviceToHost, ctx->st), "d2h");
-    CK(cudaMemcpyAsync(&tot_r, ctx->offr.as<unsigned long long>() + nhist, 8, cudaMemcpyDeviceToHost, ctx->st), "d2h");
+    std::vector<uint32_t> nd(C);
+    CK(cudaMemcpyAsync(cstats, ctx->misc.as<uint8_t>() + MISC_CUT_STATS, 24, cudaMemcpyDeviceToHost, ctx->st), "d2h");
+    CK(cudaMemcpyAsync(nd.data(), ctx->misc.as<uint8_t>() + MISC_NDESC, (size_t)C * 4, cudaMemcpyDeviceToHost,
+                       ctx->st), "d2h");
     CK(cudaStreamSynchronize(ctx->st), "phase 1");
-    // ---- buffers: bucketed descriptors, phase-2 scratch (keys included), output
+    // ---- buffers: phase-2 scratch (keys included), output
     const uint64_t n_kmers = cstats[0];
-    CK(ctx->ensure(ctx->records, tot_r * 8 + 64), "alloc bucket descriptors");
     const uint64_t out_cap = std::max<uint64_t>(n_kmers, 1);
     CK(ctx->ensure(ctx->okeys, out_cap * key_bytes(W)), "alloc output keys");
     CK(ctx->ensure(ctx->ocnt, out_cap * 4), "alloc output counts");
     P2Input in{};
     in.W = W;
     in.k = k;
-    in.p1 = p1;
     in.p1_bits = p1_bits;
     in.n_sm = (uint32_t)ctx->n_sm;
     in.packed = ctx->packed.as<uint32_t>();
-    in.bdesc = ctx->records.as<uint64_t>();
-    in.recs = hsz.data();
-    in.kmers = hk.data();
+    in.desc = ctx->desc.as<uint64_t>();
+    in.desc_cap = j->desc_cap;
+    in.n_lists = C;
+    in.n_desc = nd.data();
+    in.binhist = ctx->hist.as<uint32_t>();
+    in.n_kmers = n_kmers;
     in.ci = j->o.ci;
     in.cx = j->o.cx;
     const size_t p2_bytes = phase2_scratch_bytes(in);
     CK(ctx->ensure(ctx->scratch, p2_bytes), "alloc phase-2 scratch");
-    // ---- descriptors into bucket order
-    BucketParams BP{};
-    BP.p1_bits = p1_bits;
-    BP.n_cta = C;
-    BP.desc = ctx->desc.as<uint64_t>();
-    BP.desc_cap = j->desc_cap;
-    BP.n_desc = reinterpret_cast<const uint32_t*>(ctx->misc.as<uint8_t>() + MISC_NDESC);
-    BP.off_r = ctx->offr.as<unsigned long long>();
-    BP.bdesc = ctx->records.as<uint64_t>();
-    CK(cudaEventRecord(ctx->ev[5], ctx->st), "event");
-    CK(launch_bucket(BP, ctx->st), "k_bucket");
-    ++launches;
     CK(cudaEventRecord(ctx->ev[6], ctx->st), "event");
     // ---- phase 2
     P2Output out{};
@@ -497,13 +464,11 @@ tg_status tg_job_run(tg_job* j) {
     S.fallback_groups = out.fallback_groups;
     S.groups = out.groups;
     S.heavy_groups = (uint32_t)out.heavy_groups;
-    S.record_bytes = tot_r * 8;
+    S.record_bytes = cstats[1] * 8;
     cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]); S.pack_ms = ms;
     cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]); S.phase1_cut_ms = ms;
-    float scan_ms = 0;
-    cudaEventElapsedTime(&scan_ms, ctx->ev[4], ctx->ev[5]);
-    cudaEventElapsedTime(&ms, ctx->ev[5], ctx->ev[6]); S.phase1_scatter_ms = ms;
-    S.phase1_ms = S.phase1_cut_ms + scan_ms + S.phase1_scatter_ms;
+    S.phase1_scatter_ms = 0;  // records stay in the cut's lists
+    S.phase1_ms = S.phase1_cut_ms;
     cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[8]); S.phase2_ms = ms;
     cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]); S.phase2_keys_ms = ms;
     cudaEventElapsedTime(&ms, ctx->ev[7], ctx->ev[8]); S.phase2_count_ms = ms;

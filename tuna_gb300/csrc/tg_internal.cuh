@@ -10,8 +10,8 @@
 //   desc    u64[C][cap]      per Phase-1 CTA: one descriptor per superkmer record
 //                            (start position, k-mer count, low 20 bits of its
 //                            minimizer hash; see desc_pack)
-//   hist    u32[P][C]        records per (bucket, CTA), then u64[P] k-mers per bucket
-//   bdesc   u64[]            the descriptors again, bucket-major (phase 2 input)
+//   binhist u32[2^20]        k-mer instances per (bucket, bin): the 20 low bits of the
+//                            minimizer hash, bucket bits first; scanned into kofs
 //   keys    u64 x W [K]      every canonical k-mer instance, bucket-major and, inside
 //                            a bucket, grouped by minimizer bin (W = 1 for k <= 31)
 //   out     keys + u32 counts of the distinct k-mers that pass ci/cx
@@ -44,6 +44,7 @@ struct HashTables {
 // positions [start, start + nk) of the stream; its bases are read from
 // `packed` when it is counted. mlo = low 20 bits of the minimizer hash: the
 // low log2(P) bits pick the bucket, the rest the bin inside the bucket.
+constexpr int MLO_BITS = 20;
 constexpr int DESC_START_BITS = 36;
 __host__ __device__ __forceinline__ uint64_t desc_pack(uint64_t start, uint32_t nk, uint32_t mlo) {
     return start | ((uint64_t)nk << DESC_START_BITS) | ((uint64_t)(mlo & 0xFFFFFu) << 44);
@@ -51,6 +52,10 @@ __host__ __device__ __forceinline__ uint64_t desc_pack(uint64_t start, uint32_t 
 __host__ __device__ __forceinline__ uint64_t desc_start(uint64_t d) { return d & ((1ull << DESC_START_BITS) - 1); }
 __host__ __device__ __forceinline__ uint32_t desc_nk(uint64_t d) { return (uint32_t)(d >> DESC_START_BITS) & 0xFFu; }
 __host__ __device__ __forceinline__ uint32_t desc_mlo(uint64_t d) { return (uint32_t)(d >> 44); }
+// Index of (bucket, bin) of a minimizer's low bits in bucket-major order.
+__host__ __device__ __forceinline__ uint32_t bin_index(uint32_t mlo, uint32_t p1_bits) {
+    return ((mlo & ((1u << p1_bits) - 1)) << (MLO_BITS - p1_bits)) | (mlo >> p1_bits);
+}
 
 // Offset (in u32 units) of the u64 per-bucket k-mer counters that follow the
 // u32 [P][C] record histogram: rounded up so the u64 array is 8-byte aligned
@@ -71,29 +76,19 @@ struct CutParams {
     uint64_t* desc;          // [n_cta][desc_cap] record descriptors
     uint64_t desc_cap;
     uint32_t* n_desc;        // [n_cta]
-    uint32_t* hist;          // u32 [P][n_cta] records, then u64 [P] k-mers per bucket
+    uint32_t* hist;          // export cut: u32 [P][n_cta] records, then u64 [P] k-mers per bucket
+    uint32_t* binhist;       // counting cut: [2^20] k-mers per (bucket, bin), bucket-major
     unsigned long long* stats;  // [0] kmers, [1] records, [2] runs
     uint32_t* overflow;      // set when a CTA's descriptor list is full
     // export mode: full descriptors (start, minimizer hash, min_pos, nk)
     uint64_t* xdesc;         // [n_cta][desc_cap][3] or null
 };
 
-struct BucketParams {
-    uint32_t p1_bits;
-    uint32_t n_cta;
-    const uint64_t* desc;
-    uint64_t desc_cap;
-    const uint32_t* n_desc;
-    const unsigned long long* off_r;   // exclusive scan over [P][C] of records
-    uint64_t* bdesc;                   // descriptors in bucket order
-};
-
-// Phase 2 works on slices of the bucket-major descriptors (one slice never
-// spans two buckets) and on groups: runs of whole minimizer bins of one bucket
-// whose keys are contiguous in the key array.
+// Phase 2 works on slices of the phase-1 descriptor lists and on groups: runs
+// of whole minimizer bins of one bucket, whose keys are contiguous in the key
+// array (the keys are laid out bucket-major, bin-major inside a bucket).
 struct Slice {
-    uint64_t r_lo, r_hi;  // descriptor range in bdesc
-    uint32_t bucket, pad;
+    uint64_t r_lo, r_hi;  // descriptor range in the phase-1 lists
 };
 
 struct Group {
@@ -116,15 +111,13 @@ enum P2Counter : int {
 
 struct KeysParams {
     const uint32_t* packed;
-    const uint64_t* bdesc;
+    const uint64_t* desc;              // phase-1 descriptor lists
     const Slice* slices;
-    const uint32_t* slice_first;       // [P + 1] first slice of each bucket
-    const unsigned long long* kbase;   // [P + 1] first key of each bucket
-    uint32_t* shist;                   // [n_slices][nb]: k-mers per bin, then key offsets
-    uint32_t p1_bits, nb;              // nb = bins per bucket
+    unsigned long long* kofs;          // [2^20 + 1] first key of each (bucket, bin); advanced by k_keys
+    uint32_t p1_bits, nb;              // buckets, bins per bucket (p1 * nb = 2^20)
     uint32_t target;                   // k-mer instances per group
     int k;
-    void* keys;                        // u64 x W per k-mer instance, bin-major per bucket
+    void* keys;                        // u64 x W per k-mer instance
     Group* groups[2];                  // [0] normal, [1] heavy
     uint64_t groups_cap;
     unsigned long long* ctr;           // P2Counter

@@ -19,20 +19,22 @@ cudaError_t launch_pack(const uint8_t* seq, uint64_t n, uint32_t* packed, uint32
 cudaError_t launch_cut(const CutParams& P, const HashTables* gT, bool exp, cudaStream_t st);
 cudaError_t launch_scan(const uint32_t* in, uint64_t n, unsigned long long* out, unsigned long long* sums,
                         unsigned long long* total, cudaStream_t st, int* launches);
-cudaError_t launch_bucket(const BucketParams& P, cudaStream_t st);
 size_t key_bytes(int W);
 uint32_t count_slots(int W);
 
-// Phase 2 of one job, shared by the entry points: bucket-major descriptors in,
-// distinct keys and counts out.
+// Phase 2 of one job, shared by the entry points: the phase-1 descriptor lists
+// and (bucket, bin) k-mer counts in, distinct keys and counts out.
 struct P2Input {
     int W, k;                          // key words, k
-    uint32_t p1, p1_bits;              // buckets
+    uint32_t p1_bits;                  // log2 buckets
     uint32_t n_sm;
     const uint32_t* packed;
-    const uint64_t* bdesc;
-    const unsigned long long* recs;    // [p1] descriptors per bucket (host)
-    const unsigned long long* kmers;   // [p1] k-mer instances per bucket (host)
+    const uint64_t* desc;              // [n_lists][desc_cap] phase-1 descriptors
+    uint64_t desc_cap;
+    uint32_t n_lists;
+    const uint32_t* n_desc;            // [n_lists] descriptors per list (host)
+    const uint32_t* binhist;           // [2^20] k-mers per (bucket, bin) (device)
+    uint64_t n_kmers;                  // k-mer instances in all
     uint64_t ci, cx;
 };
 struct P2Output {
@@ -53,6 +55,4 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
 // ntHash roll / init tables for minimizer length m (host side).
 HashTables make_hash_tables(int m);
 
-__global__ void k_sizes(const unsigned long long* off_r, uint32_t n_buckets, uint32_t C,
-                        unsigned long long* out_recs);
 }  // namespace tg

@@ -8,8 +8,8 @@
 // pre-reserved pool), or a latency-critical loop where an allocation would
 // synchronise the device. tg_count_seq_device_noalloc takes the input and the
 // output buffers from the caller and keeps every intermediate array (packed
-// bases, superkmer descriptors, histograms, bucket offsets, bucketed
-// descriptors, k-mer keys, group lists, fallback table) in one file-scope device array of
+// bases, superkmer descriptors, the (bucket, bin) histogram and key offsets,
+// k-mer keys, group lists, fallback table) in one file-scope device array of
 // TG_NOALLOC_SCRATCH_BYTES that the CUDA runtime reserves when the library is
 // loaded on a device and that stays reserved until the process exits.
 //
@@ -136,13 +136,7 @@ extern "C" tg_status tg_count_seq_device_noalloc(const tg_job_opts* opts, const 
     const uint64_t desc_cap = chunk + 2ull * tile + L + 64;
     uint64_t* desc = cv.take<uint64_t>((size_t)C * desc_cap);
     uint32_t* n_desc = cv.take<uint32_t>(C);
-    const uint64_t nhist = (uint64_t)p1 * C;
-    uint32_t* hist = cv.take<uint32_t>(hist_kmers_offset(p1, C) + 2 * (size_t)p1);  // + u64 per-bucket k-mers
-    unsigned long long* bucket_kmers = reinterpret_cast<unsigned long long*>(hist + hist_kmers_offset(p1, C));
-    unsigned long long* offr = cv.take<unsigned long long>(nhist + 1);
-    const uint64_t nsum = (nhist + 8191) / 8192 + 1;
-    unsigned long long* sums = cv.take<unsigned long long>(nsum + 2);
-    unsigned long long* sizes = cv.take<unsigned long long>(p1);
+    uint32_t* binhist = cv.take<uint32_t>((size_t)1 << MLO_BITS);
     if (!cv.ok) { set_err(errbuf, errlen, "input too large for the no-allocation scratch"); return TG_ERR_ARG; }
     // counters in misc (u64 indices): [0..2] k-mers/records/runs, [3] bases, [4] overflow (u32)
     uint32_t* overflow = reinterpret_cast<uint32_t*>(misc + 4);
@@ -150,7 +144,7 @@ extern "C" tg_status tg_count_seq_device_noalloc(const tg_job_opts* opts, const 
     const HashTables T = make_hash_tables(m);
     NA_CK(cudaMemcpyAsync(tables, &T, sizeof T, cudaMemcpyHostToDevice, st), "upload tables");
     NA_CK(cudaMemsetAsync(misc, 0, 32 * 8, st), "memset");
-    NA_CK(cudaMemsetAsync(bucket_kmers, 0, (size_t)p1 * 8, st), "memset");
+    NA_CK(cudaMemsetAsync(binhist, 0, (size_t)4 << MLO_BITS, st), "memset");
     // ---- phase 1
     NA_CK(launch_pack(d_seq, n, packed, valid, pw, misc + 3, st), "k_pack");
     CutParams P{};
@@ -158,32 +152,22 @@ extern "C" tg_status tg_count_seq_device_noalloc(const tg_job_opts* opts, const 
     P.k = k; P.m = m; P.w = w; P.L = L;
     P.p1_bits = p1_bits; P.n_cta = C; P.chunk = chunk;
     P.desc = desc; P.desc_cap = desc_cap; P.n_desc = n_desc;
-    P.hist = hist; P.stats = misc; P.overflow = overflow; P.xdesc = nullptr;
+    P.hist = nullptr; P.binhist = binhist; P.stats = misc; P.overflow = overflow; P.xdesc = nullptr;
     NA_CK(launch_cut(P, tables, false, st), "k_cut");
     int launches = 0;
-    NA_CK(launch_scan(hist, nhist, offr, sums, offr + nhist, st, &launches), "scan");
-    k_sizes<<<(p1 + 255) / 256, 256, 0, st>>>(offr, p1, C, sizes);
-    NA_CK(cudaGetLastError(), "k_sizes");
-    std::vector<unsigned long long> hsz(p1), hk(p1);
-    unsigned long long tot_r = 0, cstats[3] = {0, 0, 0};
+    std::vector<uint32_t> nd(C);
+    unsigned long long cstats[3] = {0, 0, 0};
     uint32_t ovf = 0;
-    NA_CK(cudaMemcpyAsync(hsz.data(), sizes, (size_t)p1 * 8, cudaMemcpyDeviceToHost, st), "d2h");
-    NA_CK(cudaMemcpyAsync(hk.data(), bucket_kmers, (size_t)p1 * 8, cudaMemcpyDeviceToHost, st), "d2h");
-    NA_CK(cudaMemcpyAsync(&tot_r, offr + nhist, 8, cudaMemcpyDeviceToHost, st), "d2h");
+    NA_CK(cudaMemcpyAsync(nd.data(), n_desc, (size_t)C * 4, cudaMemcpyDeviceToHost, st), "d2h");
     NA_CK(cudaMemcpyAsync(cstats, misc, 24, cudaMemcpyDeviceToHost, st), "d2h");
     NA_CK(cudaMemcpyAsync(&ovf, overflow, 4, cudaMemcpyDeviceToHost, st), "d2h");
     NA_CK(cudaStreamSynchronize(st), "phase 1");
     if (ovf) { set_err(errbuf, errlen, "descriptor capacity exceeded"); return TG_ERR_DEVICE; }
-    // ---- bucketed descriptors, then phase 2 in what is left
-    uint64_t* bdesc = cv.take<uint64_t>(tot_r + 8);
-    if (!cv.ok) { set_err(errbuf, errlen, "input too large for the no-allocation scratch"); return TG_ERR_ARG; }
-    BucketParams BP{};
-    BP.p1_bits = p1_bits; BP.n_cta = C; BP.desc = desc; BP.desc_cap = desc_cap; BP.n_desc = n_desc;
-    BP.off_r = offr; BP.bdesc = bdesc;
-    NA_CK(launch_bucket(BP, st), "k_bucket");
+    // ---- phase 2 in what is left
     P2Input in{};
-    in.W = W; in.k = k; in.p1 = p1; in.p1_bits = p1_bits; in.n_sm = (uint32_t)n_sm;
-    in.packed = packed; in.bdesc = bdesc; in.recs = hsz.data(); in.kmers = hk.data();
+    in.W = W; in.k = k; in.p1_bits = p1_bits; in.n_sm = (uint32_t)n_sm;
+    in.packed = packed; in.desc = desc; in.desc_cap = desc_cap; in.n_lists = C; in.n_desc = nd.data();
+    in.binhist = binhist; in.n_kmers = cstats[0];
     in.ci = o.ci; in.cx = o.cx;
     const size_t p2_bytes = phase2_scratch_bytes(in);
     uint8_t* p2_scratch = cv.take<uint8_t>(p2_bytes);

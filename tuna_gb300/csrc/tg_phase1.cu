@@ -468,18 +468,16 @@ k_cut(CutParams P, const HashTables* __restrict__ gT) {
 constexpr int SEG = 64;
 
 struct SeqSmem {
-    size_t tables, hist_r, hist_k, pk, vb, vh, vs, sum, total;
+    size_t tables, pk, vb, vh, vs, sum, total;
     uint32_t npk, nvb;
     __host__ __device__ static size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
-    __host__ __device__ void layout(int w, uint32_t p1, int nt, int k) {
+    __host__ __device__ void layout(int w, int nt, int k) {
         // bases [t0 - 1, t0 + nt * SEG + k) from a 32-base boundary
         const uint32_t span = (uint32_t)nt * SEG + (uint32_t)k + 96;
         npk = span / 16 + 2;
         nvb = span / 32 + 2;
         size_t o = 0;
         tables = o; o = align16(o + sizeof(HashTables));
-        hist_r = o; o = align16(o + 4 * (size_t)p1);
-        hist_k = o; o = align16(o + 4 * (size_t)p1);
         pk = o; o = align16(o + 4 * (size_t)npk);
         vb = o; o = align16(o + 4 * (size_t)nvb);
         vh = o; o = align16(o + 8 * (size_t)(w + 1) * nt);
@@ -559,10 +557,8 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 2)
 k_cut_seq(CutParams P, const HashTables* __restrict__ gT) {
     extern __shared__ __align__(16) uint8_t smem[];
     SeqSmem L;
-    L.layout(P.w, 1u << P.p1_bits, NT, P.k);
+    L.layout(P.w, NT, P.k);
     HashTables& T = *reinterpret_cast<HashTables*>(smem + L.tables);
-    uint32_t* s_hr = reinterpret_cast<uint32_t*>(smem + L.hist_r);
-    uint32_t* s_hk = reinterpret_cast<uint32_t*>(smem + L.hist_k);
     uint32_t* s_pk = reinterpret_cast<uint32_t*>(smem + L.pk);
     uint32_t* s_vb = reinterpret_cast<uint32_t*>(smem + L.vb);
     uint64_t* vH = reinterpret_cast<uint64_t*>(smem + L.vh);
@@ -579,14 +575,12 @@ k_cut_seq(CutParams P, const HashTables* __restrict__ gT) {
     __shared__ uint32_t s_ndesc;
 
     const int tid = threadIdx.x, lane = tid & 31;
-    const uint32_t p1 = 1u << P.p1_bits;
     const int k = P.k, m = P.m, w = P.w, B = w + 1;
     const uint32_t c = blockIdx.x;
     {
         const uint64_t* src = reinterpret_cast<const uint64_t*>(gT);
         uint64_t* dst = reinterpret_cast<uint64_t*>(&T);
         for (int i = tid; i < (int)(sizeof(HashTables) / 8); i += NT) dst[i] = src[i];
-        for (uint32_t i = tid; i < p1; i += NT) { s_hr[i] = 0; s_hk[i] = 0; }
         if (tid == 0) { s_carry_cs = -1; s_carry_m = 0; s_open = -1; s_open_m = 0; s_open_own = 0; s_ndesc = 0; }
     }
     __syncthreads();
@@ -602,9 +596,7 @@ k_cut_seq(CutParams P, const HashTables* __restrict__ gT) {
     auto put = [&](uint32_t idx, int64_t st, uint32_t nk, uint32_t mlo) {
         if (idx < P.desc_cap) dlist[idx] = desc_pack((uint64_t)st, nk, mlo);
         else overflowed = true;
-        const uint32_t b = mlo & (p1 - 1);
-        atomicAdd(&s_hr[b], 1u);
-        atomicAdd(&s_hk[b], nk);
+        atomicAdd(&P.binhist[bin_index(mlo, P.p1_bits)], nk);  // the key array's layout
         loc_kmers += nk;
         loc_recs += 1;
     };
@@ -725,12 +717,7 @@ k_cut_seq(CutParams P, const HashTables* __restrict__ gT) {
         if (tid == 0 && last_t >= 0) { s_carry_cs = s_cs[last_t]; s_carry_m = s_cm[last_t]; }
         __syncthreads();
     }
-    // ---- flush histograms and counters
-    for (uint32_t i = tid; i < p1; i += NT) {
-        P.hist[(uint64_t)i * P.n_cta + c] = s_hr[i];
-        if (s_hk[i]) atomicAdd(reinterpret_cast<unsigned long long*>(P.hist + hist_kmers_offset(p1, P.n_cta)) + i,
-                               (unsigned long long)s_hk[i]);
-    }
+    // ---- counters
     if (tid == 0) P.n_desc[c] = s_ndesc;
     if (overflowed) atomicExch(P.overflow, 1u);
     for (int o = 16; o > 0; o >>= 1) {
@@ -797,28 +784,6 @@ __global__ void k_scan_add(unsigned long long* __restrict__ out, uint64_t n, con
     if (i < n) out[i] += sums[i / SCAN_ITEMS];
 }
 
-// ---------------------------------------------------------------- buckets
-// One CTA per Phase-1 chunk: its descriptors go to their bucket's range of
-// the bucket-major array (one 8-byte store each).
-constexpr int BUCKET_THREADS = 1024;
-
-__global__ void __launch_bounds__(BUCKET_THREADS)
-k_bucket(BucketParams P) {
-    extern __shared__ __align__(16) uint32_t cur[];  // [p1]
-    const uint32_t p1 = 1u << P.p1_bits;
-    for (uint32_t i = threadIdx.x; i < p1; i += BUCKET_THREADS) cur[i] = 0;
-    __syncthreads();
-    const uint32_t c = blockIdx.x;
-    const uint32_t nd = (uint32_t)min((uint64_t)P.n_desc[c], P.desc_cap);
-    const uint64_t* src = P.desc + (uint64_t)c * P.desc_cap;
-    for (uint32_t i = threadIdx.x; i < nd; i += BUCKET_THREADS) {
-        const uint64_t d = __ldcs(src + i);
-        const uint32_t b = desc_mlo(d) & (p1 - 1);
-        const uint32_t o = atomicAdd(&cur[b], 1u);
-        P.bdesc[P.off_r[(uint64_t)b * P.n_cta + c] + o] = d;
-    }
-}
-
 // ---------------------------------------------------------------- launchers
 size_t cut_smem_bytes(int w, int k, uint32_t p1, bool exp) {
     if (exp) {
@@ -827,7 +792,7 @@ size_t cut_smem_bytes(int w, int k, uint32_t p1, bool exp) {
         return L.total;
     }
     SeqSmem L;
-    L.layout(w, p1, seq_threads(w), k);
+    L.layout(w, seq_threads(w), k);
     return L.total;
 }
 
@@ -881,12 +846,5 @@ cudaError_t launch_scan(const uint32_t* in, uint64_t n, unsigned long long* out,
     return cudaGetLastError();
 }
 
-cudaError_t launch_bucket(const BucketParams& P, cudaStream_t st) {
-    const size_t sm = 4 * (size_t)(1u << P.p1_bits);
-    cudaError_t e = cudaFuncSetAttribute(k_bucket, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
-    k_bucket<<<P.n_cta, BUCKET_THREADS, sm, st>>>(P);
-    return cudaGetLastError();
-}
 
 }  // namespace tg

@@ -11,11 +11,11 @@
 //   keep ci <= count <= cx        src/count.hpp:202, :250, :287
 //
 // Pipeline (all instances of a canonical k-mer share its minimizer, hence its
-// bucket and its bin = further bits of the minimizer hash):
-//   k_binhist   per slice of a bucket's descriptors: k-mer instances per bin
-//   k_binscan   per bucket: key offset of every (slice, bin); greedy runs of
-//               whole bins of at most `target` k-mers become groups
-//   k_keys      per slice: every k-mer's canonical key, written bin-major, so
+// bucket and its bin = further bits of the minimizer hash; phase 1 counted the
+// k-mer instances of every (bucket, bin)):
+//   k_scan_*    (bucket, bin) counts -> key offsets, bucket-major
+//   k_plan      per bucket: groups of whole bins of about `target` k-mers
+//   k_keys      every k-mer's canonical key, written at its bin's cursor, so
 //               the keys of a group are one contiguous range of the key array
 //   k_count     persistent, one CTA per SM: each group's keys are read with
 //               coalesced loads (the next round's already in flight while one
@@ -153,143 +153,84 @@ __device__ __forceinline__ U128 kmer_key<2>(const uint32_t* __restrict__ pk, uin
     return key;
 }
 
-// Block-wide exclusive scan of one value per thread (blockDim == P2_THREADS);
-// `total` = the sum.
-__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_warp, uint32_t& total) {
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    uint32_t x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) s_warp[wid] = x;
-    __syncthreads();
-    if (wid == 0) {
-        uint32_t t = lane < P2_THREADS / 32 ? s_warp[lane] : 0;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
-            if (lane >= o) t += y;
-        }
-        if (lane < P2_THREADS / 32) s_warp[lane] = t;
-    }
-    __syncthreads();
-    total = s_warp[P2_THREADS / 32 - 1];
-    const uint32_t r = (wid ? s_warp[wid - 1] : 0) + x - v;
-    __syncthreads();  // s_warp may be reused right after
-    return r;
-}
+// ---------------------------------------------------------------- k_plan
+// One warp per bucket: its groups, from the scanned (bucket, bin) key offsets
+// ko[0 .. nb]. Greedy, in bin order: a group starting at bin s takes the most
+// bins e - s with at most `target` keys (one bin if that bin alone is larger;
+// such a group is listed as heavy). Each step is one upper-bound search over
+// ko, done by the warp as a 32-way search.
+constexpr int PLAN_THREADS = 256;
 
-__device__ __forceinline__ uint32_t bin_of(uint64_t d, uint32_t p1_bits, uint32_t nb) {
-    return (desc_mlo(d) >> p1_bits) & (nb - 1);
-}
-
-// ---------------------------------------------------------------- k_binhist
-// k-mer instances per bin of one slice.
-__global__ void __launch_bounds__(P2_THREADS) k_binhist(KeysParams P) {
-    __shared__ uint32_t h[NBINS];
-    const int tid = threadIdx.x;
-    const Slice sl = P.slices[blockIdx.x];
-    for (uint32_t i = tid; i < P.nb; i += P2_THREADS) h[i] = 0;
-    __syncthreads();
-    const uint64_t* d = P.bdesc + sl.r_lo;
-    const uint32_t n = (uint32_t)(sl.r_hi - sl.r_lo);
-    for (uint32_t i0 = tid; i0 < n; i0 += 4 * P2_THREADS) {
-        uint64_t v[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const uint32_t i = i0 + u * P2_THREADS;
-            v[u] = i < n ? d[i] : 0;
+__global__ void __launch_bounds__(PLAN_THREADS) k_plan(KeysParams P, uint32_t n_buckets) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t b = blockIdx.x * (PLAN_THREADS / 32) + (threadIdx.x >> 5);
+    if (b >= n_buckets) return;  // warp-uniform
+    const uint32_t nb = P.nb;
+    const unsigned long long* ko = P.kofs + (uint64_t)b * nb;
+    const unsigned long long end = ko[nb];
+    const unsigned long long T = P.target;
+    uint32_t s = 0;
+    unsigned long long ks = ko[0];
+    while (ks < end) {
+        // largest e in [s + 1, nb] with ko[e] <= ks + T (e = s + 1 if there is none)
+        const unsigned long long lim = ks + T;
+        uint32_t lo = s + 1, hi = nb;
+        if (ko[lo] <= lim) {
+            while (lo < hi) {  // invariant: ko[lo] <= lim, the answer is in [lo, hi]
+                const uint32_t step = (hi - lo + 31) / 32;
+                const uint32_t e = lo + (uint32_t)lane * step;
+                const unsigned ok = __ballot_sync(0xffffffffu, e <= hi && ko[e] <= lim);  // bit 0 is set
+                const int l = 31 - __clz(ok);
+                const uint32_t nlo = lo + (uint32_t)l * step;
+                hi = l == 31 ? hi : min(nlo + step - 1, hi);
+                lo = nlo;
+            }
         }
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-            if (desc_nk(v[u])) atomicAdd(&h[bin_of(v[u], P.p1_bits, P.nb)], desc_nk(v[u]));
-    }
-    __syncthreads();
-    for (uint32_t i = tid; i < P.nb; i += P2_THREADS) P.shist[(uint64_t)blockIdx.x * P.nb + i] = h[i];
-}
-
-// ---------------------------------------------------------------- k_binscan
-// One CTA per bucket: key offsets (from the bucket's first key) of every
-// (slice, bin), bins in order and slices in order inside a bin; then the
-// bucket's groups: greedy runs of consecutive bins of at most `target` k-mers
-// (a single larger bin is a group of its own, listed as heavy).
-__global__ void __launch_bounds__(P2_THREADS) k_binscan(KeysParams P) {
-    __shared__ uint32_t tot[NBINS];
-    __shared__ uint32_t s_warp[P2_THREADS / 32];
-    const int tid = threadIdx.x;
-    const uint32_t b = blockIdx.x, nb = P.nb;
-    const uint32_t s0 = P.slice_first[b], s1 = P.slice_first[b + 1];
-    uint32_t t = 0;
-    if ((uint32_t)tid < nb)
-        for (uint32_t s = s0; s < s1; ++s) t += P.shist[(uint64_t)s * nb + tid];
-    uint32_t total;
-    const uint32_t ex = block_excl_scan(t, s_warp, total);
-    if ((uint32_t)tid < nb) {
-        uint32_t run = ex;
-        for (uint32_t s = s0; s < s1; ++s) {
-            uint32_t* e = P.shist + (uint64_t)s * nb + tid;
-            const uint32_t v = *e;
-            *e = run;
-            run += v;
-        }
-        tot[tid] = t;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        const unsigned long long kb = P.kbase[b];
-        auto emit = [&](uint32_t lo, uint32_t hi) {
-            const int heavy = hi - lo > P.target ? 1 : 0;
-            const unsigned long long i = atomicAdd(&P.ctr[heavy ? P2C_HEAVY : P2C_NORMAL], 1ull);
-            if (i < P.groups_cap) {
+        const uint32_t e = lo;
+        const unsigned long long ke = ko[e];
+        if (lane == 0) {
+            const int heavy = ke - ks > T ? 1 : 0;
+            const unsigned long long q = atomicAdd(&P.ctr[heavy ? P2C_HEAVY : P2C_NORMAL], 1ull);
+            if (q < P.groups_cap) {
                 Group g;
-                g.lo = kb + lo;
-                g.hi = kb + hi;
+                g.lo = ks;
+                g.hi = ke;
                 g.parts = 1;
                 g.part = 0;
                 g.pad[0] = g.pad[1] = 0;
-                P.groups[heavy][i] = g;
+                P.groups[heavy][q] = g;
             }
-        };
-        uint32_t lo = 0, cur = 0;
-        for (uint32_t i = 0; i < nb; ++i) {
-            const uint32_t ki = tot[i];
-            if (ki == 0) continue;
-            if (cur > 0 && cur + ki > P.target) {
-                emit(lo, lo + cur);
-                lo += cur;
-                cur = 0;
-            }
-            cur += ki;
         }
-        if (cur > 0) emit(lo, lo + cur);
+        s = e;
+        ks = ke;
     }
 }
 
 // ---------------------------------------------------------------- k_keys
-// Every k-mer of a slice: canonical key written at its bin's cursor. A warp
-// takes 32 descriptors at a time; each reserves its k-mers' places with one
-// shared-memory atomic on its bin cursor, then the warp's lanes take the
-// batch's k-mers in order (consecutive lanes, consecutive keys).
+// Every k-mer of a slice of the phase-1 descriptor lists (in stream order, so
+// the packed bases are read front to back): canonical key written at its
+// (bucket, bin) cursor. A warp takes 32 descriptors at a time; each reserves
+// its k-mers' places with one global atomic on its bin cursor, then the
+// warp's lanes take the batch's k-mers in order (consecutive lanes,
+// consecutive keys).
 template <int W>
 __global__ void __launch_bounds__(P2_THREADS) k_keys(KeysParams P) {
     using O = KeyOps<W>;
-    __shared__ uint32_t cur[NBINS];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const Slice sl = P.slices[blockIdx.x];
-    for (uint32_t i = tid; i < P.nb; i += P2_THREADS) cur[i] = P.shist[(uint64_t)blockIdx.x * P.nb + i];
-    __syncthreads();
-    const unsigned long long kb = P.kbase[sl.bucket];
-    const uint64_t* d = P.bdesc + sl.r_lo;
+    const uint64_t* d = P.desc + sl.r_lo;
     const uint32_t n = (uint32_t)(sl.r_hi - sl.r_lo);
     const int k = P.k;
+    uint64_t dnext = (uint32_t)wid * 32 + lane < n ? d[(uint32_t)wid * 32 + lane] : 0;
     for (uint32_t base = (uint32_t)wid * 32; base < n; base += P2_THREADS) {
-        const uint32_t i = base + lane;
-        const uint64_t dv = i < n ? d[i] : 0;
+        const uint64_t dv = dnext;  // this batch; the next one is loaded while it is processed
+        {
+            const uint32_t i = base + P2_THREADS + lane;
+            dnext = i < n ? d[i] : 0;
+        }
         const uint32_t nk = desc_nk(dv);  // 0 past the slice; at least 1 otherwise
-        uint32_t koff = 0;
-        if (nk) koff = atomicAdd(&cur[bin_of(dv, P.p1_bits, P.nb)], nk);
+        unsigned long long koff = 0;
+        if (nk) koff = atomicAdd(&P.kofs[bin_index(desc_mlo(dv), P.p1_bits)], (unsigned long long)nk);
         uint32_t incl = nk;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -301,7 +242,7 @@ __global__ void __launch_bounds__(P2_THREADS) k_keys(KeysParams P) {
         // k-mer t of the batch belongs to lane o: stream position srcb_o + t,
         // key index dstb_o + t
         const uint64_t srcb = desc_start(dv) - excl;
-        const uint64_t dstb = kb + koff - excl;
+        const uint64_t dstb = koff - excl;
         for (uint32_t t0 = 0; t0 < total; t0 += 32 * KEYS_UNROLL) {
             typename O::Key kv[KEYS_UNROLL];
             uint64_t dst[KEYS_UNROLL];
@@ -706,41 +647,32 @@ struct Carve {
     }
 };
 
+constexpr uint32_t NBIN_ALL = 1u << MLO_BITS;  // (bucket, bin) pairs
+
 struct P2Plan {
-    uint64_t n_slices = 0, groups_cap = 0, retry_cap = 0, n_keys = 0, n_keys_alloc = 0;
-    uint32_t nb = 0;
+    uint64_t n_slices = 0, groups_cap = 0, retry_cap = 0, n_keys_alloc = 0, nsum = 0;
     std::vector<Slice> slices;
-    std::vector<uint32_t> slice_first;
-    std::vector<unsigned long long> kbase;
 };
 
 P2Plan make_plan(const P2Input& in) {
     P2Plan L;
-    L.nb = std::min<uint32_t>(NBINS, 1u << (20 - in.p1_bits));
-    L.slice_first.resize(in.p1 + 1);
-    L.kbase.resize(in.p1 + 1);
-    uint64_t r = 0, kb = 0;
-    for (uint32_t b = 0; b < in.p1; ++b) {
-        L.slice_first[b] = (uint32_t)L.slices.size();
-        L.kbase[b] = kb;
-        for (uint64_t s = 0; s < in.recs[b]; s += SLICE_DESC) {
+    for (uint32_t c = 0; c < in.n_lists; ++c) {
+        const uint64_t nd = std::min<uint64_t>(in.n_desc[c], in.desc_cap);
+        for (uint64_t s = 0; s < nd; s += SLICE_DESC) {
             Slice sl;
-            sl.r_lo = r + s;
-            sl.r_hi = r + std::min<uint64_t>(in.recs[b], s + SLICE_DESC);
-            sl.bucket = b;
-            sl.pad = 0;
+            sl.r_lo = (uint64_t)c * in.desc_cap + s;
+            sl.r_hi = (uint64_t)c * in.desc_cap + std::min<uint64_t>(nd, s + SLICE_DESC);
             L.slices.push_back(sl);
         }
-        r += in.recs[b];
-        kb += in.kmers[b];
     }
-    L.slice_first[in.p1] = (uint32_t)L.slices.size();
-    L.kbase[in.p1] = kb;
     L.n_slices = L.slices.size();
-    L.groups_cap = (uint64_t)in.p1 * L.nb;
-    L.retry_cap = std::max<uint64_t>(4096, L.groups_cap);
-    L.n_keys = kb;
-    L.n_keys_alloc = kb + 16 / key_bytes(in.W) + 1;  // a bulk copy may read to the next 16 bytes
+    // a bucket of K keys has fewer than 2 K / target + 1 groups (two neighbouring
+    // groups of k_plan hold more than `target` keys together)
+    const uint64_t target = count_slots(in.W) * 7 / 10;
+    L.groups_cap = 2 * in.n_kmers / target + ((uint64_t)1 << in.p1_bits) + 1;
+    L.retry_cap = std::max<uint64_t>(4096, 2 * L.groups_cap);
+    L.n_keys_alloc = in.n_kmers + 1;
+    L.nsum = (NBIN_ALL + 8191) / 8192 + 2;
     return L;
 }
 
@@ -748,10 +680,9 @@ P2Plan make_plan(const P2Input& in) {
 struct P2Regions {
     unsigned long long* ctr;
     unsigned long long* aux;  // [0..1] retry counters, [2..3] list sizes of a retry pass
+    unsigned long long* kofs;
+    unsigned long long* sums;
     Slice* slices;
-    uint32_t* slice_first;
-    unsigned long long* kbase;
-    uint32_t* shist;
     Group* normal;
     Group* heavy;
     Group* retry[2];
@@ -763,10 +694,9 @@ P2Regions carve(Carve& c, const P2Input& in, const P2Plan& L) {
     P2Regions R;
     R.ctr = c.take<unsigned long long>(P2C_COUNT);
     R.aux = c.take<unsigned long long>(4);
+    R.kofs = c.take<unsigned long long>(NBIN_ALL + 1);
+    R.sums = c.take<unsigned long long>(L.nsum);
     R.slices = c.take<Slice>(L.n_slices + 1);
-    R.slice_first = c.take<uint32_t>(in.p1 + 1);
-    R.kbase = c.take<unsigned long long>(in.p1 + 1);
-    R.shist = c.take<uint32_t>(L.n_slices * L.nb + 1);
     R.normal = c.take<Group>(L.groups_cap);
     R.heavy = c.take<Group>(L.groups_cap);
     R.retry[0] = c.take<Group>(L.retry_cap);
@@ -798,51 +728,44 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
                      int* launches, std::string& err) {
     const P2Plan L = make_plan(in);
     const int W = in.W;
-    for (uint32_t b = 0; b < in.p1; ++b)
-        if (in.kmers[b] >= (1ull << 32)) {
-            err = "a bucket holds 2^32 k-mer instances or more";
-            return TG_ERR_UNSUPPORTED;
-        }
+    const uint32_t nb = NBIN_ALL >> in.p1_bits;
     Carve c{static_cast<uint8_t*>(scratch), 0, scratch_cap, true};
     const P2Regions R = carve(c, in, L);
     if (!c.ok) { err = "phase-2 scratch too small"; return TG_ERR_OOM; }
     const uint32_t slots = count_slots(W);
 
-    P2_CK(cudaMemsetAsync(R.ctr, 0, (P2C_COUNT + 0) * 8, st), "memset");
+    P2_CK(cudaMemsetAsync(R.ctr, 0, P2C_COUNT * 8, st), "memset");
     if (L.n_slices)
         P2_CK(cudaMemcpyAsync(R.slices, L.slices.data(), L.n_slices * sizeof(Slice), cudaMemcpyHostToDevice, st),
               "h2d");
-    P2_CK(cudaMemcpyAsync(R.slice_first, L.slice_first.data(), (in.p1 + 1) * 4, cudaMemcpyHostToDevice, st), "h2d");
-    P2_CK(cudaMemcpyAsync(R.kbase, L.kbase.data(), (in.p1 + 1) * 8, cudaMemcpyHostToDevice, st), "h2d");
-    // the bytes a bulk copy may read past the last key
-    P2_CK(cudaMemsetAsync(R.keys + L.n_keys * key_bytes(W), 0, (L.n_keys_alloc - L.n_keys) * key_bytes(W), st),
-          "memset");
+    // (bucket, bin) k-mer counts -> first key of each bin
+    P2_CK(launch_scan(in.binhist, NBIN_ALL, R.kofs, R.sums, R.kofs + NBIN_ALL, st, launches), "scan");
 
     KeysParams K{};
     K.packed = in.packed;
-    K.bdesc = in.bdesc;
+    K.desc = in.desc;
     K.slices = R.slices;
-    K.slice_first = R.slice_first;
-    K.kbase = R.kbase;
-    K.shist = R.shist;
+    K.kofs = R.kofs;
     K.p1_bits = in.p1_bits;
-    K.nb = L.nb;
-    K.target = slots * 7 / 10;
+    K.nb = nb;
+    K.target = slots * 7 / 10;  // as in make_plan
     K.k = in.k;
     K.keys = R.keys;
     K.groups[0] = R.normal;
     K.groups[1] = R.heavy;
     K.groups_cap = L.groups_cap;
     K.ctr = R.ctr;
+    {
+        const uint32_t p1 = 1u << in.p1_bits, warps = PLAN_THREADS / 32;
+        k_plan<<<(p1 + warps - 1) / warps, PLAN_THREADS, 0, st>>>(K, p1);  // before k_keys moves the cursors
+    }
+    P2_CK(cudaGetLastError(), "k_plan");
+    ++*launches;
     if (L.n_slices) {
-        k_binhist<<<(unsigned)L.n_slices, P2_THREADS, 0, st>>>(K);
-        P2_CK(cudaGetLastError(), "k_binhist");
-        k_binscan<<<in.p1, P2_THREADS, 0, st>>>(K);
-        P2_CK(cudaGetLastError(), "k_binscan");
         if (W == 1) k_keys<1><<<(unsigned)L.n_slices, P2_THREADS, 0, st>>>(K);
         else k_keys<2><<<(unsigned)L.n_slices, P2_THREADS, 0, st>>>(K);
         P2_CK(cudaGetLastError(), "k_keys");
-        *launches += 3;
+        ++*launches;
     }
     if (ev_keys) P2_CK(cudaEventRecord(ev_keys, st), "event");
 
