@@ -618,47 +618,68 @@ k_cut_seq(CutParams P, const HashTables* __restrict__ gT) {
         for (uint32_t i = tid; i < L.nvb; i += NT) s_vb[i] = P.valid[(A0 >> 5) + i];
         __syncthreads();
 
-        // ---- pass 1: walk positions [ps, ps + SEG) (m-mers from ps - 1 on)
+        // ---- pass 1: walk positions [ps, ps + SEG) (m-mers from ps - 1 on).
+        // Positions inside the walk are relative to pb = ps - 1 (32-bit). The
+        // segments start 64 bases apart, so every thread crosses a packed word
+        // (16 bases) or validity word (32) at the same step: the bases come
+        // from register copies of the words, shifted once per step.
         const int64_t ps = t0 + (int64_t)tid * SEG;
-        const uint32_t ra = (uint32_t)((uint64_t)(ps - 1 + TG_PAD) - A0);  // staged index of m-mer ps - 1
+        const int64_t pb = ps - 1;  // m-mer 0; k-mer kp = i - w starts at pb + kp
+        const uint32_t ra = (uint32_t)((uint64_t)(pb + TG_PAD) - A0);  // staged index of base pb
         uint64_t f, r;
         nt_init(T, s_pk, ra, m, f, r);
-        int64_t inv_last;  // last invalid base among those entered so far
+        int il;  // last invalid base entered so far, relative to pb (-1: none)
         {
-            const uint64_t inval = ~valid64(s_vb, ra) & kmask;  // bases ps - 1 .. ps - 2 + k
-            inv_last = inval ? ps - 1 + (63 - __clzll((long long)inval)) : ps - 2;
+            const uint64_t inval = ~valid64(s_vb, ra) & kmask;  // bases pb .. pb + k - 1
+            il = inval ? 63 - __clzll((long long)inval) : -1;
         }
-        uint64_t pmin = ~0ull, mprev = 0;
-        bool vprev = false;
-        int64_t first_ev = -1, last_ev = -1, last_cs = -1;
-        bool last_is_cs = false, open = false;
-        int64_t rs = 0;
+        auto rel = [&](int64_t x) {  // x - pb clamped to [-1, 2^31 - 1]: comparisons with kp keep
+            const int64_t d = x - pb;
+            return (int)(d < -1 ? -1 : (d > 0x7FFFFFFF ? 0x7FFFFFFF : d));
+        };
+        const int ownlo = rel(cstart), ownhi = rel(cend);
+        uint32_t oi = ra, ii = ra + (uint32_t)m;  // bases leaving / entering at the next step
+        uint32_t ow = s_pk[oi >> 4] << (2 * (oi & 15));
+        uint32_t iw = s_pk[ii >> 4] << (2 * (ii & 15));
+        uint32_t vw = s_vb[ii >> 5] >> (ii & 31);
+        uint64_t h = f ^ r, pmin = h, mprev = 0;
+        vH[tid] = h;  // m-mer 0 opens block 0 (w >= 1: no k-mer ends here)
+        bool vprev = false, last_is_cs = false, open = false;
+        int first_ev = -1, last_ev = -1, last_cs = -1, rs = 0;
         uint32_t rm = 0, last_cs_m = 0;
-        int o = 0;  // offset of the m-mer in its block
-        for (int i = 0; i <= SEG + w; ++i) {
-            const uint32_t rin = ra + (uint32_t)(i + m - 1);  // base entering the m-mer (and the k-mer)
-            if (i > 0) nt_roll(T, base_at(s_pk, ra + (uint32_t)i - 1), base_at(s_pk, rin), f, r);
-            const uint64_t h = f ^ r;
+        int o = 1;  // offset of the m-mer in its block
+        for (int i = 1; i <= SEG + w; ++i) {
+            const uint32_t bo = ow >> 30, bi = iw >> 30, vb = vw & 1u;  // vb: base pb + i + m - 1
+            ow <<= 2;
+            iw <<= 2;
+            vw >>= 1;
+            ++oi;
+            ++ii;
+            if ((oi & 15) == 0) ow = s_pk[oi >> 4];
+            if ((ii & 15) == 0) iw = s_pk[ii >> 4];
+            if ((ii & 31) == 0) vw = s_vb[ii >> 5];
+            nt_roll(T, bo, bi, f, r);
+            h = f ^ r;
             vH[o * NT + tid] = h;
             pmin = min(pmin, h);
             if (i >= w) {
-                const int64_t p = ps - 1 + (i - w);  // k-mer whose window ends at this m-mer
+                const int kp = i - w;  // the k-mer whose window ends at this m-mer
                 const uint64_t M = o == B - 1 ? pmin : min(vS[(o + 1) * NT + tid], pmin);
-                if (i > w && !valid_base(s_vb, rin)) inv_last = p + k - 1;
-                const bool v = inv_last < p;
+                if (i > w && !vb) il = kp + k - 1;  // its last base is pb + i + m - 1
+                const bool v = il < kp;
                 if (i > w) {
                     const bool first = v && !vprev;
                     const bool cs = v && (first || M != mprev);
                     const bool cut = cs || (!v && vprev);  // a new chain, or the end of a run
-                    if (first && p >= cstart && p < cend) ++loc_runs;
-                    const bool close = cut && open && owned(rs);
-                    emit_warp(close, rs, (uint32_t)(p - rs), rm);
+                    if (first && kp >= ownlo && kp < ownhi) ++loc_runs;
+                    const bool close = cut && open && rs >= ownlo && rs < ownhi;
+                    emit_warp(close, pb + rs, (uint32_t)(kp - rs), rm);
                     if (cut) {
-                        if (first_ev < 0) first_ev = p;
-                        last_ev = p;
+                        if (first_ev < 0) first_ev = kp;
+                        last_ev = kp;
                         last_is_cs = cs;
                         open = cs;
-                        if (cs) { rs = p; rm = (uint32_t)(M & 0xFFFFFu); last_cs = p; last_cs_m = rm; }
+                        if (cs) { rs = kp; rm = (uint32_t)(M & 0xFFFFFu); last_cs = kp; last_cs_m = rm; }
                     }
                 }
                 mprev = M;
@@ -678,8 +699,9 @@ k_cut_seq(CutParams P, const HashTables* __restrict__ gT) {
             }
         }
         // ---- chain in force at the segment start: the last cut of a lower thread
-        s_cs[tid] = last_is_cs ? last_cs : -1;
+        s_cs[tid] = last_is_cs ? pb + last_cs : -1;
         s_cm[tid] = last_cs_m;
+        const int64_t first_abs = first_ev >= 0 ? pb + first_ev : -1;
         int last_t;
         const int prev = seq_excl_max<NT>(last_ev >= 0 ? tid : -1, s_w, last_t);
         int64_t cs_in = s_carry_cs;
@@ -691,17 +713,17 @@ k_cut_seq(CutParams P, const HashTables* __restrict__ gT) {
             const int64_t d = ps - cs_in;
             const int64_t rem = d % Lr;
             const int64_t cand = ps + (rem ? Lr - rem : 0);
-            if (cand < ps + SEG && (first_ev < 0 || cand < first_ev)) fc = cand;
+            if (cand < ps + SEG && (first_abs < 0 || cand < first_abs)) fc = cand;
         }
         // a forced-split record closed by the segment's first cut
-        emit_warp(fc >= 0 && first_ev >= 0 && owned(cs_in), fc, (uint32_t)(first_ev - fc), m_in);
+        emit_warp(fc >= 0 && first_abs >= 0 && owned(cs_in), fc, (uint32_t)(first_abs - fc), m_in);
         // the record open at the segment's end, if it starts in the segment
         bool oo = false, oown = false;
         int64_t os = 0;
         uint32_t om = 0;
-        if (open) { oo = true; os = rs; om = rm; oown = owned(rs); }
-        else if (fc >= 0 && first_ev < 0) { oo = true; os = fc; om = m_in; oown = owned(cs_in); }
-        const int64_t fe = fc >= 0 ? fc : first_ev;
+        if (open) { oo = true; os = pb + rs; om = rm; oown = owned(os); }
+        else if (fc >= 0 && first_abs < 0) { oo = true; os = fc; om = m_in; oown = owned(cs_in); }
+        const int64_t fe = fc >= 0 ? fc : first_abs;
         s_fe[tid] = fe;
         int first_t;
         const int nxt = seq_excl_min_rev<NT>(fe >= 0 ? tid : NT, s_w, first_t);

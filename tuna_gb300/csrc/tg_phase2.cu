@@ -32,6 +32,8 @@
 namespace tg {
 
 constexpr int P2_THREADS = 1024;         // threads of the phase-2 CTAs
+constexpr int COUNT_THREADS = 1024;      // threads of a k_count CTA
+constexpr int COUNT_PER_SM = 1;          // one CTA per SM: the largest table, the largest groups
 constexpr uint32_t NBINS = 1024;         // minimizer-bit bins per bucket (at most)
 constexpr uint32_t PROBE_LIMIT = 128;    // linear-probe steps before a group is split
 constexpr uint32_t MAX_PARTS = 64;       // key-hash parts of one range before the global table
@@ -364,9 +366,9 @@ struct CountSmem {
     }
 };
 
-// Persistent: one CTA per SM takes groups in order (list 1, then list 0) from a
+// Persistent: COUNT_PER_SM CTAs per SM take groups in order (list 1, then list 0) from a
 // global counter. A group's keys are one contiguous range; they are inserted
-// in rounds of RK keys, thread t taking keys t, t + P2_THREADS, ... of a round,
+// in rounds of RK keys, thread t taking keys t, t + COUNT_THREADS, ... of a round,
 // and each thread's keys of the next round (or of the next group's first round)
 // are loaded into registers while it inserts the current ones, so there is no
 // barrier inside a group. After a group every thread scans its slots of the
@@ -375,11 +377,11 @@ struct CountSmem {
 // comes back as its two key-hash halves. Group entries are fetched two groups
 // ahead (cp.async) into a ring of three.
 template <int W>
-__global__ void __launch_bounds__(P2_THREADS, 1) k_count(CountParams P) {
+__global__ void __launch_bounds__(COUNT_THREADS, COUNT_PER_SM) k_count(CountParams P) {
     using O = KeyOps<W>;
     using Key = typename O::Key;
     constexpr int U = W == 1 ? 4 : 2;                 // keys per thread per round
-    constexpr uint32_t RK = U * P2_THREADS;           // keys per round
+    constexpr uint32_t RK = U * COUNT_THREADS;           // keys per round
     constexpr uint32_t SPT = W == 1 ? 16 : 8;         // table slots per thread
     extern __shared__ __align__(128) uint8_t smem[];
     CountSmem<W> L;
@@ -388,12 +390,12 @@ __global__ void __launch_bounds__(P2_THREADS, 1) k_count(CountParams P) {
     uint32_t* cnt = reinterpret_cast<uint32_t*>(smem + L.cnt);
     __shared__ __align__(16) Group s_grp[3];          // groups g, g + 1, g + 2
     __shared__ uint32_t s_fail;
-    __shared__ uint32_t s_wnew[P2_THREADS / 32];      // new keys of the group, per warp
-    __shared__ uint32_t s_wout[P2_THREADS / 32];      // output keys per warp, then their offsets
+    __shared__ uint32_t s_wnew[COUNT_THREADS / 32];      // new keys of the group, per warp
+    __shared__ uint32_t s_wout[COUNT_THREADS / 32];      // output keys per warp, then their offsets
     __shared__ unsigned long long s_obase;
 
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const uint32_t S = P.smem_slots, mask = S - 1;    // S == SPT * P2_THREADS
+    const uint32_t S = P.smem_slots, mask = S - 1;    // S == SPT * COUNT_THREADS
     const uint32_t fill_cap = S - S / 8;
     // counts are at least 1 and fit in 32 bits: without ci/cx limits every key is kept
     const bool filtered = P.ci > 1 || P.cx < 0xFFFFFFFFull;
@@ -401,8 +403,8 @@ __global__ void __launch_bounds__(P2_THREADS, 1) k_count(CountParams P) {
     const Key* src = static_cast<const Key*>(P.keys);
     unsigned long long distinct = 0;                  // per warp, in lane 0
 
-    for (uint32_t i = tid; i < S; i += P2_THREADS) { keys[i] = O::empty(); cnt[i] = 0; }
-    if (tid < P2_THREADS / 32) s_wnew[tid] = 0;
+    for (uint32_t i = tid; i < S; i += COUNT_THREADS) { keys[i] = O::empty(); cnt[i] = 0; }
+    if (tid < COUNT_THREADS / 32) s_wnew[tid] = 0;
     unsigned long long gi_pend = ~0ull;               // thread 0: index of group g + 3
     if (tid == 0) {
         s_fail = 0;
@@ -416,7 +418,7 @@ __global__ void __launch_bounds__(P2_THREADS, 1) k_count(CountParams P) {
     auto load_round = [&](const Group& g, uint32_t r, Key (&K)[U]) {
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-            const unsigned long long i = g.lo + (unsigned long long)r * RK + (uint32_t)u * P2_THREADS + tid;
+            const unsigned long long i = g.lo + (unsigned long long)r * RK + (uint32_t)u * COUNT_THREADS + tid;
             K[u] = i < g.hi ? src[i] : O::empty();
         }
     };
@@ -466,14 +468,14 @@ __global__ void __launch_bounds__(P2_THREADS, 1) k_count(CountParams P) {
             gi_pend = atomicAdd(&P.ctr[P2C_WORK], 1ull);
         }
         if (wid == 0) {
-            const uint32_t t = __reduce_add_sync(0xffffffffu, s_wnew[lane]);
+            const uint32_t t = __reduce_add_sync(0xffffffffu, lane < COUNT_THREADS / 32 ? s_wnew[lane] : 0u);
             if (lane == 0 && t > fill_cap) s_fail = 1;  // more than 7/8 full: split the group
         }
         __syncthreads();
         if (s_fail) {
             // clear the table; the group comes back as two halves
 #pragma unroll
-            for (uint32_t j = 0; j < SPT; ++j) { keys[tid + j * P2_THREADS] = O::empty(); cnt[tid + j * P2_THREADS] = 0; }
+            for (uint32_t j = 0; j < SPT; ++j) { keys[tid + j * COUNT_THREADS] = O::empty(); cnt[tid + j * COUNT_THREADS] = 0; }
             if (tid == 0) {
                 Group f = g;
                 if (g.parts < MAX_PARTS) {
@@ -491,13 +493,13 @@ __global__ void __launch_bounds__(P2_THREADS, 1) k_count(CountParams P) {
                 }
             }
         } else {
-            // ---- output: thread t owns slots t + j * P2_THREADS (a warp's accesses
+            // ---- output: thread t owns slots t + j * COUNT_THREADS (a warp's accesses
             // are consecutive); per warp and round j one ballot places the kept
             // keys contiguously
             uint32_t keepm = 0, nocc = 0;
 #pragma unroll
             for (uint32_t j = 0; j < SPT; ++j) {
-                const uint32_t sl = tid + j * P2_THREADS;
+                const uint32_t sl = tid + j * COUNT_THREADS;
                 const bool occ = !O::is_empty(keys[sl]);
                 nocc += occ ? 1u : 0u;
                 bool keep = occ;
@@ -514,21 +516,21 @@ __global__ void __launch_bounds__(P2_THREADS, 1) k_count(CountParams P) {
             if (lane == 0) { s_wout[wid] = wtot; distinct += nocc; }
             __syncthreads();
             if (wid == 0) {
-                const uint32_t v = s_wout[lane];
+                const uint32_t v = lane < COUNT_THREADS / 32 ? s_wout[lane] : 0u;
                 uint32_t x = v;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
                     const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
                     if (lane >= o) x += y;
                 }
-                s_wout[lane] = x - v;
+                if (lane < COUNT_THREADS / 32) s_wout[lane] = x - v;
                 if (lane == 31) s_obase = x ? atomicAdd(&P.ctr[P2C_OUT], (unsigned long long)x) : 0;
             }
             __syncthreads();
             unsigned long long o = s_obase + s_wout[wid];
 #pragma unroll
             for (uint32_t j = 0; j < SPT; ++j) {
-                const uint32_t sl = tid + j * P2_THREADS;
+                const uint32_t sl = tid + j * COUNT_THREADS;
                 const bool keep = (keepm >> j) & 1u;
                 const unsigned bal = __ballot_sync(0xffffffffu, keep);
                 if (keep) {
@@ -796,8 +798,8 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
         Q.n_retry = R.aux + (pass & 1);
         P2_CK(cudaMemsetAsync(Q.n_retry, 0, 8, st), "memset");
         P2_CK(cudaMemsetAsync(R.ctr + P2C_WORK, 0, 8, st), "memset");
-        if (W == 1) k_count<1><<<in.n_sm, P2_THREADS, sm, st>>>(Q);
-        else k_count<2><<<in.n_sm, P2_THREADS, sm, st>>>(Q);
+        if (W == 1) k_count<1><<<in.n_sm * COUNT_PER_SM, COUNT_THREADS, sm, st>>>(Q);
+        else k_count<2><<<in.n_sm * COUNT_PER_SM, COUNT_THREADS, sm, st>>>(Q);
         P2_CK(cudaGetLastError(), "k_count");
         ++*launches;
         unsigned long long nret = 0;
