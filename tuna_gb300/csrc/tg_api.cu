@@ -103,6 +103,10 @@ struct tg_ctx {
     DevBuf seq, packed, valid, desc, xdesc, hist, scratch, okeys, ocnt,
         misc, fbtab, tables;
     cudaEvent_t ev[12] = {};
+    // results copied to the host while counting runs (tg_count_seq)
+    cudaStream_t st_copy = nullptr;
+    unsigned long long* wave_out = nullptr;  // pinned host, 16 entries
+    cudaEvent_t wave_ev[16] = {};
     tg_job* active = nullptr;
     int prepared_m = -1;
 
@@ -142,6 +146,8 @@ struct tg_job {
     // results
     uint64_t n_out = 0;
     tg_stats st{};
+    // optional: output ranges handed out as phase 2 finishes them
+    const P2Overlap* overlap = nullptr;
     const uint8_t* seq_ptr() const { return ext ? ext : ctx->seq.as<uint8_t>(); }
 };
 
@@ -179,6 +185,9 @@ tg_status tg_ctx_create(const tg_ctx_opts* opts, tg_ctx** out) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, o.device);
     ctx->smem_optin = (size_t)optin;
     for (int i = 0; i < 12 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->ev[i]);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->st_copy, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaHostAlloc(&ctx->wave_out, 16 * sizeof(unsigned long long), cudaHostAllocDefault);
+    for (int i = 0; i < 16 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&ctx->wave_ev[i], cudaEventDisableTiming);
     if (e != cudaSuccess) {
         delete ctx;
         return TG_ERR_CUDA;
@@ -198,6 +207,13 @@ tg_status tg_ctx_destroy(tg_ctx* ctx) {
         if (b->p) cudaFree(b->p);
     for (auto& e : ctx->ev)
         if (e) cudaEventDestroy(e);
+    for (auto& e : ctx->wave_ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->st_copy) {
+        cudaStreamSynchronize(ctx->st_copy);
+        cudaStreamDestroy(ctx->st_copy);
+    }
+    if (ctx->wave_out) cudaFreeHost(ctx->wave_out);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
     return TG_OK;
@@ -446,7 +462,7 @@ tg_status tg_job_run(tg_job* j) {
         return ctx->ensure(ctx->fbtab, bytes) == cudaSuccess ? ctx->fbtab.p : nullptr;
     };
     const tg_status ps = phase2_run(in, ctx->scratch.p, p2_bytes, out, fallback_table, ctx->st, ctx->ev[7],
-                                    &launches, msg);
+                                    &launches, msg, j->overlap ? *j->overlap : P2Overlap());
     if (ps != TG_OK) return ctx->fail(ps, msg);
     CK(cudaEventRecord(ctx->ev[8], ctx->st), "event");
     CK(cudaEventSynchronize(ctx->ev[8]), "sync");
@@ -625,11 +641,36 @@ tg_status tg_count_seq(tg_ctx* ctx, const tg_job_opts* opts, const uint8_t* seq,
     tg_status s = tg_job_begin(ctx, opts, &j);
     if (s != TG_OK) return s;
     s = tg_job_feed_seq(j, seq, len);
+    // the counting pass runs in waves; each wave's pairs go to the caller's
+    // buffers on the copy stream while the next waves count
+    P2Overlap ov;
+    ov.waves = 8;
+    ov.wave_out = ctx->wave_out;
+    ov.wave_ev = ctx->wave_ev;
+    double d2h_issue_ms = 0;
+    const int W = j->W;
+    ov.on_range = [&](uint64_t lo, uint64_t hi) -> tg_status {
+        const uint64_t h = std::min<uint64_t>(hi, cap);
+        if (h <= lo) return TG_OK;
+        const double t0 = now_ms();
+        if (keys)
+            CK(cudaMemcpyAsync(keys + lo * W, ctx->okeys.as<uint8_t>() + lo * key_bytes(W), (h - lo) * key_bytes(W),
+                               cudaMemcpyDeviceToHost, ctx->st_copy), "d2h keys");
+        if (counts)
+            CK(cudaMemcpyAsync(counts + lo, ctx->ocnt.as<uint32_t>() + lo, (h - lo) * 4, cudaMemcpyDeviceToHost,
+                               ctx->st_copy), "d2h counts");
+        d2h_issue_ms += now_ms() - t0;
+        return TG_OK;
+    };
+    j->overlap = &ov;
     if (s == TG_OK) s = tg_job_run(j);
+    const double t_wait = now_ms();
+    const cudaError_t ce = cudaStreamSynchronize(ctx->st_copy);
+    j->st.d2h_ms += d2h_issue_ms + (now_ms() - t_wait);
+    if (s == TG_OK && ce != cudaSuccess) s = ctx->cuda_fail(ce, "d2h");
     if (s == TG_OK) {
         *n_out = j->n_out;
         if (j->n_out > cap) s = ctx->fail(TG_ERR_ARG, "result buffer too small");
-        else s = tg_job_result_copy(j, keys, counts, 0, j->n_out);
     }
     if (stats) *stats = j->st;
     tg_job_end(j);

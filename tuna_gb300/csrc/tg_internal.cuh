@@ -101,7 +101,6 @@ struct Group {
 enum P2Counter : int {
     P2C_NORMAL = 0,   // groups of at most `target` k-mers
     P2C_HEAVY,        // groups larger than `target`
-    P2C_WORK,         // next group of the current k_count launch
     P2C_RETRY,        // groups pushed back for another pass with more parts
     P2C_FALLBACK,     // key ranges left to the global-memory table
     P2C_OUT,          // output cursor
@@ -138,6 +137,8 @@ struct CountParams {
     uint64_t out_cap;
     unsigned long long* ctr;           // P2Counter
     uint32_t smem_slots;               // table capacity in shared memory
+    unsigned long long g_begin, g_end; // this launch counts groups [g_begin, g_end) of the sequence
+    unsigned long long* work;          // this launch's group counter (starts at 0)
 };
 
 // A key range that did not fit in shared memory, counted in a global table.

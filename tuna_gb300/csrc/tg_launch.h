@@ -43,6 +43,17 @@ struct P2Output {
     uint64_t cap;
     uint64_t n_out, distinct, groups, heavy_groups, fallback_groups;
 };
+// Results handed out while phase 2 still runs: the first counting pass runs in
+// `waves` launches, and after each one on_range(lo, hi) is called (on the host,
+// in order) with the output range [lo, hi) that is now final in P2Output;
+// the last call comes after the retry passes. wave_out: pinned host memory of
+// `waves` u64; wave_ev: `waves` events. Empty on_range: one launch, no calls.
+struct P2Overlap {
+    uint32_t waves = 1;
+    unsigned long long* wave_out = nullptr;
+    cudaEvent_t* wave_ev = nullptr;
+    std::function<tg_status(uint64_t lo, uint64_t hi)> on_range;
+};
 // Device scratch one run needs (key array included).
 size_t phase2_scratch_bytes(const P2Input& in);
 // Runs phase 2 on `st` and waits for it. fallback_table(bytes) returns device
@@ -50,7 +61,7 @@ size_t phase2_scratch_bytes(const P2Input& in);
 // keys are written.
 tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Output& out,
                      const std::function<void*(size_t)>& fallback_table, cudaStream_t st, cudaEvent_t ev_keys,
-                     int* launches, std::string& err);
+                     int* launches, std::string& err, const P2Overlap& ov = P2Overlap());
 
 // ntHash roll / init tables for minimizer length m (host side).
 HashTables make_hash_tables(int m);

@@ -399,7 +399,9 @@ __global__ void __launch_bounds__(COUNT_THREADS, COUNT_PER_SM) k_count(CountPara
     const uint32_t fill_cap = S - S / 8;
     // counts are at least 1 and fit in 32 bits: without ci/cx limits every key is kept
     const bool filtered = P.ci > 1 || P.cx < 0xFFFFFFFFull;
-    const unsigned long long n1 = P.n_list[1], ntot = P.n_list[0] + n1;
+    const unsigned long long n1 = P.n_list[1];
+    const unsigned long long ntot = min(P.n_list[0] + n1, P.g_end);
+    const unsigned long long g0 = P.g_begin;
     const Key* src = static_cast<const Key*>(P.keys);
     unsigned long long distinct = 0;                  // per warp, in lane 0
 
@@ -408,8 +410,8 @@ __global__ void __launch_bounds__(COUNT_THREADS, COUNT_PER_SM) k_count(CountPara
     unsigned long long gi_pend = ~0ull;               // thread 0: index of group g + 3
     if (tid == 0) {
         s_fail = 0;
-        for (int q = 0; q < 3; ++q) copy_group(&s_grp[q], P, atomicAdd(&P.ctr[P2C_WORK], 1ull), n1, ntot);
-        gi_pend = atomicAdd(&P.ctr[P2C_WORK], 1ull);
+        for (int q = 0; q < 3; ++q) copy_group(&s_grp[q], P, g0 + atomicAdd(P.work, 1ull), n1, ntot);
+        gi_pend = g0 + atomicAdd(P.work, 1ull);
         asm volatile("cp.async.wait_all;" ::: "memory");
     }
     __syncthreads();
@@ -465,7 +467,7 @@ __global__ void __launch_bounds__(COUNT_THREADS, COUNT_PER_SM) k_count(CountPara
             // group g + 3's entry into slot q (landed before the group's last
             // barrier), the index after it claimed
             copy_group(&s_grp[q], P, gi_pend, n1, ntot);
-            gi_pend = atomicAdd(&P.ctr[P2C_WORK], 1ull);
+            gi_pend = g0 + atomicAdd(P.work, 1ull);
         }
         if (wid == 0) {
             const uint32_t t = __reduce_add_sync(0xffffffffu, lane < COUNT_THREADS / 32 ? s_wnew[lane] : 0u);
@@ -682,6 +684,7 @@ P2Plan make_plan(const P2Input& in) {
 struct P2Regions {
     unsigned long long* ctr;
     unsigned long long* aux;  // [0..1] retry counters, [2..3] list sizes of a retry pass
+    unsigned long long* work; // [0..15] group counters of the first pass's launches, [16] of a retry pass
     unsigned long long* kofs;
     unsigned long long* sums;
     Slice* slices;
@@ -696,6 +699,7 @@ P2Regions carve(Carve& c, const P2Input& in, const P2Plan& L) {
     P2Regions R;
     R.ctr = c.take<unsigned long long>(P2C_COUNT);
     R.aux = c.take<unsigned long long>(4);
+    R.work = c.take<unsigned long long>(17);
     R.kofs = c.take<unsigned long long>(NBIN_ALL + 1);
     R.sums = c.take<unsigned long long>(L.nsum);
     R.slices = c.take<Slice>(L.n_slices + 1);
@@ -727,7 +731,7 @@ size_t phase2_scratch_bytes(const P2Input& in) {
 
 tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Output& out,
                      const std::function<void*(size_t)>& fallback_table, cudaStream_t st, cudaEvent_t ev_keys,
-                     int* launches, std::string& err) {
+                     int* launches, std::string& err, const P2Overlap& ov) {
     const P2Plan L = make_plan(in);
     const int W = in.W;
     const uint32_t nb = NBIN_ALL >> in.p1_bits;
@@ -792,24 +796,54 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
     else
         P2_CK(cudaFuncSetAttribute(k_count<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm), "smem");
     unsigned long long h[P2C_COUNT];
+    // the groups of the first pass: their number is known once k_plan has run
+    P2_CK(cudaMemcpyAsync(h, R.ctr, sizeof h, cudaMemcpyDeviceToHost, st), "d2h");
+    P2_CK(cudaStreamSynchronize(st), "phase 2");
+    if (h[P2C_NORMAL] > L.groups_cap || h[P2C_HEAVY] > L.groups_cap) {
+        err = "group list overflow";
+        return TG_ERR_TABLE;
+    }
+    const unsigned long long ngroups = h[P2C_NORMAL] + h[P2C_HEAVY];
+    const uint32_t waves = ov.on_range && ov.wave_out && ov.wave_ev ? std::max<uint32_t>(1, std::min(ov.waves, 16u)) : 1;
+    P2_CK(cudaMemsetAsync(R.work, 0, 8 * 17, st), "memset");
+    uint64_t done = 0;  // output keys already handed to on_range
     for (int pass = 0;; ++pass) {
         // pass p writes its split groups to retry[p & 1]; pass p + 1 counts them
         Q.retry = R.retry[pass & 1];
         Q.n_retry = R.aux + (pass & 1);
         P2_CK(cudaMemsetAsync(Q.n_retry, 0, 8, st), "memset");
-        P2_CK(cudaMemsetAsync(R.ctr + P2C_WORK, 0, 8, st), "memset");
-        if (W == 1) k_count<1><<<in.n_sm * COUNT_PER_SM, COUNT_THREADS, sm, st>>>(Q);
-        else k_count<2><<<in.n_sm * COUNT_PER_SM, COUNT_THREADS, sm, st>>>(Q);
-        P2_CK(cudaGetLastError(), "k_count");
-        ++*launches;
+        // the first pass in `waves` launches over slices of the group sequence;
+        // each slice's output range goes to on_range as soon as it is final
+        const uint32_t nw = pass == 0 ? waves : 1;
+        for (uint32_t wv = 0; wv < nw; ++wv) {
+            Q.g_begin = pass == 0 ? ngroups * wv / nw : 0;
+            Q.g_end = pass == 0 ? ngroups * (wv + 1) / nw : ~0ull;
+            Q.work = R.work + (pass == 0 ? wv : 16);
+            if (pass > 0) P2_CK(cudaMemsetAsync(Q.work, 0, 8, st), "memset");
+            if (W == 1) k_count<1><<<in.n_sm * COUNT_PER_SM, COUNT_THREADS, sm, st>>>(Q);
+            else k_count<2><<<in.n_sm * COUNT_PER_SM, COUNT_THREADS, sm, st>>>(Q);
+            P2_CK(cudaGetLastError(), "k_count");
+            ++*launches;
+            if (nw > 1) {
+                P2_CK(cudaMemcpyAsync(ov.wave_out + wv, R.ctr + P2C_OUT, 8, cudaMemcpyDeviceToHost, st), "d2h");
+                P2_CK(cudaEventRecord(ov.wave_ev[wv], st), "event");
+            }
+        }
+        if (nw > 1) {
+            for (uint32_t wv = 0; wv < nw; ++wv) {
+                P2_CK(cudaEventSynchronize(ov.wave_ev[wv]), "wave");
+                const uint64_t hi = std::min<uint64_t>(ov.wave_out[wv], out.cap);
+                if (hi > done) {
+                    const tg_status rs = ov.on_range(done, hi);
+                    if (rs != TG_OK) { err = "result copy failed"; return rs; }
+                    done = hi;
+                }
+            }
+        }
         unsigned long long nret = 0;
         P2_CK(cudaMemcpyAsync(&nret, Q.n_retry, 8, cudaMemcpyDeviceToHost, st), "d2h");
         P2_CK(cudaMemcpyAsync(h, R.ctr, sizeof h, cudaMemcpyDeviceToHost, st), "d2h");
         P2_CK(cudaStreamSynchronize(st), "phase 2");
-        if (pass == 0 && (h[P2C_NORMAL] > L.groups_cap || h[P2C_HEAVY] > L.groups_cap)) {
-            err = "group list overflow";
-            return TG_ERR_TABLE;
-        }
         if (nret > L.retry_cap) { err = "too many groups to split"; return TG_ERR_TABLE; }
         if (nret == 0) break;
         const unsigned long long nl[2] = {0, nret};
@@ -863,6 +897,10 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
         P2_CK(cudaStreamSynchronize(st), "fallback");
     }
     out.n_out = h[P2C_OUT];
+    if (ov.on_range && std::min<uint64_t>(out.n_out, out.cap) > done) {
+        const tg_status rs = ov.on_range(done, std::min<uint64_t>(out.n_out, out.cap));
+        if (rs != TG_OK) { err = "result copy failed"; return rs; }
+    }
     out.distinct = h[P2C_DISTINCT];
     out.groups = h[P2C_NORMAL] + h[P2C_HEAVY];
     out.heavy_groups = h[P2C_HEAVY];
