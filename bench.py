@@ -48,7 +48,8 @@ def parse_args():
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the 3.1 Gbp workload")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-shard-mbp", type=float, default=2.5, help="CPU sample: one shard of this size per core")
+    ap.add_argument("--cpu-shard-mbp", type=float, default=80.0,
+                    help="CPU sample: one shard of this size per core (about 10 s of work on 16 cores)")
     return ap.parse_args()
 
 
@@ -139,14 +140,20 @@ def cpu_sample(scale_shard_mbp: float, threads: int):
     return np.append(s, np.uint8(10)), total
 
 
-def time_cpu(threads: int, shard_mbp: float, steps: int = 1):
+def time_cpu(threads: int, shard_mbp: float, steps: int = 1, warmup: int = 0, sample=None):
+    """Median seconds of `steps` runs of the oracle port over the CPU sample
+    (after `warmup` untimed runs; at least a short warm-up of the library)."""
     from oracle import oracle as O
-    sample, bases = cpu_sample(shard_mbp, threads)
-    O.count_stream_unsorted(sample[: min(sample.size, 2_000_000)], K, M, NPARTS, threads=threads)  # warm
+    if sample is None:
+        sample = cpu_sample(shard_mbp, threads)
+    s, bases = sample
+    O.count_stream_unsorted(s[: min(s.size, 2_000_000)], K, M, NPARTS, threads=threads)  # load, warm
+    for _ in range(warmup):
+        O.count_stream_unsorted(s, K, M, n_parts=NPARTS, threads=threads)
     ts = []
-    for _ in range(steps):
+    for _ in range(max(1, steps)):
         t0 = time.perf_counter()
-        r = O.count_stream_unsorted(sample, K, M, n_parts=NPARTS, threads=threads)
+        r = O.count_stream_unsorted(s, K, M, n_parts=NPARTS, threads=threads)
         ts.append(time.perf_counter() - t0)
     t = statistics.median(ts)
     return {"value": bases / t / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
@@ -160,15 +167,13 @@ def run_reference(args, rank: int):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    base = time_cpu(threads, args.cpu_shard_mbp, steps=1)  # warm-up + one measurement
-    vals = []
-    for _ in range(max(1, args.steps)):
-        vals.append(time_cpu(threads, args.cpu_shard_mbp, steps=1)["value"])
-    v = statistics.median(vals)
+    sample = cpu_sample(args.cpu_shard_mbp, threads)
+    base = time_cpu(threads, args.cpu_shard_mbp, steps=args.steps, warmup=args.warmup, sample=sample)
+    v = base["value"]
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-            "ms_per_step": base["seconds"] * 1e3,
+            "ms_per_step": base["seconds"] * 1e3,  # median over the timed steps
             "config": {"workload": "3.1 Gbp repetitive assembly (24 contigs), k=31 m=23 n=4096",
                        "k": K, "m": M, "n_parts": NPARTS, "sample": base["sample"]},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",

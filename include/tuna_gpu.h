@@ -161,6 +161,19 @@ typedef int (*tg_part_sink_fn)(uint32_t part, const uint8_t* data, size_t len, v
 tg_status tg_job_export_partitions(tg_job* job, tg_part_sink_fn sink, void* user);
 tg_status tg_job_end(tg_job* job);
 
+/* ---- several samples in one job ------------------------------------------
+ * No counterpart in the reference, which counts one input set per run. A job
+ * may hold up to TG_MAX_SAMPLES independent samples: feed the first, call
+ * tg_job_next_sample(), feed the second, and so on. Each sample is counted on
+ * its own (a k-mer present in two samples gives two pairs, each with its own
+ * count), all of them in one pass of the device pipeline; the result of a
+ * sample is the same as when it runs alone. tg_job_result_samples gives the
+ * sample index of each pair. Partition export needs a job of one sample. */
+#define TG_MAX_SAMPLES 65536u
+tg_status tg_job_next_sample(tg_job* job);
+uint32_t tg_job_sample_count(const tg_job* job);
+tg_status tg_job_result_samples(tg_job* job, uint32_t* samples, uint64_t first, uint64_t n);
+
 /* ---- one-call helpers --------------------------------------------------- */
 /* Count a host sequence stream end to end: H2D, both phases, D2H of the
  * filtered pairs into caller buffers of capacity cap (n_out receives the
@@ -168,6 +181,12 @@ tg_status tg_job_end(tg_job* job);
 tg_status tg_count_seq(tg_ctx* ctx, const tg_job_opts* opts, const uint8_t* seq, size_t len,
                        uint64_t* keys, uint32_t* counts, uint64_t cap, uint64_t* n_out,
                        tg_stats* stats);
+/* The same for n_samples host sequence streams counted as separate samples in
+ * one job; samples (cap u32, may be NULL) receives the sample of each pair. */
+tg_status tg_count_batch(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_samples,
+                         const uint8_t* const* seqs, const size_t* lens, uint64_t* keys,
+                         uint32_t* counts, uint32_t* samples, uint64_t cap, uint64_t* n_out,
+                         tg_stats* stats);
 
 /* ---- counting without device allocation --------------------------------
  * No counterpart in the reference: tuna allocates its partition buffers and

@@ -1,0 +1,103 @@
+"""Jobs of several samples: every sample's pairs are the same as when it runs
+alone (bit-exact), whatever else is in the job — uneven sizes, empty and
+tiny samples, samples that share k-mers, k = 31 and k = 63, the job API and
+the one-call tg_count_batch."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _samples(n, seed):
+    from tuna_gb300 import synth
+    rng = np.random.default_rng(seed)
+    out = []
+    shared = synth.genome(60_000, seed, 0.45)
+    for i in range(n):
+        if i % 7 == 3:
+            out.append(np.zeros(0, dtype=np.uint8))                     # empty sample
+            continue
+        if i % 7 == 5:
+            out.append(np.frombuffer(b"ACGTACGTAC\nACG", dtype=np.uint8))  # shorter than k
+            continue
+        glen = int(rng.integers(5_000, 200_000))
+        g = shared if i % 3 == 0 else synth.genome(glen, seed * 1000 + i, 0.41, fam_a=(3, 300, 0.2),
+                                                    div=(0.05, 0.1), micro=0.03)
+        cov = float(rng.uniform(2, 12))
+        nreads = max(1, int(glen * cov / 150))
+        fq = synth.reads_fastq(g, nreads, 150, 0.005, 0.0005, seed * 7 + i)
+        out.append(synth.fastq_sequence_stream(fq))
+    return out
+
+
+def _same(a, b):
+    a, b = a.sorted(), b.sorted()
+    return len(a) == len(b) and np.array_equal(a.keys, b.keys) and np.array_equal(a.counts, b.counts)
+
+
+@pytest.mark.parametrize("k,m", [(31, 21), (63, 21), (21, 17)])
+def test_each_sample_alone_and_in_the_mix(k, m):
+    import tuna_gb300 as T
+    smp = _samples(12, 5)
+    with T.Context(0) as ctx:
+        mix, _ = ctx.run(k, m, samples=smp)
+        assert mix.samples is not None and len(mix.samples) == len(mix)
+        assert int(mix.samples.max(initial=0)) < len(smp)
+        for i, s in enumerate(smp):
+            alone, _ = ctx.run(k, m, seq=s)
+            assert _same(mix.sample(i), alone), f"sample {i}"
+
+
+def test_many_small_samples():
+    import tuna_gb300 as T
+    from tuna_gb300 import synth
+    smp = []
+    for i in range(300):
+        g = synth.genome(3_000 + 50 * i, 900 + i, 0.5)
+        fq = synth.reads_fastq(g, 60, 150, 0.005, 0.0, 3 + i)
+        smp.append(synth.fastq_sequence_stream(fq))
+    with T.Context(0) as ctx:
+        mix, _ = ctx.run(31, 21, samples=smp)
+        for i in (0, 1, 57, 150, 299):
+            alone, _ = ctx.run(31, 21, seq=smp[i])
+            assert _same(mix.sample(i), alone), f"sample {i}"
+        assert sum(len(ctx.run(31, 21, seq=s)[0]) for s in smp[:20]) == int((mix.samples < 20).sum())
+
+
+def test_count_batch_one_call():
+    import tuna_gb300 as T
+    torch = pytest.importorskip("torch")
+    smp = _samples(9, 8)
+    with T.Context(0) as ctx:
+        want, _ = ctx.run(31, 21, samples=smp)
+        L = T.library()
+        bufs = [torch.from_numpy(np.array(s, dtype=np.uint8)).pin_memory() if s.size else None for s in smp]
+        ptrs = (ctypes.c_void_p * len(smp))(*[b.data_ptr() if b is not None else None for b in bufs])
+        lens = (ctypes.c_size_t * len(smp))(*[int(s.size) for s in smp])
+        cap = len(want) + 5
+        keys = torch.zeros(cap, dtype=torch.int64, pin_memory=True)
+        cnt = torch.zeros(cap, dtype=torch.int32, pin_memory=True)
+        sid = torch.zeros(cap, dtype=torch.int32, pin_memory=True)
+        o = T._JobOpts(31, 21, 16, 1, (1 << 64) - 1, 0, 0)
+        n_out = ctypes.c_uint64()
+        st = T._Stats()
+        rc = L.tg_count_batch(ctx.h, ctypes.byref(o), len(smp), ptrs, lens, ctypes.c_void_p(keys.data_ptr()),
+                              ctypes.c_void_p(cnt.data_ptr()), ctypes.c_void_p(sid.data_ptr()), cap,
+                              ctypes.byref(n_out), ctypes.byref(st))
+        assert rc == 0, L.tg_last_error(ctx.h)
+        n = int(n_out.value)
+        got = T.Result(keys[:n].numpy().view(np.uint64).reshape(n, 1), cnt[:n].numpy().view(np.uint32), {}, 31,
+                       sid[:n].numpy().view(np.uint32))
+        assert n == len(want)
+        for i in range(len(smp)):
+            assert _same(got.sample(i), want.sample(i)), f"sample {i}"
+
+
+def test_export_needs_one_sample():
+    import tuna_gb300 as T
+    smp = _samples(3, 2)
+    with T.Context(0) as ctx:
+        with pytest.raises(T.GpuError):
+            ctx.run(31, 21, samples=smp, export=True, want_results=False)

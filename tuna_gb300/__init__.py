@@ -76,7 +76,8 @@ ABI_SYMBOLS = ["tg_ctx_create", "tg_ctx_destroy", "tg_last_error", "tg_ctx_strea
                "tg_job_begin", "tg_job_feed_seq", "tg_job_feed_seq_device", "tg_job_feed_fastx",
                "tg_job_feed_file", "tg_job_run", "tg_job_stats", "tg_job_result_size", "tg_job_key_words",
                "tg_job_result_copy", "tg_job_drain", "tg_job_write", "tg_job_export_partitions", "tg_job_end",
-               "tg_count_seq", "tg_count_seq_device_noalloc"]
+               "tg_count_seq", "tg_count_seq_device_noalloc", "tg_job_next_sample", "tg_job_sample_count",
+               "tg_job_result_samples", "tg_count_batch"]
 
 
 def library(build_if_missing: bool = True) -> ctypes.CDLL:
@@ -120,9 +121,16 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
     L.tg_count_seq_device_noalloc.argtypes = [ctypes.POINTER(_JobOpts), vp, sz, vp, vp, u64,
                                               ctypes.POINTER(u64), vp, ctypes.c_char_p, sz]
     L.tg_count_seq_device_noalloc.restype = i32
+    L.tg_job_next_sample.argtypes = [vp]
+    L.tg_job_sample_count.argtypes = [vp]
+    L.tg_job_sample_count.restype = u32
+    L.tg_job_result_samples.argtypes = [vp, vp, u64, u64]
+    L.tg_count_batch.argtypes = [vp, ctypes.POINTER(_JobOpts), u32, ctypes.POINTER(vp), ctypes.POINTER(sz), vp, vp,
+                                 vp, u64, ctypes.POINTER(u64), ctypes.POINTER(_Stats)]
     for fn in ("tg_ctx_create", "tg_ctx_destroy", "tg_job_begin", "tg_job_feed_seq", "tg_job_feed_seq_device",
                "tg_job_feed_fastx", "tg_job_feed_file", "tg_job_run", "tg_job_stats", "tg_job_result_copy",
-               "tg_job_drain", "tg_job_write", "tg_job_export_partitions", "tg_job_end", "tg_count_seq"):
+               "tg_job_drain", "tg_job_write", "tg_job_export_partitions", "tg_job_end", "tg_count_seq",
+               "tg_job_next_sample", "tg_job_result_samples", "tg_count_batch"):
         getattr(L, fn).restype = i32
     _lib = L
     return L
@@ -145,13 +153,22 @@ class Result:
     counts: np.ndarray        # (n,) uint32
     stats: Dict[str, float] = field(default_factory=dict)
     k: int = 0
+    samples: Optional[np.ndarray] = None  # (n,) uint32 sample of each pair (jobs of several samples)
 
     def __len__(self) -> int:
         return int(self.counts.shape[0])
 
     def sorted(self) -> "Result":
         order = np.lexsort(tuple(self.keys[:, i] for i in range(self.keys.shape[1])))
-        return Result(self.keys[order], self.counts[order], self.stats, self.k)
+        return Result(self.keys[order], self.counts[order], self.stats, self.k,
+                      None if self.samples is None else self.samples[order])
+
+    def sample(self, i: int) -> "Result":
+        """The pairs of sample i (all pairs for a job of one sample)."""
+        if self.samples is None:
+            return self
+        sel = self.samples == i
+        return Result(self.keys[sel], self.counts[sel], self.stats, self.k)
 
 
 def label_array(keys: np.ndarray, k: int) -> np.ndarray:
@@ -224,16 +241,24 @@ class Context:
         return _JobOpts(k, m, n_parts, ci, min(cx, _U64_MAX), gpu_parts, 0)
 
     def run(self, k: int, m: int, *, seq=None, dev_seq=None, dev_len: int = 0, fastx=None, files=(),
-            n_parts: int = 16, ci: int = 1, cx: int = _U64_MAX, gpu_parts: int = 0,
+            samples=None, n_parts: int = 16, ci: int = 1, cx: int = _U64_MAX, gpu_parts: int = 0,
             export: bool = False, want_results: bool = True):
         """Run one job. seq: host stream (bytes / uint8 array); dev_seq: device
-        pointer (int) of dev_len bytes; fastx: FASTA/FASTQ bytes; files: paths.
+        pointer (int) of dev_len bytes; fastx: FASTA/FASTQ bytes; files: paths;
+        samples: host streams counted as separate samples of the job (the
+        Result then carries the sample of each pair).
         Returns (Result, partitions or None)."""
         L = self._L
         o = self._opts(k, m, n_parts, ci, cx, gpu_parts)
         j = ctypes.c_void_p()
         self.check(L.tg_job_begin(self.h, ctypes.byref(o), ctypes.byref(j)))
         try:
+            for i, smp in enumerate(samples or ()):
+                if i:
+                    self.check(L.tg_job_next_sample(j))
+                a = np.ascontiguousarray(np.frombuffer(smp, dtype=np.uint8) if isinstance(smp, (bytes, bytearray))
+                                         else smp, dtype=np.uint8)
+                self.check(L.tg_job_feed_seq(j, a.ctypes.data if a.size else None, a.size))
             if seq is not None:
                 a = np.ascontiguousarray(np.frombuffer(seq, dtype=np.uint8) if isinstance(seq, (bytes, bytearray))
                                          else seq, dtype=np.uint8)
@@ -253,8 +278,13 @@ class Context:
             W = int(L.tg_job_key_words(j))
             keys = np.empty((n, W), dtype=np.uint64)
             counts = np.empty(n, dtype=np.uint32)
+            smp = None
             if want_results and n:
                 self.check(L.tg_job_result_copy(j, keys.ctypes.data, counts.ctypes.data, 0, n))
+            if samples is not None and len(samples) > 1:
+                smp = np.zeros(n, dtype=np.uint32)
+                if want_results and n:
+                    self.check(L.tg_job_result_samples(j, smp.ctypes.data, 0, n))
             parts = None
             if export:
                 parts = [b""] * n_parts
@@ -265,7 +295,7 @@ class Context:
 
                 cb = _PART_SINK(sink)
                 self.check(L.tg_job_export_partitions(j, cb, None))
-            return Result(keys, counts, st.as_dict(), k), parts
+            return Result(keys, counts, st.as_dict(), k, smp), parts
         finally:
             L.tg_job_end(j)
 

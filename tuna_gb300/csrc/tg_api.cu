@@ -100,7 +100,7 @@ struct tg_ctx {
     size_t smem_optin = 0;
     unsigned host_threads = 1;
     std::string err;
-    DevBuf seq, packed, valid, desc, xdesc, hist, scratch, okeys, ocnt,
+    DevBuf seq, packed, valid, desc, xdesc, hist, scratch, okeys, ocnt, osamp, samp,
         misc, fbtab, tables;
     cudaEvent_t ev[12] = {};
     // results copied to the host while counting runs (tg_count_seq)
@@ -148,6 +148,8 @@ struct tg_job {
     tg_stats st{};
     // optional: output ranges handed out as phase 2 finishes them
     const P2Overlap* overlap = nullptr;
+    // samples: sample i starts at stream position sample_start[i]
+    std::vector<unsigned long long> sample_start{0};
     const uint8_t* seq_ptr() const { return ext ? ext : ctx->seq.as<uint8_t>(); }
 };
 
@@ -202,7 +204,7 @@ tg_status tg_ctx_destroy(tg_ctx* ctx) {
     if (ctx->st) cudaStreamSynchronize(ctx->st);
     DevBuf* bufs[] = {&ctx->seq, &ctx->packed, &ctx->valid, &ctx->desc, &ctx->xdesc, &ctx->hist,
                       &ctx->scratch,
-                      &ctx->okeys, &ctx->ocnt, &ctx->misc, &ctx->fbtab, &ctx->tables};
+                      &ctx->okeys, &ctx->ocnt, &ctx->osamp, &ctx->samp, &ctx->misc, &ctx->fbtab, &ctx->tables};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
     for (auto& e : ctx->ev)
@@ -299,6 +301,20 @@ tg_status tg_job_feed_seq_device(tg_job* j, const uint8_t* dseq, size_t len) {
     return append_stream(j, dseq, len, cudaMemcpyDeviceToDevice);
 }
 
+tg_status tg_job_next_sample(tg_job* j) {
+    if (!j) return TG_ERR_ARG;
+    if (j->ran) return j->ctx->fail(TG_ERR_STATE, "feed after run");
+    if (j->sample_start.size() >= TG_MAX_SAMPLES) return j->ctx->fail(TG_ERR_ARG, "too many samples in one job");
+    if (j->ext) {  // a device feed used in place: move it into the context buffer first
+        const tg_status s = append_stream(j, nullptr, 0, cudaMemcpyDeviceToDevice);
+        if (s != TG_OK) return s;
+    }
+    j->sample_start.push_back(j->n);
+    return TG_OK;
+}
+
+uint32_t tg_job_sample_count(const tg_job* j) { return j ? (uint32_t)j->sample_start.size() : 0; }
+
 tg_status tg_job_feed_fastx(tg_job* j, const uint8_t* data, size_t len) {
     if (!j || (!data && len)) return TG_ERR_ARG;
     if (len == 0) return j->ctx->fail(TG_ERR_PARSE, "Empty file");
@@ -323,7 +339,14 @@ tg_status tg_job_feed_file(tg_job* j, const char* path) {
 }
 
 // Phase 1 cut (optionally the export variant) over the current stream.
-static tg_status run_cut(tg_job* j, bool exp, uint32_t p1_bits, int* launches) {
+struct CutSamples {
+    const unsigned long long* start = nullptr;  // device arrays of the bin layout (counting cut)
+    const uint32_t* base = nullptr;
+    const uint8_t* bits = nullptr;
+    uint32_t n = 0;
+};
+
+static tg_status run_cut(tg_job* j, bool exp, uint32_t p1_bits, int* launches, const CutSamples& cs = CutSamples()) {
     tg_ctx* ctx = j->ctx;
     const uint64_t n = j->n;
     const uint32_t p1 = 1u << p1_bits;
@@ -349,8 +372,8 @@ static tg_status run_cut(tg_job* j, bool exp, uint32_t p1_bits, int* launches) {
             CK(ctx->ensure(ctx->hist, kmers_off + (size_t)p1 * 8), "alloc histograms");
             CK(cudaMemsetAsync(ctx->hist.as<uint8_t>() + kmers_off, 0, (size_t)p1 * 8, ctx->st), "memset");
         } else {
-            CK(ctx->ensure(ctx->hist, (size_t)4 << MLO_BITS), "alloc bin histogram");
-            CK(cudaMemsetAsync(ctx->hist.p, 0, (size_t)4 << MLO_BITS, ctx->st), "memset");
+            CK(ctx->ensure(ctx->hist, (size_t)4 << BIN_BITS), "alloc bin histogram");
+            CK(cudaMemsetAsync(ctx->hist.p, 0, (size_t)4 << BIN_BITS, ctx->st), "memset");
         }
         CK(cudaMemsetAsync(ctx->misc.as<uint8_t>() + MISC_CUT_STATS, 0, 24, ctx->st), "memset");
         CK(cudaMemsetAsync(ctx->misc.as<uint8_t>() + MISC_OVERFLOW, 0, 4, ctx->st), "memset");
@@ -370,6 +393,10 @@ static tg_status run_cut(tg_job* j, bool exp, uint32_t p1_bits, int* launches) {
         P.stats = reinterpret_cast<unsigned long long*>(ctx->misc.as<uint8_t>() + MISC_CUT_STATS);
         P.overflow = reinterpret_cast<uint32_t*>(ctx->misc.as<uint8_t>() + MISC_OVERFLOW);
         P.xdesc = exp ? ctx->xdesc.as<uint64_t>() : nullptr;
+        P.sample_start = cs.start;
+        P.sample_bin_base = cs.base;
+        P.sample_bin_bits = cs.bits;
+        P.n_samples = cs.n;
         CK(cudaEventRecord(ctx->ev[2], ctx->st), "event");
         CK(launch_cut(P, ctx->tables.as<HashTables>(), exp, ctx->st), "k_cut");
         CK(cudaEventRecord(ctx->ev[3], ctx->st), "event");
@@ -421,7 +448,26 @@ tg_status tg_job_run(tg_job* j) {
     if (!p1) p1 = std::min<uint32_t>(1024, std::max<uint32_t>(16, next_pow2_u32(n / 32768)));
     uint32_t p1_bits = 0;
     while ((1u << p1_bits) < p1) ++p1_bits;
-    tg_status s = run_cut(j, false, p1_bits, &launches);
+    // the bins of the samples (2^20 in all, cut into p1 segments for one sample)
+    std::vector<unsigned long long> starts = j->sample_start;
+    starts.push_back(n);
+    const SampleBins B = layout_bins(starts, (1u << BIN_BITS) >> p1_bits);
+    const uint32_t ns = (uint32_t)B.base.size();
+    {
+        const size_t bytes = 8 * (size_t)(ns + 1) + 4 * (size_t)ns + ns + 64;
+        CK(ctx->ensure(ctx->samp, bytes), "alloc samples");
+        uint8_t* d = ctx->samp.as<uint8_t>();
+        CK(cudaMemcpyAsync(d, B.start.data(), 8 * (size_t)(ns + 1), cudaMemcpyHostToDevice, ctx->st), "h2d");
+        CK(cudaMemcpyAsync(d + 8 * (size_t)(ns + 1), B.base.data(), 4 * (size_t)ns, cudaMemcpyHostToDevice, ctx->st),
+           "h2d");
+        CK(cudaMemcpyAsync(d + 12 * (size_t)ns + 8, B.bits.data(), ns, cudaMemcpyHostToDevice, ctx->st), "h2d");
+    }
+    CutSamples cs;
+    cs.start = ctx->samp.as<unsigned long long>();
+    cs.base = reinterpret_cast<const uint32_t*>(ctx->samp.as<uint8_t>() + 8 * (size_t)(ns + 1));
+    cs.bits = ctx->samp.as<uint8_t>() + 12 * (size_t)ns + 8;
+    cs.n = ns;
+    tg_status s = run_cut(j, false, p1_bits, &launches, cs);
     if (s != TG_OK) return s;
     unsigned long long cstats[3] = {0, 0, 0};
     const uint32_t C = j->n_cta;
@@ -435,10 +481,12 @@ tg_status tg_job_run(tg_job* j) {
     const uint64_t out_cap = std::max<uint64_t>(n_kmers, 1);
     CK(ctx->ensure(ctx->okeys, out_cap * key_bytes(W)), "alloc output keys");
     CK(ctx->ensure(ctx->ocnt, out_cap * 4), "alloc output counts");
+    if (ns > 1) CK(ctx->ensure(ctx->osamp, out_cap * 4), "alloc output samples");
     P2Input in{};
     in.W = W;
     in.k = k;
-    in.p1_bits = p1_bits;
+    in.segs = B.segs.data();
+    in.n_segs = (uint32_t)B.segs.size();
     in.n_sm = (uint32_t)ctx->n_sm;
     in.packed = ctx->packed.as<uint32_t>();
     in.desc = ctx->desc.as<uint64_t>();
@@ -456,6 +504,7 @@ tg_status tg_job_run(tg_job* j) {
     P2Output out{};
     out.keys = ctx->okeys.p;
     out.counts = ctx->ocnt.as<uint32_t>();
+    out.samples = ns > 1 ? ctx->osamp.as<uint32_t>() : nullptr;
     out.cap = out_cap;
     std::string msg;
     auto fallback_table = [&](size_t bytes) -> void* {
@@ -476,7 +525,7 @@ tg_status tg_job_run(tg_job* j) {
     S.superkmers = cstats[1];
     S.distinct = out.distinct;
     S.out = out.n_out;
-    S.gpu_parts = p1;
+    S.gpu_parts = (uint32_t)B.segs.size();
     S.fallback_groups = out.fallback_groups;
     S.groups = out.groups;
     S.heavy_groups = (uint32_t)out.heavy_groups;
@@ -517,6 +566,22 @@ tg_status tg_job_result_copy(tg_job* j, uint64_t* keys, uint32_t* counts, uint64
            "d2h counts");
     CK(cudaStreamSynchronize(ctx->st), "d2h");
     j->st.d2h_ms += now_ms() - t0;
+    return TG_OK;
+}
+
+tg_status tg_job_result_samples(tg_job* j, uint32_t* samples, uint64_t first, uint64_t n) {
+    if (!j || (!samples && n)) return TG_ERR_ARG;
+    tg_ctx* ctx = j->ctx;
+    if (!j->ran) return ctx->fail(TG_ERR_STATE, "result before run");
+    if (first + n > j->n_out) return ctx->fail(TG_ERR_ARG, "result range out of bounds");
+    if (!n) return TG_OK;
+    if (j->sample_start.size() <= 1) {
+        memset(samples, 0, n * 4);
+        return TG_OK;
+    }
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    CK(cudaMemcpyAsync(samples, ctx->osamp.as<uint32_t>() + first, n * 4, cudaMemcpyDeviceToHost, ctx->st), "d2h");
+    CK(cudaStreamSynchronize(ctx->st), "d2h");
     return TG_OK;
 }
 
@@ -580,6 +645,7 @@ tg_status tg_job_export_partitions(tg_job* j, tg_part_sink_fn sink, void* user) 
     if (!j || !sink) return TG_ERR_ARG;
     tg_ctx* ctx = j->ctx;
     if (!j->ran) return ctx->fail(TG_ERR_STATE, "export before run");
+    if (j->sample_start.size() > 1) return ctx->fail(TG_ERR_UNSUPPORTED, "partition export of a job of several samples");
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
     int launches = 0;
     // packed bases stay valid until the next run on this context
@@ -634,21 +700,49 @@ tg_status tg_job_end(tg_job* j) {
     return TG_OK;
 }
 
-tg_status tg_count_seq(tg_ctx* ctx, const tg_job_opts* opts, const uint8_t* seq, size_t len, uint64_t* keys,
-                       uint32_t* counts, uint64_t cap, uint64_t* n_out, tg_stats* stats) {
-    if (!ctx || !opts || !n_out) return TG_ERR_ARG;
+// The one-call entry points: feed, run with the counting pass in waves whose
+// pairs are copied to the caller's buffers (on the copy stream) while the
+// next waves count, wait for the copies.
+static tg_status count_host(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_samples, const uint8_t* const* seqs,
+                            const size_t* lens, uint64_t* keys, uint32_t* counts, uint32_t* samples, uint64_t cap,
+                            uint64_t* n_out, tg_stats* stats) {
+    if (!ctx || !opts || !n_out || (n_samples && (!seqs || !lens))) return TG_ERR_ARG;
+    *n_out = 0;
+    if (n_samples > TG_MAX_SAMPLES) return ctx->fail(TG_ERR_ARG, "too many samples in one job");
     tg_job* j = nullptr;
     tg_status s = tg_job_begin(ctx, opts, &j);
     if (s != TG_OK) return s;
-    s = tg_job_feed_seq(j, seq, len);
-    // the counting pass runs in waves; each wave's pairs go to the caller's
-    // buffers on the copy stream while the next waves count
+    // one buffer, separators everywhere, then every sample copied to its place
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < n_samples; ++i) {
+        if (!seqs[i] && lens[i]) s = TG_ERR_ARG;
+        total += lens[i] + 1;
+    }
+    if (s == TG_OK && total) {
+        const double t0 = now_ms();
+        cudaError_t e = cudaSetDevice(ctx->device);
+        if (e == cudaSuccess) e = ctx->ensure(ctx->seq, total + 1);
+        if (e == cudaSuccess) e = cudaMemsetAsync(ctx->seq.p, '\n', total, ctx->st);
+        uint64_t off = 0;
+        for (uint32_t i = 0; i < n_samples && e == cudaSuccess; ++i) {
+            if (i > 0) j->sample_start.push_back(off);
+            if (lens[i]) e = cudaMemcpyAsync(ctx->seq.as<uint8_t>() + off, seqs[i], lens[i], cudaMemcpyHostToDevice, ctx->st);
+            off += lens[i] + 1;
+            j->st.input_bytes += lens[i];
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+        if (e != cudaSuccess) s = ctx->cuda_fail(e, "copy input");
+        j->n = total;
+        j->used_ctx_seq = true;
+        j->st.h2d_ms += now_ms() - t0;
+    }
     P2Overlap ov;
     ov.waves = 8;
     ov.wave_out = ctx->wave_out;
     ov.wave_ev = ctx->wave_ev;
     double d2h_issue_ms = 0;
     const int W = j->W;
+    const bool multi = n_samples > 1;
     ov.on_range = [&](uint64_t lo, uint64_t hi) -> tg_status {
         const uint64_t h = std::min<uint64_t>(hi, cap);
         if (h <= lo) return TG_OK;
@@ -659,6 +753,9 @@ tg_status tg_count_seq(tg_ctx* ctx, const tg_job_opts* opts, const uint8_t* seq,
         if (counts)
             CK(cudaMemcpyAsync(counts + lo, ctx->ocnt.as<uint32_t>() + lo, (h - lo) * 4, cudaMemcpyDeviceToHost,
                                ctx->st_copy), "d2h counts");
+        if (samples && multi)
+            CK(cudaMemcpyAsync(samples + lo, ctx->osamp.as<uint32_t>() + lo, (h - lo) * 4, cudaMemcpyDeviceToHost,
+                               ctx->st_copy), "d2h samples");
         d2h_issue_ms += now_ms() - t0;
         return TG_OK;
     };
@@ -671,10 +768,24 @@ tg_status tg_count_seq(tg_ctx* ctx, const tg_job_opts* opts, const uint8_t* seq,
     if (s == TG_OK) {
         *n_out = j->n_out;
         if (j->n_out > cap) s = ctx->fail(TG_ERR_ARG, "result buffer too small");
+        else if (samples && !multi) memset(samples, 0, j->n_out * 4);
     }
     if (stats) *stats = j->st;
     tg_job_end(j);
     return s;
+}
+
+tg_status tg_count_seq(tg_ctx* ctx, const tg_job_opts* opts, const uint8_t* seq, size_t len, uint64_t* keys,
+                       uint32_t* counts, uint64_t cap, uint64_t* n_out, tg_stats* stats) {
+    if (!seq && len) return TG_ERR_ARG;
+    return count_host(ctx, opts, 1, &seq, &len, keys, counts, nullptr, cap, n_out, stats);
+}
+
+tg_status tg_count_batch(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_samples, const uint8_t* const* seqs,
+                         const size_t* lens, uint64_t* keys, uint32_t* counts, uint32_t* samples, uint64_t cap,
+                         uint64_t* n_out, tg_stats* stats) {
+    if (n_samples == 0) return TG_ERR_ARG;
+    return count_host(ctx, opts, n_samples, seqs, lens, keys, counts, samples, cap, n_out, stats);
 }
 
 }  // extern "C"

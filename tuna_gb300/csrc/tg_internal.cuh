@@ -10,10 +10,10 @@
 //   desc    u64[C][cap]      per Phase-1 CTA: one descriptor per superkmer record
 //                            (start position, k-mer count, low 20 bits of its
 //                            minimizer hash; see desc_pack)
-//   binhist u32[2^20]        k-mer instances per (bucket, bin): the 20 low bits of the
-//                            minimizer hash, bucket bits first; scanned into kofs
-//   keys    u64 x W [K]      every canonical k-mer instance, bucket-major and, inside
-//                            a bucket, grouped by minimizer bin (W = 1 for k <= 31)
+//   binhist u32[2^20]        k-mer instances per bin (each sample owns a range of bins,
+//                            one picked by minimizer hash); scanned into kofs
+//   keys    u64 x W [K]      every canonical k-mer instance, grouped by bin
+//                            (W = 1 for k <= 31)
 //   out     keys + u32 counts of the distinct k-mers that pass ci/cx
 #pragma once
 #include <cstdint>
@@ -42,20 +42,20 @@ struct HashTables {
 
 // Superkmer record descriptor (u64): the record covers the k-mers starting at
 // positions [start, start + nk) of the stream; its bases are read from
-// `packed` when it is counted. mlo = low 20 bits of the minimizer hash: the
-// low log2(P) bits pick the bucket, the rest the bin inside the bucket.
-constexpr int MLO_BITS = 20;
+// `packed` when it is counted. bin (20 bits) places the record's k-mers in the
+// key array: the 2^20 bins are shared out among the samples of a job, sample s
+// owning [base_s, base_s + 2^bits_s), and a record of sample s goes to bin
+// base_s + (minimizer hash mod 2^bits_s). All instances of a canonical k-mer
+// of one sample share its minimizer, hence its bin. (The export cut stores
+// the low 20 bits of the minimizer hash there instead.)
 constexpr int DESC_START_BITS = 36;
-__host__ __device__ __forceinline__ uint64_t desc_pack(uint64_t start, uint32_t nk, uint32_t mlo) {
-    return start | ((uint64_t)nk << DESC_START_BITS) | ((uint64_t)(mlo & 0xFFFFFu) << 44);
+constexpr int BIN_BITS = 20;
+__host__ __device__ __forceinline__ uint64_t desc_pack(uint64_t start, uint32_t nk, uint32_t bin) {
+    return start | ((uint64_t)nk << DESC_START_BITS) | ((uint64_t)(bin & 0xFFFFFu) << 44);
 }
 __host__ __device__ __forceinline__ uint64_t desc_start(uint64_t d) { return d & ((1ull << DESC_START_BITS) - 1); }
 __host__ __device__ __forceinline__ uint32_t desc_nk(uint64_t d) { return (uint32_t)(d >> DESC_START_BITS) & 0xFFu; }
-__host__ __device__ __forceinline__ uint32_t desc_mlo(uint64_t d) { return (uint32_t)(d >> 44); }
-// Index of (bucket, bin) of a minimizer's low bits in bucket-major order.
-__host__ __device__ __forceinline__ uint32_t bin_index(uint32_t mlo, uint32_t p1_bits) {
-    return ((mlo & ((1u << p1_bits) - 1)) << (MLO_BITS - p1_bits)) | (mlo >> p1_bits);
-}
+__host__ __device__ __forceinline__ uint32_t desc_bin(uint64_t d) { return (uint32_t)(d >> 44); }
 
 // Offset (in u32 units) of the u64 per-bucket k-mer counters that follow the
 // u32 [P][C] record histogram: rounded up so the u64 array is 8-byte aligned
@@ -77,7 +77,12 @@ struct CutParams {
     uint64_t desc_cap;
     uint32_t* n_desc;        // [n_cta]
     uint32_t* hist;          // export cut: u32 [P][n_cta] records, then u64 [P] k-mers per bucket
-    uint32_t* binhist;       // counting cut: [2^20] k-mers per (bucket, bin), bucket-major
+    uint32_t* binhist;       // counting cut: [2^20] k-mers per bin
+    // samples of the job (counting cut): sample i is positions [start[i], start[i+1])
+    const unsigned long long* sample_start;  // [n_samples + 1]
+    const uint32_t* sample_bin_base;         // [n_samples] first bin of each sample
+    const uint8_t* sample_bin_bits;          // [n_samples] log2 bins of each sample
+    uint32_t n_samples;
     unsigned long long* stats;  // [0] kmers, [1] records, [2] runs
     uint32_t* overflow;      // set when a CTA's descriptor list is full
     // export mode: full descriptors (start, minimizer hash, min_pos, nk)
@@ -94,7 +99,12 @@ struct Slice {
 struct Group {
     unsigned long long lo, hi;  // key range [lo, hi)
     uint32_t parts, part;       // count only the keys whose hash part is `part` of `parts`
-    uint32_t pad[2];
+    uint32_t sample, pad;       // the sample whose keys these are
+};
+
+// A run of consecutive bins of one sample that k_plan cuts into groups.
+struct Segment {
+    uint32_t bin_lo, bin_hi, sample, pad;
 };
 
 // Counters of one Phase-2 run (device, u64 each).
@@ -112,8 +122,9 @@ struct KeysParams {
     const uint32_t* packed;
     const uint64_t* desc;              // phase-1 descriptor lists
     const Slice* slices;
-    unsigned long long* kofs;          // [2^20 + 1] first key of each (bucket, bin); advanced by k_keys
-    uint32_t p1_bits, nb;              // buckets, bins per bucket (p1 * nb = 2^20)
+    unsigned long long* kofs;          // [2^20 + 1] first key of each bin; advanced by k_keys
+    const Segment* segs;               // k_plan: one warp per segment
+    uint32_t n_segs;
     uint32_t target;                   // k-mer instances per group
     int k;
     void* keys;                        // u64 x W per k-mer instance
@@ -134,6 +145,7 @@ struct CountParams {
     uint64_t ci, cx;
     void* out_keys;                    // u64 x W per distinct k-mer
     uint32_t* out_counts;
+    uint32_t* out_sample;              // sample of each pair (jobs of several samples), or null
     uint64_t out_cap;
     unsigned long long* ctr;           // P2Counter
     uint32_t smem_slots;               // table capacity in shared memory
@@ -145,7 +157,7 @@ struct CountParams {
 struct FallbackParams {
     const void* keys;
     unsigned long long lo, hi;
-    uint32_t parts, part;
+    uint32_t parts, part, sample;
     void* tkeys;          // S slots
     uint32_t* tcnt;
     uint32_t mask;

@@ -5,6 +5,7 @@
 
 #include <functional>
 #include <string>
+#include <vector>
 
 #include "tuna_gpu.h"
 
@@ -23,23 +24,37 @@ size_t key_bytes(int W);
 uint32_t count_slots(int W);
 
 // Phase 2 of one job, shared by the entry points: the phase-1 descriptor lists
-// and (bucket, bin) k-mer counts in, distinct keys and counts out.
+// and the k-mer counts per bin in, distinct keys and counts (and their
+// samples) out.
+// Bins of one sample per segment; the host helper below lays them out.
+struct SampleBins {
+    std::vector<unsigned long long> start;  // [n + 1] stream position of each sample, then the end
+    std::vector<uint32_t> base;             // [n] first bin
+    std::vector<uint8_t> bits;              // [n] log2 bins
+    std::vector<Segment> segs;
+};
+// Shares the 2^20 bins out among samples in proportion to their length (a
+// power of two each) and cuts each sample's bins into segments of at most
+// seg_bins bins.
+SampleBins layout_bins(const std::vector<unsigned long long>& sample_start, uint32_t seg_bins);
 struct P2Input {
     int W, k;                          // key words, k
-    uint32_t p1_bits;                  // log2 buckets
+    const Segment* segs;               // [n_segs] (host): runs of bins of one sample, cut into groups
+    uint32_t n_segs;
     uint32_t n_sm;
     const uint32_t* packed;
     const uint64_t* desc;              // [n_lists][desc_cap] phase-1 descriptors
     uint64_t desc_cap;
     uint32_t n_lists;
     const uint32_t* n_desc;            // [n_lists] descriptors per list (host)
-    const uint32_t* binhist;           // [2^20] k-mers per (bucket, bin) (device)
+    const uint32_t* binhist;           // [2^20] k-mers per bin (device)
     uint64_t n_kmers;                  // k-mer instances in all
     uint64_t ci, cx;
 };
 struct P2Output {
     void* keys;                        // u64 x W per distinct k-mer
     uint32_t* counts;
+    uint32_t* samples = nullptr;       // sample of each pair, or null
     uint64_t cap;
     uint64_t n_out, distinct, groups, heavy_groups, fallback_groups;
 };

@@ -136,7 +136,12 @@ extern "C" tg_status tg_count_seq_device_noalloc(const tg_job_opts* opts, const 
     const uint64_t desc_cap = chunk + 2ull * tile + L + 64;
     uint64_t* desc = cv.take<uint64_t>((size_t)C * desc_cap);
     uint32_t* n_desc = cv.take<uint32_t>(C);
-    uint32_t* binhist = cv.take<uint32_t>((size_t)1 << MLO_BITS);
+    uint32_t* binhist = cv.take<uint32_t>((size_t)1 << BIN_BITS);
+    // one sample: all 2^20 bins, cut into p1 segments
+    const SampleBins B = layout_bins({0ull, (unsigned long long)n}, (1u << BIN_BITS) >> p1_bits);
+    unsigned long long* s_start = cv.take<unsigned long long>(2);
+    uint32_t* s_base = cv.take<uint32_t>(1);
+    uint8_t* s_bits = cv.take<uint8_t>(1);
     if (!cv.ok) { set_err(errbuf, errlen, "input too large for the no-allocation scratch"); return TG_ERR_ARG; }
     // counters in misc (u64 indices): [0..2] k-mers/records/runs, [3] bases, [4] overflow (u32)
     uint32_t* overflow = reinterpret_cast<uint32_t*>(misc + 4);
@@ -144,7 +149,10 @@ extern "C" tg_status tg_count_seq_device_noalloc(const tg_job_opts* opts, const 
     const HashTables T = make_hash_tables(m);
     NA_CK(cudaMemcpyAsync(tables, &T, sizeof T, cudaMemcpyHostToDevice, st), "upload tables");
     NA_CK(cudaMemsetAsync(misc, 0, 32 * 8, st), "memset");
-    NA_CK(cudaMemsetAsync(binhist, 0, (size_t)4 << MLO_BITS, st), "memset");
+    NA_CK(cudaMemsetAsync(binhist, 0, (size_t)4 << BIN_BITS, st), "memset");
+    NA_CK(cudaMemcpyAsync(s_start, B.start.data(), 16, cudaMemcpyHostToDevice, st), "h2d");
+    NA_CK(cudaMemcpyAsync(s_base, B.base.data(), 4, cudaMemcpyHostToDevice, st), "h2d");
+    NA_CK(cudaMemcpyAsync(s_bits, B.bits.data(), 1, cudaMemcpyHostToDevice, st), "h2d");
     // ---- phase 1
     NA_CK(launch_pack(d_seq, n, packed, valid, pw, misc + 3, st), "k_pack");
     CutParams P{};
@@ -153,6 +161,7 @@ extern "C" tg_status tg_count_seq_device_noalloc(const tg_job_opts* opts, const 
     P.p1_bits = p1_bits; P.n_cta = C; P.chunk = chunk;
     P.desc = desc; P.desc_cap = desc_cap; P.n_desc = n_desc;
     P.hist = nullptr; P.binhist = binhist; P.stats = misc; P.overflow = overflow; P.xdesc = nullptr;
+    P.sample_start = s_start; P.sample_bin_base = s_base; P.sample_bin_bits = s_bits; P.n_samples = 1;
     NA_CK(launch_cut(P, tables, false, st), "k_cut");
     int launches = 0;
     std::vector<uint32_t> nd(C);
@@ -165,7 +174,7 @@ extern "C" tg_status tg_count_seq_device_noalloc(const tg_job_opts* opts, const 
     if (ovf) { set_err(errbuf, errlen, "descriptor capacity exceeded"); return TG_ERR_DEVICE; }
     // ---- phase 2 in what is left
     P2Input in{};
-    in.W = W; in.k = k; in.p1_bits = p1_bits; in.n_sm = (uint32_t)n_sm;
+    in.W = W; in.k = k; in.segs = B.segs.data(); in.n_segs = (uint32_t)B.segs.size(); in.n_sm = (uint32_t)n_sm;
     in.packed = packed; in.desc = desc; in.desc_cap = desc_cap; in.n_lists = C; in.n_desc = nd.data();
     in.binhist = binhist; in.n_kmers = cstats[0];
     in.ci = o.ci; in.cx = o.cx;

@@ -593,10 +593,25 @@ k_cut_seq(CutParams P, const HashTables* __restrict__ gT) {
     bool overflowed = false;
     uint64_t* dlist = P.desc + (uint64_t)c * P.desc_cap;
     auto owned = [&](int64_t cs) { return cs >= cstart && cs < cend; };
-    auto put = [&](uint32_t idx, int64_t st, uint32_t nk, uint32_t mlo) {
-        if (idx < P.desc_cap) dlist[idx] = desc_pack((uint64_t)st, nk, mlo);
+    // sample holding position pos: the last i with sample_start[i] <= pos
+    auto sample_of = [&](int64_t pos) -> uint32_t {
+        uint32_t lo = 0, hi = P.n_samples - 1;
+        while (lo < hi) {
+            const uint32_t md = (lo + hi + 1) >> 1;
+            if ((int64_t)P.sample_start[md] <= pos) lo = md; else hi = md - 1;
+        }
+        return lo;
+    };
+    // the thread's current segment [seg_lo, seg_lo + SEG) and, if it lies in one
+    // sample, that sample (else ~0: look each record up)
+    int64_t seg_lo = 0;
+    uint32_t seg_s = 0;
+    auto put = [&](uint32_t idx, int64_t st, uint32_t nk, uint32_t mh) {
+        const uint32_t smp = (seg_s != ~0u && st >= seg_lo && st < seg_lo + SEG) ? seg_s : sample_of(st);
+        const uint32_t bin = P.sample_bin_base[smp] + (mh & ((1u << P.sample_bin_bits[smp]) - 1));
+        if (idx < P.desc_cap) dlist[idx] = desc_pack((uint64_t)st, nk, bin);
         else overflowed = true;
-        atomicAdd(&P.binhist[bin_index(mlo, P.p1_bits)], nk);  // the key array's layout
+        atomicAdd(&P.binhist[bin], nk);  // the key array's layout
         loc_kmers += nk;
         loc_recs += 1;
     };
@@ -625,6 +640,11 @@ k_cut_seq(CutParams P, const HashTables* __restrict__ gT) {
         // from register copies of the words, shifted once per step.
         const int64_t ps = t0 + (int64_t)tid * SEG;
         const int64_t pb = ps - 1;  // m-mer 0; k-mer kp = i - w starts at pb + kp
+        seg_lo = ps;
+        {
+            const uint32_t a = sample_of(ps), b = sample_of(ps + SEG - 1);
+            seg_s = a == b ? a : ~0u;
+        }
         const uint32_t ra = (uint32_t)((uint64_t)(pb + TG_PAD) - A0);  // staged index of base pb
         uint64_t f, r;
         nt_init(T, s_pk, ra, m, f, r);

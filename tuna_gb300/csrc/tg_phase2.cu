@@ -156,19 +156,20 @@ __device__ __forceinline__ U128 kmer_key<2>(const uint32_t* __restrict__ pk, uin
 }
 
 // ---------------------------------------------------------------- k_plan
-// One warp per bucket: its groups, from the scanned (bucket, bin) key offsets
-// ko[0 .. nb]. Greedy, in bin order: a group starting at bin s takes the most
-// bins e - s with at most `target` keys (one bin if that bin alone is larger;
-// such a group is listed as heavy). Each step is one upper-bound search over
-// ko, done by the warp as a 32-way search.
+// One warp per segment (a run of consecutive bins of one sample): its groups,
+// from the scanned key offsets ko[bin]. Greedy, in bin order: a group starting
+// at bin s takes the most bins e - s with at most `target` keys (one bin if that
+// bin alone is larger; such a group is listed as heavy). Each step is one
+// upper-bound search over ko, done by the warp as a 32-way search.
 constexpr int PLAN_THREADS = 256;
 
-__global__ void __launch_bounds__(PLAN_THREADS) k_plan(KeysParams P, uint32_t n_buckets) {
+__global__ void __launch_bounds__(PLAN_THREADS) k_plan(KeysParams P) {
     const int lane = threadIdx.x & 31;
-    const uint32_t b = blockIdx.x * (PLAN_THREADS / 32) + (threadIdx.x >> 5);
-    if (b >= n_buckets) return;  // warp-uniform
-    const uint32_t nb = P.nb;
-    const unsigned long long* ko = P.kofs + (uint64_t)b * nb;
+    const uint32_t sg = blockIdx.x * (PLAN_THREADS / 32) + (threadIdx.x >> 5);
+    if (sg >= P.n_segs) return;  // warp-uniform
+    const Segment seg = P.segs[sg];
+    const uint32_t nb = seg.bin_hi - seg.bin_lo;
+    const unsigned long long* ko = P.kofs + seg.bin_lo;
     const unsigned long long end = ko[nb];
     const unsigned long long T = P.target;
     uint32_t s = 0;
@@ -199,7 +200,8 @@ __global__ void __launch_bounds__(PLAN_THREADS) k_plan(KeysParams P, uint32_t n_
                 g.hi = ke;
                 g.parts = 1;
                 g.part = 0;
-                g.pad[0] = g.pad[1] = 0;
+                g.sample = seg.sample;
+                g.pad = 0;
                 P.groups[heavy][q] = g;
             }
         }
@@ -232,7 +234,7 @@ __global__ void __launch_bounds__(P2_THREADS) k_keys(KeysParams P) {
         }
         const uint32_t nk = desc_nk(dv);  // 0 past the slice; at least 1 otherwise
         unsigned long long koff = 0;
-        if (nk) koff = atomicAdd(&P.kofs[bin_index(desc_mlo(dv), P.p1_bits)], (unsigned long long)nk);
+        if (nk) koff = atomicAdd(&P.kofs[desc_bin(dv)], (unsigned long long)nk);
         uint32_t incl = nk;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -540,6 +542,7 @@ __global__ void __launch_bounds__(COUNT_THREADS, COUNT_PER_SM) k_count(CountPara
                     if (i < P.out_cap) {
                         O::store(P.out_keys, i, keys[sl]);
                         P.out_counts[i] = cnt[sl];
+                        if (P.out_sample) P.out_sample[i] = g.sample;
                     }
                 }
                 keys[sl] = O::empty();
@@ -585,7 +588,7 @@ __global__ void k_fb_init(void* keys, uint32_t* cnt, uint64_t S) {
 // Write the occupied slots that pass ci/cx (warp-aggregated output atomics).
 template <int W>
 __global__ void __launch_bounds__(256) k_fb_extract(const void* keys, const uint32_t* cnt, uint64_t S,
-                                                    CountParams P) {
+                                                    CountParams P, uint32_t sample) {
     using O = KeyOps<W>;
     const auto* kk = reinterpret_cast<const typename O::Key*>(keys);
     const int lane = threadIdx.x & 31;
@@ -614,6 +617,7 @@ __global__ void __launch_bounds__(256) k_fb_extract(const void* keys, const uint
             if (o < P.out_cap) {
                 O::store(P.out_keys, o, key);
                 P.out_counts[o] = c;
+                if (P.out_sample) P.out_sample[o] = sample;
             }
         }
     }
@@ -651,7 +655,7 @@ struct Carve {
     }
 };
 
-constexpr uint32_t NBIN_ALL = 1u << MLO_BITS;  // (bucket, bin) pairs
+constexpr uint32_t NBIN_ALL = 1u << BIN_BITS;
 
 struct P2Plan {
     uint64_t n_slices = 0, groups_cap = 0, retry_cap = 0, n_keys_alloc = 0, nsum = 0;
@@ -670,10 +674,10 @@ P2Plan make_plan(const P2Input& in) {
         }
     }
     L.n_slices = L.slices.size();
-    // a bucket of K keys has fewer than 2 K / target + 1 groups (two neighbouring
+    // a segment of K keys has fewer than 2 K / target + 1 groups (two neighbouring
     // groups of k_plan hold more than `target` keys together)
     const uint64_t target = count_slots(in.W) * 7 / 10;
-    L.groups_cap = 2 * in.n_kmers / target + ((uint64_t)1 << in.p1_bits) + 1;
+    L.groups_cap = 2 * in.n_kmers / target + in.n_segs + 1;
     L.retry_cap = std::max<uint64_t>(4096, 2 * L.groups_cap);
     L.n_keys_alloc = in.n_kmers + 1;
     L.nsum = (NBIN_ALL + 8191) / 8192 + 2;
@@ -687,6 +691,7 @@ struct P2Regions {
     unsigned long long* work; // [0..15] group counters of the first pass's launches, [16] of a retry pass
     unsigned long long* kofs;
     unsigned long long* sums;
+    Segment* segs;
     Slice* slices;
     Group* normal;
     Group* heavy;
@@ -702,6 +707,7 @@ P2Regions carve(Carve& c, const P2Input& in, const P2Plan& L) {
     R.work = c.take<unsigned long long>(17);
     R.kofs = c.take<unsigned long long>(NBIN_ALL + 1);
     R.sums = c.take<unsigned long long>(L.nsum);
+    R.segs = c.take<Segment>(in.n_segs + 1);
     R.slices = c.take<Slice>(L.n_slices + 1);
     R.normal = c.take<Group>(L.groups_cap);
     R.heavy = c.take<Group>(L.groups_cap);
@@ -712,6 +718,42 @@ P2Regions carve(Carve& c, const P2Input& in, const P2Plan& L) {
     return R;
 }
 }  // namespace
+
+SampleBins layout_bins(const std::vector<unsigned long long>& sample_start, uint32_t seg_bins) {
+    SampleBins B;
+    B.start = sample_start;
+    const size_t n = sample_start.size() - 1;
+    const double total = (double)std::max<unsigned long long>(1, sample_start[n] - sample_start[0]);
+    B.base.resize(n);
+    B.bits.resize(n);
+    // 2^bits <= the sample's share of `budget` bins (at least one bin)
+    auto assign = [&](double budget) {
+        uint64_t used = 0;
+        for (size_t i = 0; i < n; ++i) {
+            const double share = budget * (double)(sample_start[i + 1] - sample_start[i]) / total;
+            uint32_t b = 0;
+            while (b < BIN_BITS && (double)(2ull << b) <= share) ++b;
+            B.bits[i] = (uint8_t)b;
+            B.base[i] = (uint32_t)used;
+            used += 1ull << b;
+        }
+        return used;
+    };
+    if (assign((double)NBIN_ALL) > NBIN_ALL) assign((double)(NBIN_ALL - n));  // one bin set aside per sample
+    seg_bins = std::max<uint32_t>(1, seg_bins);
+    for (size_t i = 0; i < n; ++i) {
+        const uint32_t hi = B.base[i] + (1u << B.bits[i]);
+        for (uint32_t lo = B.base[i]; lo < hi; lo += seg_bins) {
+            Segment sg;
+            sg.bin_lo = lo;
+            sg.bin_hi = std::min(hi, lo + seg_bins);
+            sg.sample = (uint32_t)i;
+            sg.pad = 0;
+            B.segs.push_back(sg);
+        }
+    }
+    return B;
+}
 
 size_t phase2_scratch_bytes(const P2Input& in) {
     const P2Plan L = make_plan(in);
@@ -734,7 +776,6 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
                      int* launches, std::string& err, const P2Overlap& ov) {
     const P2Plan L = make_plan(in);
     const int W = in.W;
-    const uint32_t nb = NBIN_ALL >> in.p1_bits;
     Carve c{static_cast<uint8_t*>(scratch), 0, scratch_cap, true};
     const P2Regions R = carve(c, in, L);
     if (!c.ok) { err = "phase-2 scratch too small"; return TG_ERR_OOM; }
@@ -744,7 +785,8 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
     if (L.n_slices)
         P2_CK(cudaMemcpyAsync(R.slices, L.slices.data(), L.n_slices * sizeof(Slice), cudaMemcpyHostToDevice, st),
               "h2d");
-    // (bucket, bin) k-mer counts -> first key of each bin
+    P2_CK(cudaMemcpyAsync(R.segs, in.segs, (size_t)in.n_segs * sizeof(Segment), cudaMemcpyHostToDevice, st), "h2d");
+    // k-mer counts per bin -> first key of each bin
     P2_CK(launch_scan(in.binhist, NBIN_ALL, R.kofs, R.sums, R.kofs + NBIN_ALL, st, launches), "scan");
 
     KeysParams K{};
@@ -752,8 +794,8 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
     K.desc = in.desc;
     K.slices = R.slices;
     K.kofs = R.kofs;
-    K.p1_bits = in.p1_bits;
-    K.nb = nb;
+    K.segs = R.segs;
+    K.n_segs = in.n_segs;
     K.target = slots * 7 / 10;  // as in make_plan
     K.k = in.k;
     K.keys = R.keys;
@@ -762,8 +804,8 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
     K.groups_cap = L.groups_cap;
     K.ctr = R.ctr;
     {
-        const uint32_t p1 = 1u << in.p1_bits, warps = PLAN_THREADS / 32;
-        k_plan<<<(p1 + warps - 1) / warps, PLAN_THREADS, 0, st>>>(K, p1);  // before k_keys moves the cursors
+        const uint32_t warps = PLAN_THREADS / 32;
+        k_plan<<<(in.n_segs + warps - 1) / warps, PLAN_THREADS, 0, st>>>(K);  // before k_keys moves the cursors
     }
     P2_CK(cudaGetLastError(), "k_plan");
     ++*launches;
@@ -786,6 +828,7 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
     Q.cx = in.cx;
     Q.out_keys = out.keys;
     Q.out_counts = out.counts;
+    Q.out_sample = out.samples;
     Q.out_cap = out.cap;
     Q.ctr = R.ctr;
     Q.retry_cap = L.retry_cap;
@@ -871,6 +914,7 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
             F.hi = g.hi;
             F.parts = g.parts;
             F.part = g.part;
+            F.sample = g.sample;
             F.tkeys = tab;
             F.tcnt = reinterpret_cast<uint32_t*>(tab + kbytes);
             F.mask = (uint32_t)(S - 1);
@@ -880,11 +924,11 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
             if (W == 1) {
                 k_fb_init<1><<<grid, 256, 0, st>>>(F.tkeys, F.tcnt, S);
                 k_fb_insert<1><<<grid, 256, 0, st>>>(F);
-                k_fb_extract<1><<<grid, 256, 0, st>>>(F.tkeys, F.tcnt, S, Q);
+                k_fb_extract<1><<<grid, 256, 0, st>>>(F.tkeys, F.tcnt, S, Q, g.sample);
             } else {
                 k_fb_init<2><<<grid, 256, 0, st>>>(F.tkeys, F.tcnt, S);
                 k_fb_insert<2><<<grid, 256, 0, st>>>(F);
-                k_fb_extract<2><<<grid, 256, 0, st>>>(F.tkeys, F.tcnt, S, Q);
+                k_fb_extract<2><<<grid, 256, 0, st>>>(F.tkeys, F.tcnt, S, Q, g.sample);
             }
             P2_CK(cudaGetLastError(), "fallback");
             *launches += 3;
