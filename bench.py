@@ -31,6 +31,8 @@ import sys
 import tempfile
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -48,6 +50,13 @@ def parse_args():
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the 3.1 Gbp workload")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-plain section")
+    ap.add_argument("--no-serve", action="store_true", help="skip the served section")
+    ap.add_argument("--batch-samples", type=int, default=2000)
+    ap.add_argument("--batch-scale", type=float, default=0.004,
+                    help="genome sizes of the batched mix: log-uniform 10 kbp - 50 Mbp times this")
+    ap.add_argument("--serve-seconds", type=float, default=10.0, help="length of the arrival trace")
+    ap.add_argument("--serve-scale", type=float, default=0.05, help="request sizes: median 20 Mbp times this")
     ap.add_argument("--cpu-shard-mbp", type=float, default=80.0,
                     help="CPU sample: one shard of this size per core (about 10 s of work on 16 cores)")
     return ap.parse_args()
@@ -160,6 +169,112 @@ def time_cpu(threads: int, shard_mbp: float, steps: int = 1, warmup: int = 0, sa
             "sample": f"{threads} shards x {shard_mbp:g} Mbp of the workload ({bases / 1e6:.0f} Mbp), "
                       f"k={K} m={M} n={NPARTS}; phase 1 parallel over shards, phase 2 over partitions",
             "seconds": t, "distinct": len(r)}
+
+
+# ------------------------------------------------------------------ batched and served
+def _pinned_copy(a):
+    import torch
+    return torch.from_numpy(np.array(a, dtype=np.uint8)).pin_memory().numpy()
+
+
+def batched_vs_plain(ctx, n_samples: int, scale: float):
+    """The 2,000-sample mix, counted sample by sample through tg_count_seq (the
+    plain path) and all at once through tg_count_batch; same pairs required."""
+    import ctypes
+    import tuna_gb300 as T
+    from tuna_gb300 import synth
+    from tuna_gb300.serve import _pinned
+    plan = synth.batch_plan(n_samples, scale=scale)
+    seqs = [_pinned_copy(synth.fastq_sequence_stream(synth.batch_sample_fastq(s, i))) for i, s in enumerate(plan)]
+    bases = int(sum(s.size for s in seqs))
+    L = T.library()
+    o = T._JobOpts(31, 21, 16, 1, (1 << 64) - 1, 0, 0)
+    cap_one = max(s.size for s in seqs)
+    k1, c1 = _pinned(cap_one, np.uint64), _pinned(cap_one, np.uint32)
+    n_out = ctypes.c_uint64()
+    st = T._Stats()
+
+    def plain(i):
+        rc = L.tg_count_seq(ctx.h, ctypes.byref(o), ctypes.c_void_p(seqs[i].ctypes.data), seqs[i].size,
+                            ctypes.c_void_p(k1.ctypes.data), ctypes.c_void_p(c1.ctypes.data), cap_one,
+                            ctypes.byref(n_out), ctypes.byref(st))
+        ctx.check(rc)
+        return int(n_out.value)
+
+    plain(0)  # warm
+    t0 = time.perf_counter()
+    per_plain = [plain(i) for i in range(len(seqs))]
+    t_plain = time.perf_counter() - t0
+    cap = bases
+    kb, cb = _pinned(cap, np.uint64), _pinned(cap, np.uint32)
+    off = np.zeros(len(seqs) + 1, dtype=np.uint64)
+    ptrs = (ctypes.c_void_p * len(seqs))(*[s.ctypes.data for s in seqs])
+    lens = (ctypes.c_size_t * len(seqs))(*[int(s.size) for s in seqs])
+
+    def batch():
+        rc = L.tg_count_batch(ctx.h, ctypes.byref(o), len(seqs), ptrs, lens, ctypes.c_void_p(kb.ctypes.data),
+                              ctypes.c_void_p(cb.ctypes.data), ctypes.c_void_p(off.ctypes.data), cap,
+                              ctypes.byref(n_out), ctypes.byref(st))
+        ctx.check(rc)
+
+    batch()  # warm
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        batch()
+        ts.append(time.perf_counter() - t0)
+    t_batch = statistics.median(ts)
+    per_batch = np.diff(off.astype(np.int64)).tolist()
+    same_sizes = per_batch == per_plain
+    # bit-exact on a few samples: the plain result against the sample's range of the batch
+    exact = True
+    for i in (0, 1, len(seqs) // 2, len(seqs) - 1):
+        n = plain(i)
+        a = T.Result(k1[:n].reshape(n, 1).copy(), c1[:n].copy(), {}, 31).sorted()
+        lo, hi = int(off[i]), int(off[i + 1])
+        b = T.Result(kb[lo:hi].reshape(-1, 1).copy(), cb[lo:hi].copy(), {}, 31).sorted()
+        exact &= np.array_equal(a.keys, b.keys) and np.array_equal(a.counts, b.counts)
+    return {"workload": f"{len(seqs)} samples, genomes log-uniform {10_000 * scale / 1e3:g} kbp - "
+                        f"{50e6 * scale / 1e3:g} kbp, 150 bp reads at 5-50x, 0.3-1% errors, k=31 m=21",
+            "samples": len(seqs), "bases": bases,
+            "plain_gbases_s": bases / t_plain / 1e9, "batched_gbases_s": bases / t_batch / 1e9,
+            "speedup": t_plain / t_batch, "plain_s": t_plain, "batched_s": t_batch,
+            "api": "tg_count_seq per sample vs tg_count_batch, pinned host buffers, results in host memory",
+            "same_pairs_per_sample": bool(same_sizes), "bit_exact_checked_samples": bool(exact)}
+
+
+def served(seconds: float, scale: float):
+    """Poisson arrivals at 50 requests/s replayed in real time against the
+    continuous-batching server; latency from arrival to result in host memory."""
+    import tuna_gb300 as T
+    from tuna_gb300 import synth
+    from tuna_gb300.serve import Server
+    plan = synth.served_plan(50.0, seconds, scale=scale)
+    seqs = [_pinned_copy(synth.fastq_sequence_stream(synth.request_fastq(r, i))) for i, r in enumerate(plan)]
+    bases = int(sum(s.size for s in seqs))
+    with Server(0, workers=2) as srv:
+        # warm both workers' contexts
+        for f in [srv.submit(seqs[0], plan[0].k, plan[0].m) for _ in range(2)]:
+            f.result()
+        srv.batches = 0
+        t0 = time.perf_counter()
+        futs = []
+        for r, s in zip(plan, seqs):
+            dt = t0 + r.arrival_s - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            futs.append(srv.submit(s, r.k, r.m))
+        ans = [f.result() for f in futs]
+        t_end = max(a.done for a in ans)
+        n_batches = srv.batches
+    lat = np.array([a.latency_s for a in ans]) * 1e3
+    return {"workload": f"Poisson 50 req/s for {seconds:g} s, sizes log-normal median {20 * scale:g} Mbp "
+                        f"(sigma 1.5, cap {2000 * scale:g} Mbp), reads 100-250 bp at 0.5% error, "
+                        f"k in {{21, 25, 31}}",
+            "requests": len(ans), "bases": bases, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max()),
+            "gbases_s": bases / (t_end - t0) / 1e9, "batches": n_batches, "workers": 2,
+            "api": "tuna_gb300.serve.Server over tg_count_batch, results in host memory"}
 
 
 # ------------------------------------------------------------------ reference arm
@@ -323,6 +438,13 @@ def main():
     else:
         parity_full = None
 
+    batched = None
+    if rank == 0 and not args.no_batch:
+        batched = batched_vs_plain(ctx, args.batch_samples, args.batch_scale)
+    serve = None
+    if rank == 0 and not args.no_serve:
+        serve = served(args.serve_seconds, args.serve_scale)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = time_cpu(os.cpu_count() or 1, args.cpu_shard_mbp)
@@ -350,6 +472,8 @@ def main():
             "cpu_baseline": cpu,
             "e2e": e2e,
             "parity": parity_full,
+            "batched": batched,
+            "serve": serve,
             "gpu_launches": launches,
             "clocks": clk,
         }

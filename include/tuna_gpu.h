@@ -167,12 +167,14 @@ tg_status tg_job_end(tg_job* job);
  * tg_job_next_sample(), feed the second, and so on. Each sample is counted on
  * its own (a k-mer present in two samples gives two pairs, each with its own
  * count), all of them in one pass of the device pipeline; the result of a
- * sample is the same as when it runs alone. tg_job_result_samples gives the
- * sample index of each pair. Partition export needs a job of one sample. */
+ * sample is the same as when it runs alone. The results of such a job are
+ * sample-major: sample i's pairs are [offsets[i], offsets[i+1]) of
+ * tg_job_result_copy, with offsets from tg_job_sample_offsets (n + 1 entries).
+ * Partition export needs a job of one sample. */
 #define TG_MAX_SAMPLES 65536u
 tg_status tg_job_next_sample(tg_job* job);
 uint32_t tg_job_sample_count(const tg_job* job);
-tg_status tg_job_result_samples(tg_job* job, uint32_t* samples, uint64_t first, uint64_t n);
+tg_status tg_job_sample_offsets(tg_job* job, uint64_t* offsets);
 
 /* ---- one-call helpers --------------------------------------------------- */
 /* Count a host sequence stream end to end: H2D, both phases, D2H of the
@@ -182,10 +184,11 @@ tg_status tg_count_seq(tg_ctx* ctx, const tg_job_opts* opts, const uint8_t* seq,
                        uint64_t* keys, uint32_t* counts, uint64_t cap, uint64_t* n_out,
                        tg_stats* stats);
 /* The same for n_samples host sequence streams counted as separate samples in
- * one job; samples (cap u32, may be NULL) receives the sample of each pair. */
+ * one job: the pairs come back sample-major, sample i's being
+ * [sample_offsets[i], sample_offsets[i+1]) (n_samples + 1 entries, may be NULL). */
 tg_status tg_count_batch(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_samples,
                          const uint8_t* const* seqs, const size_t* lens, uint64_t* keys,
-                         uint32_t* counts, uint32_t* samples, uint64_t cap, uint64_t* n_out,
+                         uint32_t* counts, uint64_t* sample_offsets, uint64_t cap, uint64_t* n_out,
                          tg_stats* stats);
 
 /* ---- counting without device allocation --------------------------------

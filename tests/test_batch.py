@@ -79,20 +79,21 @@ def test_count_batch_one_call():
         cap = len(want) + 5
         keys = torch.zeros(cap, dtype=torch.int64, pin_memory=True)
         cnt = torch.zeros(cap, dtype=torch.int32, pin_memory=True)
-        sid = torch.zeros(cap, dtype=torch.int32, pin_memory=True)
+        off = np.zeros(len(smp) + 1, dtype=np.uint64)
         o = T._JobOpts(31, 21, 16, 1, (1 << 64) - 1, 0, 0)
         n_out = ctypes.c_uint64()
         st = T._Stats()
         rc = L.tg_count_batch(ctx.h, ctypes.byref(o), len(smp), ptrs, lens, ctypes.c_void_p(keys.data_ptr()),
-                              ctypes.c_void_p(cnt.data_ptr()), ctypes.c_void_p(sid.data_ptr()), cap,
+                              ctypes.c_void_p(cnt.data_ptr()), ctypes.c_void_p(off.ctypes.data), cap,
                               ctypes.byref(n_out), ctypes.byref(st))
         assert rc == 0, L.tg_last_error(ctx.h)
         n = int(n_out.value)
-        got = T.Result(keys[:n].numpy().view(np.uint64).reshape(n, 1), cnt[:n].numpy().view(np.uint32), {}, 31,
-                       sid[:n].numpy().view(np.uint32))
-        assert n == len(want)
+        assert n == len(want) and int(off[-1]) == n and np.all(np.diff(off.astype(np.int64)) >= 0)
+        kk = keys[:n].numpy().view(np.uint64).reshape(n, 1)
+        cc = cnt[:n].numpy().view(np.uint32)
         for i in range(len(smp)):
-            assert _same(got.sample(i), want.sample(i)), f"sample {i}"
+            a, b = int(off[i]), int(off[i + 1])
+            assert _same(T.Result(kk[a:b], cc[a:b], {}, 31), want.sample(i)), f"sample {i}"
 
 
 def test_export_needs_one_sample():

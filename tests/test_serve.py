@@ -1,0 +1,52 @@
+"""The serving loop (tuna_gb300/serve.py): requests of different k and sizes,
+submitted from two client threads while batches are on the device; each
+answer must be exactly the request's result alone."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests():
+    from tuna_gb300 import synth
+    rng = np.random.default_rng(3)
+    reqs = []
+    for i in range(24):
+        k = [21, 25, 31][i % 3]
+        m = 17 if k == 21 else 21
+        glen = int(rng.integers(2_000, 120_000))
+        g = synth.genome(glen, 500 + i, 0.45, fam_a=(2, 300, 0.1), div=(0.05, 0.1))
+        fq = synth.reads_fastq(g, max(1, glen * 8 // 175), (100, 250), 0.005, 0.0, 40 + i)
+        reqs.append((synth.fastq_sequence_stream(fq), k, m))
+    return reqs
+
+
+def test_served_answers_match_alone():
+    import tuna_gb300 as T
+    from tuna_gb300.serve import Server
+    reqs = _requests()
+    futs = [None] * len(reqs)
+
+    def client(idx):
+        for i in idx:
+            futs[i] = srv.submit(reqs[i][0], reqs[i][1], reqs[i][2])
+            time.sleep(0.003)
+
+    with Server(0, workers=2) as srv:
+        th = [threading.Thread(target=client, args=(range(j, len(reqs), 2),)) for j in range(2)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        answers = [f.result(timeout=300) for f in futs]
+    with T.Context(0) as ctx:
+        for (seq, k, m), a in zip(reqs, answers):
+            want = ctx.run(k, m, seq=seq)[0].sorted()
+            got = T.Result(a.keys.copy(), a.counts.copy(), {}, k).sorted()
+            assert len(got) == len(want)
+            assert np.array_equal(got.keys, want.keys) and np.array_equal(got.counts, want.counts)
+            assert a.latency_s >= 0
+    assert max(a.batch for a in answers) >= 1

@@ -77,7 +77,7 @@ ABI_SYMBOLS = ["tg_ctx_create", "tg_ctx_destroy", "tg_last_error", "tg_ctx_strea
                "tg_job_feed_file", "tg_job_run", "tg_job_stats", "tg_job_result_size", "tg_job_key_words",
                "tg_job_result_copy", "tg_job_drain", "tg_job_write", "tg_job_export_partitions", "tg_job_end",
                "tg_count_seq", "tg_count_seq_device_noalloc", "tg_job_next_sample", "tg_job_sample_count",
-               "tg_job_result_samples", "tg_count_batch"]
+               "tg_job_sample_offsets", "tg_count_batch"]
 
 
 def library(build_if_missing: bool = True) -> ctypes.CDLL:
@@ -124,13 +124,13 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
     L.tg_job_next_sample.argtypes = [vp]
     L.tg_job_sample_count.argtypes = [vp]
     L.tg_job_sample_count.restype = u32
-    L.tg_job_result_samples.argtypes = [vp, vp, u64, u64]
+    L.tg_job_sample_offsets.argtypes = [vp, vp]
     L.tg_count_batch.argtypes = [vp, ctypes.POINTER(_JobOpts), u32, ctypes.POINTER(vp), ctypes.POINTER(sz), vp, vp,
                                  vp, u64, ctypes.POINTER(u64), ctypes.POINTER(_Stats)]
     for fn in ("tg_ctx_create", "tg_ctx_destroy", "tg_job_begin", "tg_job_feed_seq", "tg_job_feed_seq_device",
                "tg_job_feed_fastx", "tg_job_feed_file", "tg_job_run", "tg_job_stats", "tg_job_result_copy",
                "tg_job_drain", "tg_job_write", "tg_job_export_partitions", "tg_job_end", "tg_count_seq",
-               "tg_job_next_sample", "tg_job_result_samples", "tg_count_batch"):
+               "tg_job_next_sample", "tg_job_sample_offsets", "tg_count_batch"):
         getattr(L, fn).restype = i32
     _lib = L
     return L
@@ -282,9 +282,9 @@ class Context:
             if want_results and n:
                 self.check(L.tg_job_result_copy(j, keys.ctypes.data, counts.ctypes.data, 0, n))
             if samples is not None and len(samples) > 1:
-                smp = np.zeros(n, dtype=np.uint32)
-                if want_results and n:
-                    self.check(L.tg_job_result_samples(j, smp.ctypes.data, 0, n))
+                off = np.zeros(len(samples) + 1, dtype=np.uint64)
+                self.check(L.tg_job_sample_offsets(j, off.ctypes.data))
+                smp = np.repeat(np.arange(len(samples), dtype=np.uint32), np.diff(off).astype(np.int64))
             parts = None
             if export:
                 parts = [b""] * n_parts

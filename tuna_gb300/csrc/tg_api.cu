@@ -100,7 +100,7 @@ struct tg_ctx {
     size_t smem_optin = 0;
     unsigned host_threads = 1;
     std::string err;
-    DevBuf seq, packed, valid, desc, xdesc, hist, scratch, okeys, ocnt, osamp, samp,
+    DevBuf seq, packed, valid, desc, xdesc, hist, scratch, okeys, ocnt, osamp, samp, okeys2, ocnt2, osoff,
         misc, fbtab, tables;
     cudaEvent_t ev[12] = {};
     // results copied to the host while counting runs (tg_count_seq)
@@ -204,7 +204,7 @@ tg_status tg_ctx_destroy(tg_ctx* ctx) {
     if (ctx->st) cudaStreamSynchronize(ctx->st);
     DevBuf* bufs[] = {&ctx->seq, &ctx->packed, &ctx->valid, &ctx->desc, &ctx->xdesc, &ctx->hist,
                       &ctx->scratch,
-                      &ctx->okeys, &ctx->ocnt, &ctx->osamp, &ctx->samp, &ctx->misc, &ctx->fbtab, &ctx->tables};
+                      &ctx->okeys, &ctx->ocnt, &ctx->osamp, &ctx->samp, &ctx->okeys2, &ctx->ocnt2, &ctx->osoff, &ctx->misc, &ctx->fbtab, &ctx->tables};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
     for (auto& e : ctx->ev)
@@ -481,7 +481,12 @@ tg_status tg_job_run(tg_job* j) {
     const uint64_t out_cap = std::max<uint64_t>(n_kmers, 1);
     CK(ctx->ensure(ctx->okeys, out_cap * key_bytes(W)), "alloc output keys");
     CK(ctx->ensure(ctx->ocnt, out_cap * 4), "alloc output counts");
-    if (ns > 1) CK(ctx->ensure(ctx->osamp, out_cap * 4), "alloc output samples");
+    if (ns > 1) {
+        CK(ctx->ensure(ctx->osamp, out_cap * 4), "alloc output samples");
+        CK(ctx->ensure(ctx->okeys2, out_cap * key_bytes(W)), "alloc output keys");
+        CK(ctx->ensure(ctx->ocnt2, out_cap * 4), "alloc output counts");
+        CK(ctx->ensure(ctx->osoff, 8 * ((size_t)ns + 1)), "alloc sample offsets");
+    }
     P2Input in{};
     in.W = W;
     in.k = k;
@@ -497,6 +502,7 @@ tg_status tg_job_run(tg_job* j) {
     in.n_kmers = n_kmers;
     in.ci = j->o.ci;
     in.cx = j->o.cx;
+    in.n_samples = ns;
     const size_t p2_bytes = phase2_scratch_bytes(in);
     CK(ctx->ensure(ctx->scratch, p2_bytes), "alloc phase-2 scratch");
     CK(cudaEventRecord(ctx->ev[6], ctx->st), "event");
@@ -505,6 +511,12 @@ tg_status tg_job_run(tg_job* j) {
     out.keys = ctx->okeys.p;
     out.counts = ctx->ocnt.as<uint32_t>();
     out.samples = ns > 1 ? ctx->osamp.as<uint32_t>() : nullptr;
+    out.n_samples = ns;
+    if (ns > 1) {
+        out.keys2 = ctx->okeys2.p;
+        out.counts2 = ctx->ocnt2.as<uint32_t>();
+        out.sample_off = ctx->osoff.as<unsigned long long>();
+    }
     out.cap = out_cap;
     std::string msg;
     auto fallback_table = [&](size_t bytes) -> void* {
@@ -558,29 +570,31 @@ tg_status tg_job_result_copy(tg_job* j, uint64_t* keys, uint32_t* counts, uint64
     if (!n) return TG_OK;
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
     const double t0 = now_ms();
+    // jobs of several samples: the sample-major copy (each sample's pairs one range)
+    const bool multi = j->sample_start.size() > 1;
+    const uint8_t* kd = (multi ? ctx->okeys2 : ctx->okeys).as<uint8_t>();
+    const uint32_t* cd = (multi ? ctx->ocnt2 : ctx->ocnt).as<uint32_t>();
     if (keys)
-        CK(cudaMemcpyAsync(keys, ctx->okeys.as<uint8_t>() + first * key_bytes(j->W), n * key_bytes(j->W),
-                           cudaMemcpyDeviceToHost, ctx->st), "d2h keys");
-    if (counts)
-        CK(cudaMemcpyAsync(counts, ctx->ocnt.as<uint32_t>() + first, n * 4, cudaMemcpyDeviceToHost, ctx->st),
-           "d2h counts");
+        CK(cudaMemcpyAsync(keys, kd + first * key_bytes(j->W), n * key_bytes(j->W), cudaMemcpyDeviceToHost, ctx->st),
+           "d2h keys");
+    if (counts) CK(cudaMemcpyAsync(counts, cd + first, n * 4, cudaMemcpyDeviceToHost, ctx->st), "d2h counts");
     CK(cudaStreamSynchronize(ctx->st), "d2h");
     j->st.d2h_ms += now_ms() - t0;
     return TG_OK;
 }
 
-tg_status tg_job_result_samples(tg_job* j, uint32_t* samples, uint64_t first, uint64_t n) {
-    if (!j || (!samples && n)) return TG_ERR_ARG;
+tg_status tg_job_sample_offsets(tg_job* j, uint64_t* offsets) {
+    if (!j || !offsets) return TG_ERR_ARG;
     tg_ctx* ctx = j->ctx;
     if (!j->ran) return ctx->fail(TG_ERR_STATE, "result before run");
-    if (first + n > j->n_out) return ctx->fail(TG_ERR_ARG, "result range out of bounds");
-    if (!n) return TG_OK;
-    if (j->sample_start.size() <= 1) {
-        memset(samples, 0, n * 4);
+    const size_t ns = j->sample_start.size();
+    if (ns <= 1) {
+        offsets[0] = 0;
+        offsets[1] = j->n_out;
         return TG_OK;
     }
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
-    CK(cudaMemcpyAsync(samples, ctx->osamp.as<uint32_t>() + first, n * 4, cudaMemcpyDeviceToHost, ctx->st), "d2h");
+    CK(cudaMemcpyAsync(offsets, ctx->osoff.p, 8 * (ns + 1), cudaMemcpyDeviceToHost, ctx->st), "d2h");
     CK(cudaStreamSynchronize(ctx->st), "d2h");
     return TG_OK;
 }
@@ -704,7 +718,7 @@ tg_status tg_job_end(tg_job* j) {
 // pairs are copied to the caller's buffers (on the copy stream) while the
 // next waves count, wait for the copies.
 static tg_status count_host(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_samples, const uint8_t* const* seqs,
-                            const size_t* lens, uint64_t* keys, uint32_t* counts, uint32_t* samples, uint64_t cap,
+                            const size_t* lens, uint64_t* keys, uint32_t* counts, uint64_t* sample_off, uint64_t cap,
                             uint64_t* n_out, tg_stats* stats) {
     if (!ctx || !opts || !n_out || (n_samples && (!seqs || !lens))) return TG_ERR_ARG;
     *n_out = 0;
@@ -753,14 +767,20 @@ static tg_status count_host(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_sam
         if (counts)
             CK(cudaMemcpyAsync(counts + lo, ctx->ocnt.as<uint32_t>() + lo, (h - lo) * 4, cudaMemcpyDeviceToHost,
                                ctx->st_copy), "d2h counts");
-        if (samples && multi)
-            CK(cudaMemcpyAsync(samples + lo, ctx->osamp.as<uint32_t>() + lo, (h - lo) * 4, cudaMemcpyDeviceToHost,
-                               ctx->st_copy), "d2h samples");
         d2h_issue_ms += now_ms() - t0;
         return TG_OK;
     };
-    j->overlap = &ov;
+    // several samples: the pairs are reordered sample-major at the end, so they
+    // are copied once the run is over
+    j->overlap = multi ? nullptr : &ov;
     if (s == TG_OK) s = tg_job_run(j);
+    if (s == TG_OK && multi) {
+        const uint64_t h = std::min<uint64_t>(j->n_out, cap);
+        const double t0 = now_ms();
+        if (h) s = tg_job_result_copy(j, keys, counts, 0, h);
+        if (s == TG_OK && sample_off) s = tg_job_sample_offsets(j, sample_off);
+        d2h_issue_ms += now_ms() - t0;
+    }
     const double t_wait = now_ms();
     const cudaError_t ce = cudaStreamSynchronize(ctx->st_copy);
     j->st.d2h_ms += d2h_issue_ms + (now_ms() - t_wait);
@@ -768,7 +788,7 @@ static tg_status count_host(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_sam
     if (s == TG_OK) {
         *n_out = j->n_out;
         if (j->n_out > cap) s = ctx->fail(TG_ERR_ARG, "result buffer too small");
-        else if (samples && !multi) memset(samples, 0, j->n_out * 4);
+        else if (sample_off && !multi) { sample_off[0] = 0; sample_off[1] = j->n_out; }
     }
     if (stats) *stats = j->st;
     tg_job_end(j);
@@ -782,10 +802,10 @@ tg_status tg_count_seq(tg_ctx* ctx, const tg_job_opts* opts, const uint8_t* seq,
 }
 
 tg_status tg_count_batch(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_samples, const uint8_t* const* seqs,
-                         const size_t* lens, uint64_t* keys, uint32_t* counts, uint32_t* samples, uint64_t cap,
+                         const size_t* lens, uint64_t* keys, uint32_t* counts, uint64_t* sample_offsets, uint64_t cap,
                          uint64_t* n_out, tg_stats* stats) {
     if (n_samples == 0) return TG_ERR_ARG;
-    return count_host(ctx, opts, n_samples, seqs, lens, keys, counts, samples, cap, n_out, stats);
+    return count_host(ctx, opts, n_samples, seqs, lens, keys, counts, sample_offsets, cap, n_out, stats);
 }
 
 }  // extern "C"

@@ -50,11 +50,18 @@ struct P2Input {
     const uint32_t* binhist;           // [2^20] k-mers per bin (device)
     uint64_t n_kmers;                  // k-mer instances in all
     uint64_t ci, cx;
+    uint32_t n_samples = 1;
 };
 struct P2Output {
     void* keys;                        // u64 x W per distinct k-mer
     uint32_t* counts;
     uint32_t* samples = nullptr;       // sample of each pair, or null
+    // jobs of several samples: the pairs again, sample-major, and the first pair
+    // of each sample (n_samples + 1 entries, device)
+    uint32_t n_samples = 1;
+    void* keys2 = nullptr;
+    uint32_t* counts2 = nullptr;
+    unsigned long long* sample_off = nullptr;
     uint64_t cap;
     uint64_t n_out, distinct, groups, heavy_groups, fallback_groups;
 };

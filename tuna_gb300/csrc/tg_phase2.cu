@@ -625,6 +625,43 @@ __global__ void __launch_bounds__(256) k_fb_extract(const void* keys, const uint
     if (lane == 0 && distinct) atomicAdd(&P.ctr[P2C_DISTINCT], distinct);
 }
 
+// ---------------------------------------------------------------- sample-major output
+// Jobs of several samples: the pairs, in group order, go sample-major so that
+// each sample's pairs are one range. The pairs of one group are contiguous and
+// of one sample, so the lanes of a warp nearly always share a sample: one
+// atomic per distinct sample in the warp (match_any).
+__global__ void k_samp_hist(const uint32_t* __restrict__ samp, uint64_t n, uint32_t* __restrict__ hist) {
+    for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < n; i0 += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i = i0 + threadIdx.x;
+        const uint32_t s = i < n ? samp[i] : 0xFFFFFFFFu;
+        const unsigned peers = __match_any_sync(0xffffffffu, s);
+        if (s != 0xFFFFFFFFu && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&hist[s], (uint32_t)__popc(peers));
+    }
+}
+
+template <int W>
+__global__ void k_samp_scatter(const void* __restrict__ keys, const uint32_t* __restrict__ cnt,
+                               const uint32_t* __restrict__ samp, uint64_t n, unsigned long long* __restrict__ cur,
+                               void* __restrict__ keys2, uint32_t* __restrict__ cnt2) {
+    using O = KeyOps<W>;
+    const int lane = threadIdx.x & 31;
+    const auto* kk = static_cast<const typename O::Key*>(keys);
+    for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < n; i0 += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i = i0 + threadIdx.x;
+        const uint32_t s = i < n ? samp[i] : 0xFFFFFFFFu;
+        const unsigned peers = __match_any_sync(0xffffffffu, s);
+        const int leader = __ffs(peers) - 1;
+        unsigned long long base = 0;
+        if (s != 0xFFFFFFFFu && lane == leader) base = atomicAdd(&cur[s], (unsigned long long)__popc(peers));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (s != 0xFFFFFFFFu) {
+            const uint64_t o = base + __popc(peers & ((1u << lane) - 1));
+            O::store(keys2, o, kk[i]);
+            cnt2[o] = cnt[i];
+        }
+    }
+}
+
 // ---------------------------------------------------------------- host side
 size_t key_bytes(int W) { return W == 1 ? 8 : 16; }
 
@@ -697,6 +734,7 @@ struct P2Regions {
     Group* heavy;
     Group* retry[2];
     Group* fb;
+    unsigned long long* scur;  // [n_samples] cursors of the sample-major copy
     uint8_t* keys;
 };
 
@@ -714,6 +752,7 @@ P2Regions carve(Carve& c, const P2Input& in, const P2Plan& L) {
     R.retry[0] = c.take<Group>(L.retry_cap);
     R.retry[1] = c.take<Group>(L.retry_cap);
     R.fb = c.take<Group>(FALLBACK_CAP);
+    R.scur = c.take<unsigned long long>(in.n_samples + 1);
     R.keys = c.take<uint8_t>(L.n_keys_alloc * key_bytes(in.W));
     return R;
 }
@@ -946,6 +985,24 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
         if (rs != TG_OK) { err = "result copy failed"; return rs; }
     }
     out.distinct = h[P2C_DISTINCT];
+    if (out.samples && out.n_samples > 1 && out.n_samples <= in.n_samples && out.keys2 && out.counts2 && out.sample_off) {
+        // sample-major copy: per-sample totals, their scan, the scatter
+        const uint64_t n = std::min<uint64_t>(out.n_out, out.cap);
+        uint32_t* hist = reinterpret_cast<uint32_t*>(R.kofs);  // the bin offsets are no longer needed
+        P2_CK(cudaMemsetAsync(hist, 0, 4 * (size_t)out.n_samples, st), "memset");
+        const unsigned grid = (unsigned)in.n_sm * 8;
+        k_samp_hist<<<grid, 256, 0, st>>>(out.samples, n, hist);
+        P2_CK(cudaGetLastError(), "k_samp_hist");
+        P2_CK(launch_scan(hist, out.n_samples, out.sample_off, R.sums, out.sample_off + out.n_samples, st, launches),
+              "scan");
+        unsigned long long* cur = R.scur;  // the offsets, copied, as cursors
+        P2_CK(cudaMemcpyAsync(cur, out.sample_off, 8 * (size_t)out.n_samples, cudaMemcpyDeviceToDevice, st), "copy");
+        if (W == 1) k_samp_scatter<1><<<grid, 256, 0, st>>>(out.keys, out.counts, out.samples, n, cur, out.keys2, out.counts2);
+        else k_samp_scatter<2><<<grid, 256, 0, st>>>(out.keys, out.counts, out.samples, n, cur, out.keys2, out.counts2);
+        P2_CK(cudaGetLastError(), "k_samp_scatter");
+        *launches += 2;
+        P2_CK(cudaStreamSynchronize(st), "sample order");
+    }
     out.groups = h[P2C_NORMAL] + h[P2C_HEAVY];
     out.heavy_groups = h[P2C_HEAVY];
     if (out.n_out > out.cap) { err = "output capacity exceeded"; return TG_ERR_TABLE; }
