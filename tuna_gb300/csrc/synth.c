@@ -238,15 +238,15 @@ static uint64_t read_len_of(rng_t* r, const reads_job* J) {
 }
 
 static void reads_chunk(reads_job* J, uint64_t c) {
-    rng_t r;
+    rng_t r, rl;
     rng_seed(&r, J->seed, 3, c);
+    rng_seed(&rl, J->seed, 4, c);  /* read lengths: their own stream, the same in both passes */
     const uint64_t r0 = c * READS_PER_CHUNK;
     const uint64_t r1 = r0 + READS_PER_CHUNK < J->n_reads ? r0 + READS_PER_CHUNK : J->n_reads;
     if (J->pass == 0) {
         uint64_t bytes = 0;
         for (uint64_t i = r0; i < r1; ++i) {
-            const uint64_t L = read_len_of(&r, J);
-            (void)rng_next(&r); (void)rng_next(&r);
+            const uint64_t L = read_len_of(&rl, J);
             bytes += 15 + 2 * L + 4; /* "@r" + 12 digits + LF, seq, "\n+\n", qual, LF */
         }
         J->rec_off[c + 1] = bytes;
@@ -256,7 +256,7 @@ static void reads_chunk(reads_job* J, uint64_t c) {
     const uint32_t te = (uint32_t)(J->err * 4294967296.0);
     const uint32_t tn = (uint32_t)(J->n_rate * 4294967296.0);
     for (uint64_t i = r0; i < r1; ++i) {
-        const uint64_t L = read_len_of(&r, J);
+        const uint64_t L = read_len_of(&rl, J);
         const uint64_t pos = (rng_next(&r) >> 11) % (J->glen - L + 1);
         const int rc = (int)(rng_next(&r) & 1);
         *o++ = '@'; *o++ = 'r';
