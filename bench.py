@@ -234,8 +234,9 @@ def batched_vs_plain(ctx, n_samples: int, scale: float):
         lo, hi = int(off[i]), int(off[i + 1])
         b = T.Result(kb[lo:hi].reshape(-1, 1).copy(), cb[lo:hi].copy(), {}, 31).sorted()
         exact &= np.array_equal(a.keys, b.keys) and np.array_equal(a.counts, b.counts)
-    return {"workload": f"{len(seqs)} samples, genomes log-uniform {10_000 * scale / 1e3:g} kbp - "
-                        f"{50e6 * scale / 1e3:g} kbp, 150 bp reads at 5-50x, 0.3-1% errors, k=31 m=21",
+    return {"workload": f"{len(seqs)} samples, genome sizes log-uniform 10 kbp - 50 Mbp scaled by {scale:g} "
+                        f"(so {max(1000, 10_000 * scale) / 1e3:g} kbp floor - {50e6 * scale / 1e3:g} kbp), "
+                        f"150 bp reads at 5-50x, 0.3-1% errors, k=31 m=21",
             "samples": len(seqs), "bases": bases,
             "plain_gbases_s": bases / t_plain / 1e9, "batched_gbases_s": bases / t_batch / 1e9,
             "speedup": t_plain / t_batch, "plain_s": t_plain, "batched_s": t_batch,

@@ -164,6 +164,23 @@ struct FallbackParams {
     uint32_t* fail;
 };
 
+// Dynamic shared-memory cap of a kernel: the device's opt-in shared memory per
+// block minus the kernel's static shared memory. It is a cap, not a
+// reservation; every launch, from every host thread, sets this same value, so
+// one thread's launch never finds the cap lowered by another's.
+template <typename Kernel>
+inline cudaError_t set_smem_cap(Kernel kernel, size_t need) {
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes a{};
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, kernel);
+    if (e != cudaSuccess) return e;
+    const size_t cap = (size_t)optin > a.sharedSizeBytes ? (size_t)optin - a.sharedSizeBytes : 0;
+    if (need > cap) return cudaErrorInvalidValue;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap);
+}
+
 // ---------------------------------------------------------------- bit helpers
 __device__ __forceinline__ uint64_t rol64(uint64_t x, int s) {
     s &= 63;

@@ -857,7 +857,7 @@ cudaError_t launch_pack(const uint8_t* seq, uint64_t n, uint32_t* packed, uint32
 
 template <int NT>
 static cudaError_t launch_cut_seq(const CutParams& P, const HashTables* gT, size_t sm, cudaStream_t st) {
-    const cudaError_t e = cudaFuncSetAttribute(k_cut_seq<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    const cudaError_t e = set_smem_cap(k_cut_seq<NT>, sm);
     if (e != cudaSuccess) return e;
     k_cut_seq<NT><<<P.n_cta, NT, sm, st>>>(P, gT);
     return cudaGetLastError();
@@ -866,7 +866,7 @@ static cudaError_t launch_cut_seq(const CutParams& P, const HashTables* gT, size
 cudaError_t launch_cut(const CutParams& P, const HashTables* gT, bool exp, cudaStream_t st) {
     const size_t sm = cut_smem_bytes(P.w, P.k, 1u << P.p1_bits, exp);
     if (exp) {
-        const cudaError_t e = cudaFuncSetAttribute(k_cut<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        const cudaError_t e = set_smem_cap(k_cut<true>, sm);
         if (e != cudaSuccess) return e;
         k_cut<true><<<P.n_cta, CUT_THREADS, sm, st>>>(P, gT);
         return cudaGetLastError();

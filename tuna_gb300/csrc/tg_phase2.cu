@@ -874,9 +874,9 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
     Q.smem_slots = slots;
     const size_t sm = count_smem_bytes(W, slots);
     if (W == 1)
-        P2_CK(cudaFuncSetAttribute(k_count<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm), "smem");
+        P2_CK(set_smem_cap(k_count<1>, sm), "smem");
     else
-        P2_CK(cudaFuncSetAttribute(k_count<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm), "smem");
+        P2_CK(set_smem_cap(k_count<2>, sm), "smem");
     unsigned long long h[P2C_COUNT];
     // the groups of the first pass: their number is known once k_plan has run
     P2_CK(cudaMemcpyAsync(h, R.ctr, sizeof h, cudaMemcpyDeviceToHost, st), "d2h");
