@@ -9,9 +9,10 @@ benchmark set. Inputs (3.1 GB) are larger than L2, so no flush is needed.
 
   value   Gbases/s with the input already resident in HBM: k_pack -> k_cut ->
           scans -> k_scatter -> k_count, results left on the device
-  e2e     the same through the public C ABI (tg_count_seq) with pinned host
-          buffers: H2D of the input, both phases, D2H of every counted
-          (k-mer, count) pair
+  e2e     the same through the public C ABI from the FASTA file's bytes
+          (tg_count_fastx) with pinned host buffers: H2D of the FASTA, lexing
+          on the device, both phases, D2H of every counted (k-mer, count) pair;
+          e2e_stream: the same from the parsed stream (tg_count_seq)
   roofline  the dominant kernel's algorithmic bytes / its CUDA-event time
   cpu_baseline  the CPU oracle (a port of the reference path) on a bounded
           sample of the same workload, all host cores
@@ -121,17 +122,19 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ workload
-def workload(scale: float):
-    """Sequence stream of the synthetic assembly (contigs separated by LF) and
-    the number of sequence bases. The stream is exactly what the reference's
-    FASTA parser hands to Phase 1 for the 60-column FASTA of these contigs."""
+def workload(scale: float, want_fasta: bool = True):
+    """Sequence stream of the synthetic assembly (contigs separated by LF), the
+    number of sequence bases, the contig lengths and the bytes of its 60-column
+    FASTA file. The stream is exactly what the reference's FASTA parser hands
+    to Phase 1 for that file."""
     import numpy as np
     from tuna_gb300 import synth
     g, lens = synth.repetitive_genome(scale=scale)
+    fa = synth.fasta(g, lens) if want_fasta else None
     ends = np.cumsum(lens.astype(np.int64))
     stream = np.insert(g, ends[:-1], np.uint8(10))
     stream = np.append(stream, np.uint8(10))
-    return stream, int(g.size), [int(x) for x in lens]
+    return stream, int(g.size), [int(x) for x in lens], fa
 
 
 def cpu_sample(scale_shard_mbp: float, threads: int):
@@ -330,7 +333,7 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    stream_h, bases, lens = workload(args.scale)
+    stream_h, bases, lens, fasta_h = workload(args.scale, want_fasta=not args.no_e2e)
     dev = torch.from_numpy(stream_h).to(f"cuda:{local}")
     ctx = T.Context(local)
     ext = torch.cuda.ExternalStream(ctx.stream_ptr, device=f"cuda:{local}")
@@ -412,30 +415,58 @@ def main():
         nout = ctypes.c_uint64()
         sts = T._Stats()
 
-        def e2e_step():
-            rc = L.tg_count_seq(ctx.h, ctypes.byref(o), ctypes.c_void_p(h_in.data_ptr()), h_in.numel(),
-                                ctypes.c_void_p(h_keys.data_ptr()), ctypes.c_void_p(h_cnt.data_ptr()),
-                                n_out_cap, ctypes.byref(nout), ctypes.byref(sts))
+        def e2e_step(fn, h):
+            rc = fn(ctx.h, ctypes.byref(o), ctypes.c_void_p(h.data_ptr()), h.numel(),
+                    ctypes.c_void_p(h_keys.data_ptr()), ctypes.c_void_p(h_cnt.data_ptr()),
+                    n_out_cap, ctypes.byref(nout), ctypes.byref(sts))
             ctx.check(rc)
 
-        e2e_step()  # warm
-        barrier()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            e2e_step()
-            launches += int(sts.gpu_launches)
-        torch.cuda.synchronize()
-        t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps)
-        e2e = {"value": bases * world / t_e2e / 1e9, "unit": UNIT, "ms_per_step": t_e2e * 1e3,
-               "h2d_bytes_per_step": int(h_in.numel()), "d2h_bytes_per_step": int(nout.value) * (8 * W + 4),
-               "api": "tg_count_seq (include/tuna_gpu.h), pinned host buffers",
-               "excludes": "FASTA parsing on the host (the stream is the parsed FASTA)"}
+        def timed(fn, h):
+            nonlocal launches
+            e2e_step(fn, h)  # warm
+            barrier()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            parts = {"h2d_ms": 0.0, "lex_ms": 0.0, "pack_ms": 0.0, "phase1_ms": 0.0, "phase2_ms": 0.0, "d2h_ms": 0.0}
+            for _ in range(args.steps):
+                e2e_step(fn, h)
+                launches += int(sts.gpu_launches)
+                for k2 in parts:
+                    parts[k2] += getattr(sts, k2) / args.steps
+            torch.cuda.synchronize()
+            return max_over_ranks((time.perf_counter() - t0) / args.steps), parts
+
+        # the host link alone: one event-timed H2D of the same pinned buffer
+        d_tmp = torch.empty(h_in.numel(), dtype=torch.uint8, device=f"cuda:{local}")
+        c0 = torch.cuda.Event(enable_timing=True)
+        c1 = torch.cuda.Event(enable_timing=True)
+        c0.record()
+        d_tmp.copy_(h_in, non_blocking=True)
+        c1.record()
+        c1.synchronize()
+        link_h2d_gbs = h_in.numel() / (c0.elapsed_time(c1) / 1e3) / 1e9
+        del d_tmp
+        t_str, parts_str = timed(L.tg_count_seq, h_in)
+        e2e_stream = {"value": bases * world / t_str / 1e9, "unit": UNIT, "ms_per_step": t_str * 1e3,
+                      "h2d_bytes_per_step": int(h_in.numel()), "d2h_bytes_per_step": int(nout.value) * (8 * W + 4),
+                      "api": "tg_count_seq (include/tuna_gpu.h), pinned host buffers, input the parsed stream",
+                      "parts_ms": parts_str}
         # parity on the full run, size-independent: every k-mer counted once
         cnt = h_cnt[: int(nout.value)].numpy().view(np.uint32)
         sum_counts = int(cnt.astype(np.uint64).sum())
         parity_full = {"sum_counts": sum_counts, "kmers": int(st["kmers"]), "ok": sum_counts == int(st["kmers"])}
-        del h_in, h_keys, h_cnt
+        del h_in
+        h_fa = torch.from_numpy(fasta_h).pin_memory()
+        t_e2e, parts_fx = timed(L.tg_count_fastx, h_fa)
+        e2e = {"value": bases * world / t_e2e / 1e9, "unit": UNIT, "ms_per_step": t_e2e * 1e3,
+               "h2d_bytes_per_step": int(h_fa.numel()), "d2h_bytes_per_step": int(nout.value) * (8 * W + 4),
+               "api": "tg_count_fastx (include/tuna_gpu.h): 60-column FASTA bytes in pinned host memory, "
+                      "lexed on the device; pairs back in pinned host memory",
+               "parts_ms": parts_fx, "link_h2d_gbs": link_h2d_gbs, "stream": e2e_stream}
+        cnt = h_cnt[: int(nout.value)].numpy().view(np.uint32)
+        parity_full["fastx_sum_counts"] = int(cnt.astype(np.uint64).sum())
+        parity_full["ok"] = parity_full["ok"] and parity_full["fastx_sum_counts"] == int(st["kmers"])
+        del h_fa, h_keys, h_cnt
     else:
         parity_full = None
 

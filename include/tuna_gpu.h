@@ -104,6 +104,9 @@ typedef struct {
     double phase2_count_ms;   /* part of phase2_ms: the shared-memory counting kernel(s) */
     double phase2_keys_ms;    /* part of phase2_ms: bin histogram, group plan, key array */
     uint64_t groups;          /* phase-2 groups (runs of minimizer bins counted in one table) */
+    double lex_ms;            /* device time: FASTA/FASTQ lexing of the feeds */
+    uint64_t fastx_bytes;     /* FASTA/FASTQ bytes fed (before lexing) */
+    uint64_t host_parsed_bytes; /* of those, bytes parsed on the host (see tg_job_feed_fastx) */
 } tg_stats;
 
 /* Output formats of tg_job_drain. */
@@ -135,10 +138,19 @@ tg_status tg_job_feed_seq(tg_job* job, const uint8_t* seq, size_t len);
 /* Same, already in device memory on the context's device; the buffer must stay
  * valid and unchanged until tg_job_run returns. No copy is made. */
 tg_status tg_job_feed_seq_device(tg_job* job, const uint8_t* dseq, size_t len);
-/* FASTA/FASTQ bytes (FASTQ iff the first byte is '@'), parsed on the host with
- * the reference's rules. An empty buffer fails with TG_ERR_PARSE. */
+/* FASTA/FASTQ bytes (FASTQ iff the first byte is '@'): copied to the device
+ * and lexed there with the rules of the reference's parser
+ * (include/helicase_cpp/parser_fasta.hpp:233-316, parser_fastq.hpp:112-285).
+ * One case of malformed FASTQ, where the reference's 64-byte block walk departs
+ * from line counting (an empty header line ending at file offset 63 mod 64),
+ * is detected on the device and parsed on the host instead
+ * (tg_stats.host_parsed_bytes). An empty buffer fails with TG_ERR_PARSE. */
 tg_status tg_job_feed_fastx(tg_job* job, const uint8_t* data, size_t len);
-/* A FASTA/FASTQ file, plain or gzip (by the ".gz" suffix). */
+/* The same for bytes already in device memory on the context's device (read
+ * during the call only). */
+tg_status tg_job_feed_fastx_device(tg_job* job, const uint8_t* ddata, size_t len);
+/* A FASTA/FASTQ file, plain or gzip (by the ".gz" suffix): read (and
+ * inflated) on the host, lexed on the device. */
 tg_status tg_job_feed_file(tg_job* job, const char* path);
 /* Phase 1 + Phase 2 on the device. Blocks until the counts are ready. */
 tg_status tg_job_run(tg_job* job);
@@ -183,6 +195,19 @@ tg_status tg_job_sample_offsets(tg_job* job, uint64_t* offsets);
 tg_status tg_count_seq(tg_ctx* ctx, const tg_job_opts* opts, const uint8_t* seq, size_t len,
                        uint64_t* keys, uint32_t* counts, uint64_t cap, uint64_t* n_out,
                        tg_stats* stats);
+/* The same from the bytes of a FASTA/FASTQ file in host memory (pinned for
+ * full-speed copies): H2D, lexing on the device, both phases, D2H. Replaces
+ * SeqSource + run_callback (src/seq_source.hpp:190-205, src/pipeline.hpp:273-330). */
+tg_status tg_count_fastx(tg_ctx* ctx, const tg_job_opts* opts, const uint8_t* data, size_t len,
+                         uint64_t* keys, uint32_t* counts, uint64_t cap, uint64_t* n_out,
+                         tg_stats* stats);
+/* FASTA/FASTQ bytes to the sequence stream on the device, copied back to out
+ * (capacity cap; *out_len receives the stream length, TG_ERR_ARG if it does not
+ * fit). The stream holds the reference parser's ACGT runs in order, separated
+ * by non-ACGT bytes. Needs a context with no active job. Replaces the
+ * helicase parser (include/helicase_cpp/) as a stand-alone step. */
+tg_status tg_fastx_to_stream(tg_ctx* ctx, const uint8_t* data, size_t len, uint8_t* out, size_t cap,
+                             size_t* out_len);
 /* The same for n_samples host sequence streams counted as separate samples in
  * one job: the pairs come back sample-major, sample i's being
  * [sample_offsets[i], sample_offsets[i+1]) (n_samples + 1 entries, may be NULL). */

@@ -59,7 +59,8 @@ class _Stats(ctypes.Structure):
                 ("phase1_cut_ms", ctypes.c_double), ("phase1_scatter_ms", ctypes.c_double),
                 ("record_bytes", ctypes.c_uint64), ("gpu_launches", ctypes.c_uint64),
                 ("phase2_count_ms", ctypes.c_double), ("phase2_keys_ms", ctypes.c_double),
-                ("groups", ctypes.c_uint64)]
+                ("groups", ctypes.c_uint64), ("lex_ms", ctypes.c_double), ("fastx_bytes", ctypes.c_uint64),
+                ("host_parsed_bytes", ctypes.c_uint64)]
 
     def as_dict(self) -> Dict[str, float]:
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -77,7 +78,8 @@ ABI_SYMBOLS = ["tg_ctx_create", "tg_ctx_destroy", "tg_last_error", "tg_ctx_strea
                "tg_job_feed_file", "tg_job_run", "tg_job_stats", "tg_job_result_size", "tg_job_key_words",
                "tg_job_result_copy", "tg_job_drain", "tg_job_write", "tg_job_export_partitions", "tg_job_end",
                "tg_count_seq", "tg_count_seq_device_noalloc", "tg_job_next_sample", "tg_job_sample_count",
-               "tg_job_sample_offsets", "tg_count_batch"]
+               "tg_job_sample_offsets", "tg_count_batch", "tg_job_feed_fastx_device", "tg_count_fastx",
+               "tg_fastx_to_stream"]
 
 
 def library(build_if_missing: bool = True) -> ctypes.CDLL:
@@ -105,6 +107,10 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
     L.tg_job_feed_seq_device.argtypes = [vp, vp, sz]
     L.tg_job_feed_fastx.argtypes = [vp, vp, sz]
     L.tg_job_feed_file.argtypes = [vp, ctypes.c_char_p]
+    L.tg_job_feed_fastx_device.argtypes = [vp, vp, sz]
+    L.tg_count_fastx.argtypes = [vp, ctypes.POINTER(_JobOpts), vp, sz, vp, vp, u64, ctypes.POINTER(u64),
+                                 ctypes.POINTER(_Stats)]
+    L.tg_fastx_to_stream.argtypes = [vp, vp, sz, vp, sz, ctypes.POINTER(sz)]
     L.tg_job_run.argtypes = [vp]
     L.tg_job_stats.argtypes = [vp, ctypes.POINTER(_Stats)]
     L.tg_job_result_size.argtypes = [vp]
@@ -130,7 +136,8 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
     for fn in ("tg_ctx_create", "tg_ctx_destroy", "tg_job_begin", "tg_job_feed_seq", "tg_job_feed_seq_device",
                "tg_job_feed_fastx", "tg_job_feed_file", "tg_job_run", "tg_job_stats", "tg_job_result_copy",
                "tg_job_drain", "tg_job_write", "tg_job_export_partitions", "tg_job_end", "tg_count_seq",
-               "tg_job_next_sample", "tg_job_sample_offsets", "tg_count_batch"):
+               "tg_job_next_sample", "tg_job_sample_offsets", "tg_count_batch", "tg_job_feed_fastx_device",
+               "tg_count_fastx", "tg_fastx_to_stream"):
         getattr(L, fn).restype = i32
     _lib = L
     return L
@@ -240,11 +247,23 @@ class Context:
     def _opts(self, k, m, n_parts, ci, cx, gpu_parts) -> _JobOpts:
         return _JobOpts(k, m, n_parts, ci, min(cx, _U64_MAX), gpu_parts, 0)
 
+    def lex(self, data) -> bytes:
+        """FASTA/FASTQ bytes to the sequence stream, lexed on the device
+        (tg_fastx_to_stream)."""
+        a = np.ascontiguousarray(np.frombuffer(data, dtype=np.uint8) if isinstance(data, (bytes, bytearray))
+                                 else data, dtype=np.uint8)
+        out = np.empty(max(1, a.size + 1), dtype=np.uint8)
+        n = ctypes.c_size_t()
+        self.check(self._L.tg_fastx_to_stream(self.h, a.ctypes.data if a.size else None, a.size, out.ctypes.data,
+                                              out.size, ctypes.byref(n)))
+        return out[: n.value].tobytes()
+
     def run(self, k: int, m: int, *, seq=None, dev_seq=None, dev_len: int = 0, fastx=None, files=(),
-            samples=None, n_parts: int = 16, ci: int = 1, cx: int = _U64_MAX, gpu_parts: int = 0,
+            dev_fastx=None, samples=None, n_parts: int = 16, ci: int = 1, cx: int = _U64_MAX, gpu_parts: int = 0,
             export: bool = False, want_results: bool = True):
         """Run one job. seq: host stream (bytes / uint8 array); dev_seq: device
-        pointer (int) of dev_len bytes; fastx: FASTA/FASTQ bytes; files: paths;
+        pointer (int) of dev_len bytes; fastx: FASTA/FASTQ bytes; dev_fastx: device
+        pointer of dev_len FASTA/FASTQ bytes; files: paths;
         samples: host streams counted as separate samples of the job (the
         Result then carries the sample of each pair).
         Returns (Result, partitions or None)."""
@@ -265,6 +284,8 @@ class Context:
                 self.check(L.tg_job_feed_seq(j, a.ctypes.data if a.size else None, a.size))
             if dev_seq is not None:
                 self.check(L.tg_job_feed_seq_device(j, ctypes.c_void_p(dev_seq), dev_len))
+            if dev_fastx is not None:
+                self.check(L.tg_job_feed_fastx_device(j, ctypes.c_void_p(dev_fastx), dev_len))
             if fastx is not None:
                 a = np.frombuffer(fastx, dtype=np.uint8) if isinstance(fastx, (bytes, bytearray)) else fastx
                 a = np.ascontiguousarray(a, dtype=np.uint8)

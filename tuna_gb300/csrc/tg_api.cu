@@ -101,11 +101,12 @@ struct tg_ctx {
     unsigned host_threads = 1;
     std::string err;
     DevBuf seq, packed, valid, desc, xdesc, hist, scratch, okeys, ocnt, osamp, samp, okeys2, ocnt2, osoff,
-        misc, fbtab, tables;
+        misc, fbtab, tables, raw, lexs;
     cudaEvent_t ev[12] = {};
     // results copied to the host while counting runs (tg_count_seq)
     cudaStream_t st_copy = nullptr;
-    unsigned long long* wave_out = nullptr;  // pinned host, 16 entries
+    unsigned long long* wave_out = nullptr;  // mapped pinned host, OVERLAP_WORDS entries
+    unsigned long long* wave_out_dev = nullptr;
     cudaEvent_t wave_ev[16] = {};
     tg_job* active = nullptr;
     int prepared_m = -1;
@@ -150,6 +151,7 @@ struct tg_job {
     const P2Overlap* overlap = nullptr;
     // samples: sample i starts at stream position sample_start[i]
     std::vector<unsigned long long> sample_start{0};
+    int lex_launches = 0;  // lexer kernels of the feeds
     const uint8_t* seq_ptr() const { return ext ? ext : ctx->seq.as<uint8_t>(); }
 };
 
@@ -188,7 +190,9 @@ tg_status tg_ctx_create(const tg_ctx_opts* opts, tg_ctx** out) {
     ctx->smem_optin = (size_t)optin;
     for (int i = 0; i < 12 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->ev[i]);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->st_copy, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaHostAlloc(&ctx->wave_out, 16 * sizeof(unsigned long long), cudaHostAllocDefault);
+    if (e == cudaSuccess)
+        e = cudaHostAlloc(&ctx->wave_out, OVERLAP_WORDS * sizeof(unsigned long long), cudaHostAllocMapped);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer(reinterpret_cast<void**>(&ctx->wave_out_dev), ctx->wave_out, 0);
     for (int i = 0; i < 16 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&ctx->wave_ev[i], cudaEventDisableTiming);
     if (e != cudaSuccess) {
         delete ctx;
@@ -204,7 +208,8 @@ tg_status tg_ctx_destroy(tg_ctx* ctx) {
     if (ctx->st) cudaStreamSynchronize(ctx->st);
     DevBuf* bufs[] = {&ctx->seq, &ctx->packed, &ctx->valid, &ctx->desc, &ctx->xdesc, &ctx->hist,
                       &ctx->scratch,
-                      &ctx->okeys, &ctx->ocnt, &ctx->osamp, &ctx->samp, &ctx->okeys2, &ctx->ocnt2, &ctx->osoff, &ctx->misc, &ctx->fbtab, &ctx->tables};
+                      &ctx->okeys, &ctx->ocnt, &ctx->osamp, &ctx->samp, &ctx->okeys2, &ctx->ocnt2, &ctx->osoff, &ctx->misc, &ctx->fbtab, &ctx->tables,
+                      &ctx->raw, &ctx->lexs};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
     for (auto& e : ctx->ev)
@@ -250,19 +255,18 @@ tg_status tg_job_begin(tg_ctx* ctx, const tg_job_opts* opts, tg_job** out) {
     return TG_OK;
 }
 
-static tg_status append_stream(tg_job* j, const uint8_t* src, size_t len, cudaMemcpyKind kind) {
+// Room for `extra` more stream bytes in ctx->seq (a device feed used in place
+// is moved into it first); *at receives the device address of position j->n.
+static tg_status stream_reserve(tg_job* j, size_t extra, uint8_t** at) {
     tg_ctx* ctx = j->ctx;
-    if (j->ran) return ctx->fail(TG_ERR_STATE, "feed after run");
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
-    // a previous single device feed used in place is moved into the context buffer
     if (j->ext) {
-        const size_t need = j->n + 1;
-        CK(ctx->ensure(ctx->seq, need + len + 1), "alloc seq");
+        CK(ctx->ensure(ctx->seq, j->n + extra + 2), "alloc seq");
         CK(cudaMemcpyAsync(ctx->seq.p, j->ext, j->n, cudaMemcpyDeviceToDevice, ctx->st), "copy seq");
         j->ext = nullptr;
         j->used_ctx_seq = true;
     }
-    const size_t need = j->n + len + 1;
+    const size_t need = j->n + extra + 1;
     if (need > ctx->seq.cap) {
         DevBuf nb;
         CK(cudaMalloc(&nb.p, std::max(need, 2 * ctx->seq.cap)), "alloc seq");
@@ -272,16 +276,92 @@ static tg_status append_stream(tg_job* j, const uint8_t* src, size_t len, cudaMe
         if (ctx->seq.p) cudaFree(ctx->seq.p);
         ctx->seq = nb;
     }
-    uint8_t* d = ctx->seq.as<uint8_t>();
+    *at = ctx->seq.as<uint8_t>() + j->n;
+    return TG_OK;
+}
+
+static tg_status append_stream(tg_job* j, const uint8_t* src, size_t len, cudaMemcpyKind kind) {
+    tg_ctx* ctx = j->ctx;
+    if (j->ran) return ctx->fail(TG_ERR_STATE, "feed after run");
+    uint8_t* d = nullptr;
+    const tg_status s = stream_reserve(j, len + 1, &d);
+    if (s != TG_OK) return s;
     const double t0 = now_ms();
-    if (len) CK(cudaMemcpyAsync(d + j->n, src, len, kind, ctx->st), "copy input");
-    CK(cudaMemsetAsync(d + j->n + len, '\n', 1, ctx->st), "separator");
+    if (len) CK(cudaMemcpyAsync(d, src, len, kind, ctx->st), "copy input");
+    CK(cudaMemsetAsync(d + len, '\n', 1, ctx->st), "separator");
     CK(cudaStreamSynchronize(ctx->st), "copy input");
     if (kind == cudaMemcpyHostToDevice) j->st.h2d_ms += now_ms() - t0;
     j->n += len + 1;
     j->used_ctx_seq = true;
     j->st.input_bytes += len;
     return TG_OK;
+}
+
+// FASTA/FASTQ bytes in device memory (16-byte aligned) lexed on the device
+// onto the end of the stream. host_raw, when given, is the same bytes in host
+// memory. A FASTQ file the device lexer flags (an empty header line at file
+// offset 63 mod 64, where the reference's block walk departs from line
+// counting) is parsed by the host parser instead.
+static tg_status lex_append(tg_job* j, const uint8_t* draw, size_t len, const uint8_t* host_raw) {
+    tg_ctx* ctx = j->ctx;
+    if (j->ran) return ctx->fail(TG_ERR_STATE, "feed after run");
+    if (len == 0) return ctx->fail(TG_ERR_PARSE, "Empty file");
+    uint8_t* at = nullptr;
+    tg_status s = stream_reserve(j, len + 1, &at);
+    if (s != TG_OK) return s;
+    uint8_t first = 0;
+    if (host_raw) {
+        first = host_raw[0];
+    } else {
+        CK(cudaMemcpyAsync(&first, draw, 1, cudaMemcpyDeviceToHost, ctx->st), "d2h");
+        CK(cudaStreamSynchronize(ctx->st), "d2h");
+    }
+    const bool fastq = first == '@';
+    CK(ctx->ensure(ctx->lexs, lex_scratch_bytes(len)), "alloc lexer scratch");
+    LexTotals* dt = nullptr;
+    int launches = 0;
+    CK(cudaEventRecord(ctx->ev[10], ctx->st), "event");
+    CK(launch_lex(draw, len, fastq, at, ctx->lexs.p, ctx->n_sm, ctx->st, &dt, &launches), "k_lex");
+    CK(cudaEventRecord(ctx->ev[11], ctx->st), "event");
+    LexTotals t{};
+    CK(cudaMemcpyAsync(&t, dt, sizeof t, cudaMemcpyDeviceToHost, ctx->st), "d2h");
+    CK(cudaStreamSynchronize(ctx->st), "k_lex");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev[10], ctx->ev[11]);
+    j->st.lex_ms += ms;
+    j->st.fastx_bytes += len;
+    j->lex_launches += launches;
+    if (t.irregular) {
+        std::vector<uint8_t> hraw;
+        if (!host_raw) {
+            hraw.resize(len);
+            CK(cudaMemcpy(hraw.data(), draw, len, cudaMemcpyDeviceToHost), "d2h");
+            host_raw = hraw.data();
+        }
+        std::vector<uint8_t> st;
+        tgh::fastx_to_stream(host_raw, len, st);
+        j->st.host_parsed_bytes += len;
+        return append_stream(j, st.data(), st.size(), cudaMemcpyHostToDevice);
+    }
+    CK(cudaMemsetAsync(at + t.out, '\n', 1, ctx->st), "separator");
+    j->n += t.out + 1;
+    j->used_ctx_seq = true;
+    j->st.input_bytes += t.out;
+    return TG_OK;
+}
+
+// Host FASTA/FASTQ bytes: copied to the device, lexed there.
+static tg_status lex_append_host(tg_job* j, const uint8_t* data, size_t len) {
+    tg_ctx* ctx = j->ctx;
+    if (j->ran) return ctx->fail(TG_ERR_STATE, "feed after run");
+    if (len == 0) return ctx->fail(TG_ERR_PARSE, "Empty file");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    CK(ctx->ensure(ctx->raw, len + 16), "alloc raw input");
+    const double t0 = now_ms();
+    CK(cudaMemcpyAsync(ctx->raw.p, data, len, cudaMemcpyHostToDevice, ctx->st), "copy input");
+    CK(cudaStreamSynchronize(ctx->st), "copy input");
+    j->st.h2d_ms += now_ms() - t0;
+    return lex_append(j, ctx->raw.as<uint8_t>(), len, data);
 }
 
 tg_status tg_job_feed_seq(tg_job* j, const uint8_t* seq, size_t len) {
@@ -317,10 +397,21 @@ uint32_t tg_job_sample_count(const tg_job* j) { return j ? (uint32_t)j->sample_s
 
 tg_status tg_job_feed_fastx(tg_job* j, const uint8_t* data, size_t len) {
     if (!j || (!data && len)) return TG_ERR_ARG;
-    if (len == 0) return j->ctx->fail(TG_ERR_PARSE, "Empty file");
-    std::vector<uint8_t> s;
-    tgh::fastx_to_stream(data, len, s);
-    return append_stream(j, s.data(), s.size(), cudaMemcpyHostToDevice);
+    return lex_append_host(j, data, len);
+}
+
+tg_status tg_job_feed_fastx_device(tg_job* j, const uint8_t* ddata, size_t len) {
+    if (!j || (!ddata && len)) return TG_ERR_ARG;
+    tg_ctx* ctx = j->ctx;
+    if (j->ran) return ctx->fail(TG_ERR_STATE, "feed after run");
+    if (len == 0) return ctx->fail(TG_ERR_PARSE, "Empty file");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if (reinterpret_cast<uintptr_t>(ddata) & 15u) {  // the lexer loads 16-byte words
+        CK(ctx->ensure(ctx->raw, len + 16), "alloc raw input");
+        CK(cudaMemcpyAsync(ctx->raw.p, ddata, len, cudaMemcpyDeviceToDevice, ctx->st), "copy input");
+        ddata = ctx->raw.as<uint8_t>();
+    }
+    return lex_append(j, ddata, len, nullptr);
 }
 
 tg_status tg_job_feed_file(tg_job* j, const char* path) {
@@ -331,11 +422,31 @@ tg_status tg_job_feed_file(tg_job* j, const char* path) {
         const bool empty = err.rfind("Empty file", 0) == 0;
         return j->ctx->fail(empty ? TG_ERR_PARSE : TG_ERR_IO, err);
     }
-    std::vector<uint8_t> s;
-    tgh::fastx_to_stream(raw.data(), raw.size(), s);
-    raw.clear();
-    raw.shrink_to_fit();
-    return append_stream(j, s.data(), s.size(), cudaMemcpyHostToDevice);
+    return lex_append_host(j, raw.data(), raw.size());
+}
+
+tg_status tg_fastx_to_stream(tg_ctx* ctx, const uint8_t* data, size_t len, uint8_t* out, size_t cap,
+                             size_t* out_len) {
+    if (!ctx || (!data && len) || !out_len) return TG_ERR_ARG;
+    *out_len = 0;
+    tg_job_opts o{};
+    o.k = 31;
+    o.m = 21;
+    tg_job* j = nullptr;
+    tg_status s = tg_job_begin(ctx, &o, &j);
+    if (s != TG_OK) return s;
+    s = tg_job_feed_fastx(j, data, len);
+    if (s == TG_OK) {
+        const size_t n = j->n ? j->n - 1 : 0;  // without the closing separator
+        *out_len = n;
+        if (n > cap) s = ctx->fail(TG_ERR_ARG, "stream buffer too small");
+        else if (n) {
+            cudaError_t e = cudaMemcpy(out, ctx->seq.p, n, cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) s = ctx->cuda_fail(e, "d2h");
+        }
+    }
+    tg_job_end(j);
+    return s;
 }
 
 // Phase 1 cut (optionally the export variant) over the current stream.
@@ -430,8 +541,7 @@ tg_status tg_job_run(tg_job* j) {
     }
     CK(ctx->ensure(ctx->misc, MISC_BYTES), "alloc misc");
     // ---- pack
-    uint64_t pw = (TG_PAD + n + CUT_SPAN + 2 * MAX_W + 640) / 16 + 16;
-    pw = (pw + 1) & ~uint64_t(1);
+    const uint64_t pw = packed_words_for(n);
     j->packed_words = pw;
     CK(ctx->ensure(ctx->packed, pw * 4), "alloc packed");
     CK(ctx->ensure(ctx->valid, (pw / 2) * 4 + 64), "alloc valid");
@@ -549,7 +659,7 @@ tg_status tg_job_run(tg_job* j) {
     cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[8]); S.phase2_ms = ms;
     cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]); S.phase2_keys_ms = ms;
     cudaEventElapsedTime(&ms, ctx->ev[7], ctx->ev[8]); S.phase2_count_ms = ms;
-    S.gpu_launches = (uint64_t)launches;
+    S.gpu_launches = (uint64_t)(launches + j->lex_launches);
     return TG_OK;
 }
 
@@ -719,7 +829,7 @@ tg_status tg_job_end(tg_job* j) {
 // next waves count, wait for the copies.
 static tg_status count_host(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_samples, const uint8_t* const* seqs,
                             const size_t* lens, uint64_t* keys, uint32_t* counts, uint64_t* sample_off, uint64_t cap,
-                            uint64_t* n_out, tg_stats* stats) {
+                            uint64_t* n_out, tg_stats* stats, bool fastx = false) {
     if (!ctx || !opts || !n_out || (n_samples && (!seqs || !lens))) return TG_ERR_ARG;
     *n_out = 0;
     if (n_samples > TG_MAX_SAMPLES) return ctx->fail(TG_ERR_ARG, "too many samples in one job");
@@ -732,7 +842,9 @@ static tg_status count_host(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_sam
         if (!seqs[i] && lens[i]) s = TG_ERR_ARG;
         total += lens[i] + 1;
     }
-    if (s == TG_OK && total) {
+    if (s == TG_OK && fastx) {
+        s = n_samples == 1 ? lex_append_host(j, seqs[0], lens[0]) : TG_ERR_ARG;
+    } else if (s == TG_OK && total) {
         const double t0 = now_ms();
         cudaError_t e = cudaSetDevice(ctx->device);
         if (e == cudaSuccess) e = ctx->ensure(ctx->seq, total + 1);
@@ -753,6 +865,7 @@ static tg_status count_host(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_sam
     P2Overlap ov;
     ov.waves = 8;
     ov.wave_out = ctx->wave_out;
+    ov.wave_out_dev = ctx->wave_out_dev;
     ov.wave_ev = ctx->wave_ev;
     double d2h_issue_ms = 0;
     const int W = j->W;
@@ -799,6 +912,12 @@ tg_status tg_count_seq(tg_ctx* ctx, const tg_job_opts* opts, const uint8_t* seq,
                        uint32_t* counts, uint64_t cap, uint64_t* n_out, tg_stats* stats) {
     if (!seq && len) return TG_ERR_ARG;
     return count_host(ctx, opts, 1, &seq, &len, keys, counts, nullptr, cap, n_out, stats);
+}
+
+tg_status tg_count_fastx(tg_ctx* ctx, const tg_job_opts* opts, const uint8_t* data, size_t len, uint64_t* keys,
+                         uint32_t* counts, uint64_t cap, uint64_t* n_out, tg_stats* stats) {
+    if (!data && len) return TG_ERR_ARG;
+    return count_host(ctx, opts, 1, &data, &len, keys, counts, nullptr, cap, n_out, stats, true);
 }
 
 tg_status tg_count_batch(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_samples, const uint8_t* const* seqs,

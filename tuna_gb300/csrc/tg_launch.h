@@ -15,11 +15,25 @@ namespace tg {
 size_t cut_smem_bytes(int w, int k, uint32_t p1, bool exp);
 uint64_t cut_tile(int w, bool exp);                 // k-mer start positions per tile of a cut CTA
 uint32_t cut_ctas_per_sm(int w, int k, uint32_t p1, bool exp);
+// Packed words (a multiple of 4) for a stream of n bytes, padding included.
+uint64_t packed_words_for(uint64_t n);
 cudaError_t launch_pack(const uint8_t* seq, uint64_t n, uint32_t* packed, uint32_t* valid, uint64_t n_words,
                         unsigned long long* n_bases, cudaStream_t st);
 cudaError_t launch_cut(const CutParams& P, const HashTables* gT, bool exp, cudaStream_t st);
 cudaError_t launch_scan(const uint32_t* in, uint64_t n, unsigned long long* out, unsigned long long* sums,
                         unsigned long long* total, cudaStream_t st, int* launches);
+// FASTA/FASTQ lexing on the device (tg_lex.cu). raw must be 16-byte aligned;
+// out receives at most len bytes. Totals are written to device memory (*dtot,
+// inside scratch) and are valid once the stream reaches them.
+struct LexTotals {
+    unsigned long long out;        // stream bytes written
+    unsigned long long drop_from;  // FASTQ: bytes from here on were not emitted (end-of-file rule)
+    uint32_t final_state;          // automaton state at the end of the file
+    uint32_t irregular;            // FASTQ: an empty header line at offset 63 mod 64 (parse on the host)
+};
+size_t lex_scratch_bytes(uint64_t len);
+cudaError_t launch_lex(const uint8_t* raw, uint64_t len, bool fastq, uint8_t* out, void* scratch, int n_sm,
+                       cudaStream_t st, LexTotals** dtot, int* launches);
 size_t key_bytes(int W);
 uint32_t count_slots(int W);
 
@@ -72,10 +86,16 @@ struct P2Output {
 // `waves` u64; wave_ev: `waves` events. Empty on_range: one launch, no calls.
 struct P2Overlap {
     uint32_t waves = 1;
-    unsigned long long* wave_out = nullptr;
+    unsigned long long* wave_out = nullptr;      // host address of mapped pinned memory, OVERLAP_WORDS u64
+    unsigned long long* wave_out_dev = nullptr;  // its device address
     cudaEvent_t* wave_ev = nullptr;
     std::function<tg_status(uint64_t lo, uint64_t hi)> on_range;
 };
+// wave_out layout: [0, 16) output totals after each wave, [16, 64) counter reads.
+// Counters are read back by a one-warp kernel storing into this mapped memory,
+// not by cudaMemcpyAsync: a copy-engine read would queue behind the result
+// copies already issued on the copy stream.
+constexpr uint32_t OVERLAP_WORDS = 64;
 // Device scratch one run needs (key array included).
 size_t phase2_scratch_bytes(const P2Input& in);
 // Runs phase 2 on `st` and waits for it. fallback_table(bytes) returns device

@@ -119,8 +119,7 @@ extern "C" tg_status tg_count_seq_device_noalloc(const tg_job_opts* opts, const 
     // ---- fixed pieces
     HashTables* tables = cv.take<HashTables>(1);
     unsigned long long* misc = cv.take<unsigned long long>(32);  // counters, see below
-    uint64_t pw = (TG_PAD + n + CUT_SPAN + 2 * MAX_W + 640) / 16 + 16;
-    pw = (pw + 1) & ~uint64_t(1);
+    const uint64_t pw = packed_words_for(n);
     uint32_t* packed = cv.take<uint32_t>(pw);
     uint32_t* valid = cv.take<uint32_t>(pw / 2 + 16);
     // phase-1 layout: as tg_job_run, with room for one record per k-mer start

@@ -24,47 +24,76 @@
 namespace tg {
 
 // ---------------------------------------------------------------- packing
-// One thread per packed word (16 bases). Array base index a = global base + TG_PAD.
-__global__ void k_pack(const uint8_t* __restrict__ seq, uint64_t n, uint32_t* __restrict__ packed,
-                       uint32_t* __restrict__ valid, uint64_t n_words,
-                       unsigned long long* __restrict__ n_bases) {
-    const uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t code = 0, vbits = 0;
-    if (w < n_words) {
-        const int64_t g0 = (int64_t)(w * 16) - TG_PAD;
-        uint8_t b[16];
-        if (g0 >= 0 && (uint64_t)g0 + 16 <= n && ((reinterpret_cast<uintptr_t>(seq + g0) & 15) == 0)) {
-            const uint4 v = *reinterpret_cast<const uint4*>(seq + g0);
-            const uint32_t vv[4] = {v.x, v.y, v.z, v.w};
+// 2-bit kache codes (A0 C1 G2 T3, src/partition_hash.hpp:68-70) of every byte,
+// 16 bases per u32 MSB-first, and one validity bit per base (ACGTacgt). Array
+// base index a = stream position + TG_PAD. Grid-stride: a thread takes 64
+// bases (four packed words, two validity words) per step, four bytes at a time
+// with byte-wise SIMD compares; one atomic per CTA for the ACGT count.
+__device__ __forceinline__ void pack_word4(uint32_t x, uint32_t& code8, uint32_t& ok4) {
+    const uint32_t u = x & 0xDFDFDFDFu;  // upper case
+    const uint32_t ok = __vcmpeq4(u, 0x41414141u) | __vcmpeq4(u, 0x43434343u) | __vcmpeq4(u, 0x47474747u) |
+                        __vcmpeq4(u, 0x54545454u);
+    // code ((c >> 2) ^ (c >> 1)) & 3 per byte, 0 where the byte is not ACGT
+    const uint32_t t = (((x >> 2) ^ (x >> 1)) & 0x03030303u) & ok;
+    // byte i's code to bits 6-2i of the result (first base most significant)
+    code8 = (t * 0x40100401u) >> 24;
+    ok4 = ((ok & 0x01010101u) * 0x01020408u) >> 24;
+}
+
+__global__ void __launch_bounds__(256) k_pack(const uint8_t* __restrict__ seq, uint64_t n,
+                                              uint32_t* __restrict__ packed, uint32_t* __restrict__ valid,
+                                              uint64_t n_groups, unsigned long long* __restrict__ n_bases) {
+    __shared__ unsigned s_cnt;
+    if (threadIdx.x == 0) s_cnt = 0;
+    __syncthreads();
+    unsigned cnt = 0;
+    const bool aligned = (reinterpret_cast<uintptr_t>(seq) & 15u) == 0;
+    for (uint64_t gi = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; gi < n_groups;
+         gi += (uint64_t)gridDim.x * blockDim.x) {
+        const int64_t g0 = (int64_t)(gi * 64) - TG_PAD;
+        uint32_t x[16];
+        if (aligned && g0 >= 0 && (uint64_t)g0 + 64 <= n) {
+            const uint4* p = reinterpret_cast<const uint4*>(seq + g0);
 #pragma unroll
-            for (int i = 0; i < 16; ++i) b[i] = (uint8_t)(vv[i >> 2] >> (8 * (i & 3)));
+            for (int q = 0; q < 4; ++q) {
+                const uint4 v = __ldcs(p + q);
+                x[4 * q] = v.x;
+                x[4 * q + 1] = v.y;
+                x[4 * q + 2] = v.z;
+                x[4 * q + 3] = v.w;
+            }
         } else {
 #pragma unroll
-            for (int i = 0; i < 16; ++i) {
+            for (int q = 0; q < 16; ++q) x[q] = 0;
+#pragma unroll
+            for (int i = 0; i < 64; ++i) {
                 const int64_t g = g0 + i;
-                b[i] = (g >= 0 && (uint64_t)g < n) ? seq[g] : 0;
+                if (g >= 0 && (uint64_t)g < n) x[i >> 2] |= (uint32_t)seq[g] << (8 * (i & 3));
             }
         }
+        uint32_t pw[4], vw[2] = {0, 0};
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-            const uint32_t c = b[i];
-            // ACGTacgt test of include/helicase_cpp/simd.hpp:316: (c & 0xDF) == "A_C_T_G_"[c & 6]
-            const uint32_t want = (uint32_t)(0x0047005400430041ull >> (8 * (c & 6))) & 0xFFu;
-            const bool ok = (c & 0xDFu) == want;
-            const uint32_t kc = ok ? (((c >> 2) ^ (c >> 1)) & 3u) : 0u;
-            code |= kc << (30 - 2 * i);
-            vbits |= (ok ? 1u : 0u) << i;
+        for (int w = 0; w < 4; ++w) {
+            uint32_t word = 0, vb = 0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                uint32_t c8, o4;
+                pack_word4(x[4 * w + q], c8, o4);
+                word |= c8 << (24 - 8 * q);
+                vb |= o4 << (4 * q);
+            }
+            pw[w] = word;
+            vw[w >> 1] |= vb << (16 * (w & 1));
         }
-        packed[w] = code;
+        *reinterpret_cast<uint4*>(packed + 4 * gi) = make_uint4(pw[0], pw[1], pw[2], pw[3]);
+        *reinterpret_cast<uint2*>(valid + 2 * gi) = make_uint2(vw[0], vw[1]);
+        cnt += __popc(vw[0]) + __popc(vw[1]);
     }
-    // two consecutive words form one 32-bit validity word (lane pairs)
-    const uint32_t other = __shfl_down_sync(0xffffffffu, vbits, 1);
-    if (w < n_words && (w & 1) == 0) valid[w >> 1] = vbits | (other << 16);
-    // count of ACGT bases
-    unsigned cnt = __popc(vbits);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
-    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(n_bases, (unsigned long long)cnt);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&s_cnt, cnt);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_cnt) atomicAdd(n_bases, (unsigned long long)s_cnt);
 }
 
 // ---------------------------------------------------------------- block scans
@@ -848,11 +877,20 @@ uint32_t cut_ctas_per_sm(int w, int k, uint32_t p1, bool exp) {
 
 cudaError_t launch_pack(const uint8_t* seq, uint64_t n, uint32_t* packed, uint32_t* valid, uint64_t n_words,
                         unsigned long long* n_bases, cudaStream_t st) {
-    const uint64_t nw = (n_words + 1) & ~uint64_t(1);  // even: lane pairs share a validity word
+    // n_words is a multiple of 4 (packed_words_for): groups of 4 words
+    const uint64_t groups = n_words / 4;
+    int dev = 0, n_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
     const uint32_t threads = 256;
-    const uint64_t blocks = (nw + threads - 1) / threads;
-    k_pack<<<(unsigned)blocks, threads, 0, st>>>(seq, n, packed, valid, nw, n_bases);
+    const uint64_t blocks = std::min<uint64_t>((groups + threads - 1) / threads, (uint64_t)std::max(n_sm, 1) * 8);
+    k_pack<<<(unsigned)std::max<uint64_t>(blocks, 1), threads, 0, st>>>(seq, n, packed, valid, groups, n_bases);
     return cudaGetLastError();
+}
+
+uint64_t packed_words_for(uint64_t n) {
+    const uint64_t pw = (TG_PAD + n + CUT_SPAN + 2 * MAX_W + 640) / 16 + 16;
+    return (pw + 3) & ~uint64_t(3);
 }
 
 template <int NT>

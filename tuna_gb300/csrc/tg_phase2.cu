@@ -810,6 +810,36 @@ size_t phase2_scratch_bytes(const P2Input& in) {
         }                                                            \
     } while (0)
 
+// Small counter reads (see OVERLAP_WORDS): src[0, n) to the mapped host words
+// dst (device address), fenced for the host.
+__global__ void k_peek(const unsigned long long* __restrict__ a, uint32_t na, const unsigned long long* __restrict__ b,
+                       uint32_t nb, unsigned long long* dst) {
+    const uint32_t i = threadIdx.x;
+    if (i < na) dst[i] = a[i];
+    else if (i < na + nb) dst[i] = b[i - na];
+    __threadfence_system();
+}
+
+// Reads na counters at a and nb at b into out (host), then waits for the
+// stream. With mapped words (ov.wave_out_dev) a kernel stores them there;
+// otherwise cudaMemcpyAsync.
+static cudaError_t read_counters(const P2Overlap& ov, const unsigned long long* a, uint32_t na,
+                                 const unsigned long long* b, uint32_t nb, unsigned long long* out, cudaStream_t st) {
+    if (ov.wave_out && ov.wave_out_dev && na + nb <= OVERLAP_WORDS - 16) {
+        k_peek<<<1, 32, 0, st>>>(a, na, b, nb, ov.wave_out_dev + 16);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return e;
+        const volatile unsigned long long* w = ov.wave_out + 16;
+        for (uint32_t i = 0; i < na + nb; ++i) out[i] = w[i];
+        return cudaSuccess;
+    }
+    cudaError_t e = cudaMemcpyAsync(out, a, 8 * (size_t)na, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && nb) e = cudaMemcpyAsync(out + na, b, 8 * (size_t)nb, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e;
+}
+
 tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Output& out,
                      const std::function<void*(size_t)>& fallback_table, cudaStream_t st, cudaEvent_t ev_keys,
                      int* launches, std::string& err, const P2Overlap& ov) {
@@ -907,14 +937,15 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
             P2_CK(cudaGetLastError(), "k_count");
             ++*launches;
             if (nw > 1) {
-                P2_CK(cudaMemcpyAsync(ov.wave_out + wv, R.ctr + P2C_OUT, 8, cudaMemcpyDeviceToHost, st), "d2h");
+                if (ov.wave_out_dev) k_peek<<<1, 32, 0, st>>>(R.ctr + P2C_OUT, 1, nullptr, 0, ov.wave_out_dev + wv);
+                else P2_CK(cudaMemcpyAsync(ov.wave_out + wv, R.ctr + P2C_OUT, 8, cudaMemcpyDeviceToHost, st), "d2h");
                 P2_CK(cudaEventRecord(ov.wave_ev[wv], st), "event");
             }
         }
         if (nw > 1) {
             for (uint32_t wv = 0; wv < nw; ++wv) {
                 P2_CK(cudaEventSynchronize(ov.wave_ev[wv]), "wave");
-                const uint64_t hi = std::min<uint64_t>(ov.wave_out[wv], out.cap);
+                const uint64_t hi = std::min<uint64_t>(*(const volatile unsigned long long*)(ov.wave_out + wv), out.cap);
                 if (hi > done) {
                     const tg_status rs = ov.on_range(done, hi);
                     if (rs != TG_OK) { err = "result copy failed"; return rs; }
@@ -922,10 +953,10 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
                 }
             }
         }
-        unsigned long long nret = 0;
-        P2_CK(cudaMemcpyAsync(&nret, Q.n_retry, 8, cudaMemcpyDeviceToHost, st), "d2h");
-        P2_CK(cudaMemcpyAsync(h, R.ctr, sizeof h, cudaMemcpyDeviceToHost, st), "d2h");
-        P2_CK(cudaStreamSynchronize(st), "phase 2");
+        unsigned long long hr[P2C_COUNT + 1];
+        P2_CK(read_counters(ov, Q.n_retry, 1, R.ctr, P2C_COUNT, hr, st), "phase 2");
+        const unsigned long long nret = hr[0];
+        for (int c = 0; c < P2C_COUNT; ++c) h[c] = hr[c + 1];
         if (nret > L.retry_cap) { err = "too many groups to split"; return TG_ERR_TABLE; }
         if (nret == 0) break;
         const unsigned long long nl[2] = {0, nret};
@@ -976,8 +1007,7 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
             P2_CK(cudaStreamSynchronize(st), "fallback");
             if (failed) { err = "fallback table overflow"; return TG_ERR_TABLE; }
         }
-        P2_CK(cudaMemcpyAsync(h, R.ctr, sizeof h, cudaMemcpyDeviceToHost, st), "d2h");
-        P2_CK(cudaStreamSynchronize(st), "fallback");
+        P2_CK(read_counters(ov, R.ctr, P2C_COUNT, nullptr, 0, h, st), "fallback");
     }
     out.n_out = h[P2C_OUT];
     if (ov.on_range && std::min<uint64_t>(out.n_out, out.cap) > done) {
