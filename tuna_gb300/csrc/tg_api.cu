@@ -331,6 +331,7 @@ static tg_status lex_append(tg_job* j, const uint8_t* draw, size_t len, const ui
     j->st.lex_ms += ms;
     j->st.fastx_bytes += len;
     j->lex_launches += launches;
+    if (t.irregular & 2u) return ctx->fail(TG_ERR_DEVICE, "FASTA/FASTQ lexer: a staging copy did not complete");
     if (t.irregular) {
         std::vector<uint8_t> hraw;
         if (!host_raw) {

@@ -29,7 +29,8 @@ struct LexTotals {
     unsigned long long out;        // stream bytes written
     unsigned long long drop_from;  // FASTQ: bytes from here on were not emitted (end-of-file rule)
     uint32_t final_state;          // automaton state at the end of the file
-    uint32_t irregular;            // FASTQ: an empty header line at offset 63 mod 64 (parse on the host)
+    uint32_t irregular;            // bit 0: FASTQ with an empty header line at offset 63 mod 64 (parse
+                                   // on the host); bit 1: a staging wait timed out (device error)
 };
 size_t lex_scratch_bytes(uint64_t len);
 cudaError_t launch_lex(const uint8_t* raw, uint64_t len, bool fastq, uint8_t* out, void* scratch, int n_sm,
