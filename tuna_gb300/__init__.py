@@ -161,6 +161,7 @@ class Result:
     stats: Dict[str, float] = field(default_factory=dict)
     k: int = 0
     samples: Optional[np.ndarray] = None  # (n,) uint32 sample of each pair (jobs of several samples)
+    formatted: Optional[bytes] = None     # tg_job_drain output, when asked for
 
     def __len__(self) -> int:
         return int(self.counts.shape[0])
@@ -260,12 +261,14 @@ class Context:
 
     def run(self, k: int, m: int, *, seq=None, dev_seq=None, dev_len: int = 0, fastx=None, files=(),
             dev_fastx=None, samples=None, n_parts: int = 16, ci: int = 1, cx: int = _U64_MAX, gpu_parts: int = 0,
-            export: bool = False, want_results: bool = True):
+            export: bool = False, want_results: bool = True, drain: Optional[int] = None):
         """Run one job. seq: host stream (bytes / uint8 array); dev_seq: device
         pointer (int) of dev_len bytes; fastx: FASTA/FASTQ bytes; dev_fastx: device
         pointer of dev_len FASTA/FASTQ bytes; files: paths;
         samples: host streams counted as separate samples of the job (the
-        Result then carries the sample of each pair).
+        Result then carries the sample of each pair); drain: a tg_format (0 TSV,
+        1 KFF entries, 2 RAW) whose bytes tg_job_drain hands back in
+        Result.formatted.
         Returns (Result, partitions or None)."""
         L = self._L
         o = self._opts(k, m, n_parts, ci, cx, gpu_parts)
@@ -306,6 +309,17 @@ class Context:
                 off = np.zeros(len(samples) + 1, dtype=np.uint64)
                 self.check(L.tg_job_sample_offsets(j, off.ctypes.data))
                 smp = np.repeat(np.arange(len(samples), dtype=np.uint32), np.diff(off).astype(np.int64))
+            formatted = None
+            if drain is not None:
+                chunks = []
+
+                def dsink(data, nbytes, _npairs, _u):
+                    chunks.append(ctypes.string_at(data, nbytes))
+                    return 0
+
+                dcb = _SINK(dsink)
+                self.check(L.tg_job_drain(j, int(drain), dcb, None))
+                formatted = b"".join(chunks)
             parts = None
             if export:
                 parts = [b""] * n_parts
@@ -316,7 +330,7 @@ class Context:
 
                 cb = _PART_SINK(sink)
                 self.check(L.tg_job_export_partitions(j, cb, None))
-            return Result(keys, counts, st.as_dict(), k, smp), parts
+            return Result(keys, counts, st.as_dict(), k, smp, formatted), parts
         finally:
             L.tg_job_end(j)
 

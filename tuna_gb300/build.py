@@ -23,7 +23,7 @@ SYNTH_LIB = os.path.join(BUILD, "libtuna_synth.so")
 CLI_BIN = os.path.join(BUILD, "tuna")
 
 # translation units of libtuna_gpu.so
-CU_SOURCES = ["tg_api.cu", "tg_phase1.cu", "tg_phase2.cu", "tg_noalloc.cu", "tg_lex.cu"]
+CU_SOURCES = ["tg_api.cu", "tg_phase1.cu", "tg_phase2.cu", "tg_noalloc.cu", "tg_lex.cu", "tg_format.cu"]
 CPP_SOURCES = ["host/fastx.cpp", "host/output.cpp"]
 
 

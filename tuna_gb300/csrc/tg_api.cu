@@ -101,7 +101,9 @@ struct tg_ctx {
     unsigned host_threads = 1;
     std::string err;
     DevBuf seq, packed, valid, desc, xdesc, hist, scratch, okeys, ocnt, osamp, samp, okeys2, ocnt2, osoff,
-        misc, fbtab, tables, raw, lexs;
+        misc, fbtab, tables, raw, lexs, fbuf, fscr;
+    uint8_t* fhost[2] = {nullptr, nullptr};  // pinned host buffers of the output drain
+    size_t fhost_cap = 0;
     cudaEvent_t ev[12] = {};
     // results copied to the host while counting runs (tg_count_seq)
     cudaStream_t st_copy = nullptr;
@@ -209,7 +211,7 @@ tg_status tg_ctx_destroy(tg_ctx* ctx) {
     DevBuf* bufs[] = {&ctx->seq, &ctx->packed, &ctx->valid, &ctx->desc, &ctx->xdesc, &ctx->hist,
                       &ctx->scratch,
                       &ctx->okeys, &ctx->ocnt, &ctx->osamp, &ctx->samp, &ctx->okeys2, &ctx->ocnt2, &ctx->osoff, &ctx->misc, &ctx->fbtab, &ctx->tables,
-                      &ctx->raw, &ctx->lexs};
+                      &ctx->raw, &ctx->lexs, &ctx->fbuf, &ctx->fscr};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
     for (auto& e : ctx->ev)
@@ -221,6 +223,8 @@ tg_status tg_ctx_destroy(tg_ctx* ctx) {
         cudaStreamDestroy(ctx->st_copy);
     }
     if (ctx->wave_out) cudaFreeHost(ctx->wave_out);
+    for (uint8_t* h : ctx->fhost)
+        if (h) cudaFreeHost(h);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
     return TG_OK;
@@ -710,32 +714,66 @@ tg_status tg_job_sample_offsets(tg_job* j, uint64_t* offsets) {
     return TG_OK;
 }
 
-struct DrainCtx {
-    tg_sink_fn sink;
-    void* user;
-};
-static bool drain_sink(const std::string& chunk, uint64_t npairs, void* u) {
-    DrainCtx* d = static_cast<DrainCtx*>(u);
-    return d->sink(chunk.data(), chunk.size(), npairs, d->user) == 0;
-}
-
-static tg_status host_results(tg_job* j, std::vector<uint64_t>& keys, std::vector<uint32_t>& cnt) {
-    keys.resize(std::max<uint64_t>(1, j->n_out) * j->W);
-    cnt.resize(std::max<uint64_t>(1, j->n_out));
-    return tg_job_result_copy(j, keys.data(), cnt.data(), 0, j->n_out);
-}
+// Output formatting on the device in batches of DRAIN_PAIRS pairs: a batch is
+// formatted into ctx->fbuf, its byte count read through mapped memory, its
+// bytes copied into one of two pinned host buffers, and the previous batch is
+// handed to the sink while this one copies.
+constexpr uint64_t DRAIN_PAIRS = 1ull << 20;
 
 tg_status tg_job_drain(tg_job* j, tg_format fmt, tg_sink_fn sink, void* user) {
     if (!j || !sink || (int)fmt < 0 || (int)fmt > 2) return TG_ERR_ARG;
-    std::vector<uint64_t> keys;
-    std::vector<uint32_t> cnt;
-    tg_status s = host_results(j, keys, cnt);
-    if (s != TG_OK) return s;
-    tgh::Pairs p{keys.data(), cnt.data(), j->n_out, j->W, j->o.k};
-    DrainCtx d{sink, user};
-    if (!tgh::format_parallel(p, (int)fmt, j->ctx->host_threads, drain_sink, &d))
-        return j->ctx->fail(TG_ERR_IO, "output sink stopped");
-    return TG_OK;
+    tg_ctx* ctx = j->ctx;
+    if (!j->ran) return ctx->fail(TG_ERR_STATE, "drain before run");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const uint64_t n = j->n_out;
+    if (n == 0) return TG_OK;
+    const int k = j->o.k, W = j->W;
+    const bool multi = j->sample_start.size() > 1;
+    const uint64_t* keys = (multi ? ctx->okeys2 : ctx->okeys).as<uint64_t>();
+    const uint32_t* counts = (multi ? ctx->ocnt2 : ctx->ocnt).as<uint32_t>();
+    const uint64_t B = std::min<uint64_t>(n, DRAIN_PAIRS);
+    const size_t cap = (size_t)fmt_max_bytes((int)fmt, k, B) + 64;
+    CK(ctx->ensure(ctx->fbuf, cap), "alloc format buffer");
+    CK(ctx->ensure(ctx->fscr, fmt_scratch_bytes(B)), "alloc format scratch");
+    if (ctx->fhost_cap < cap) {
+        for (uint8_t*& h : ctx->fhost) {
+            if (h) cudaFreeHost(h);
+            h = nullptr;
+        }
+        ctx->fhost_cap = 0;
+        for (uint8_t*& h : ctx->fhost) CK(cudaHostAlloc(reinterpret_cast<void**>(&h), cap, cudaHostAllocDefault), "alloc pinned");
+        ctx->fhost_cap = cap;
+    }
+    const double t0 = now_ms();
+    unsigned long long* d_total = ctx->wave_out_dev + (OVERLAP_WORDS - 1);
+    const volatile unsigned long long* h_total = ctx->wave_out + (OVERLAP_WORDS - 1);
+    int launches = 0;
+    uint64_t prev_bytes = 0, prev_pairs = 0;
+    int prev = -1;
+    tg_status s = TG_OK;
+    const uint64_t nb = (n + B - 1) / B;
+    for (uint64_t b = 0; b < nb && s == TG_OK; ++b) {
+        const uint64_t first = b * B, m = std::min(B, n - first);
+        // the copy of batch b - 1 out of fbuf is ahead of this on the stream
+        CK(launch_format((int)fmt, k, keys + first * W, counts + first, m, ctx->fbuf.as<uint8_t>(), ctx->fscr.p,
+                         ctx->n_sm, ctx->st, d_total, &launches),
+           "format");
+        CK(cudaStreamSynchronize(ctx->st), "format");
+        const uint64_t bytes = fmt == TG_FMT_TSV ? (uint64_t)*h_total : fmt_max_bytes((int)fmt, k, m);
+        const int cur = (int)(b & 1);
+        CK(cudaMemcpyAsync(ctx->fhost[cur], ctx->fbuf.p, bytes, cudaMemcpyDeviceToHost, ctx->st), "d2h");
+        if (prev >= 0 && sink(ctx->fhost[prev], prev_bytes, prev_pairs, user) != 0)
+            s = ctx->fail(TG_ERR_IO, "output sink stopped");
+        prev = cur;
+        prev_bytes = bytes;
+        prev_pairs = m;
+    }
+    CK(cudaStreamSynchronize(ctx->st), "d2h");
+    if (s == TG_OK && prev >= 0 && sink(ctx->fhost[prev], prev_bytes, prev_pairs, user) != 0)
+        s = ctx->fail(TG_ERR_IO, "output sink stopped");
+    j->st.d2h_ms += now_ms() - t0;
+    j->st.gpu_launches += (uint64_t)launches;
+    return s;
 }
 
 struct FileSink {

@@ -35,6 +35,14 @@ struct LexTotals {
 size_t lex_scratch_bytes(uint64_t len);
 cudaError_t launch_lex(const uint8_t* raw, uint64_t len, bool fastq, uint8_t* out, void* scratch, int n_sm,
                        cudaStream_t st, LexTotals** dtot, int* launches);
+// Output formatting on the device (tg_format.cu): n pairs to the bytes of
+// format fmt (tg_format). TSV writes its byte count to d_total (device-
+// writable, e.g. mapped host memory); KFF and RAW records have a fixed size,
+// fmt_max_bytes, and leave d_total alone.
+size_t fmt_scratch_bytes(uint64_t n_pairs);
+uint64_t fmt_max_bytes(int fmt, int k, uint64_t n_pairs);
+cudaError_t launch_format(int fmt, int k, const uint64_t* keys, const uint32_t* counts, uint64_t n, uint8_t* out,
+                          void* scratch, int n_sm, cudaStream_t st, unsigned long long* d_total, int* launches);
 size_t key_bytes(int W);
 uint32_t count_slots(int W);
 
