@@ -53,6 +53,9 @@ def parse_args():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-plain section")
     ap.add_argument("--no-serve", action="store_true", help="skip the served section")
+    ap.add_argument("--no-output", action="store_true", help="skip the output-formatting section")
+    ap.add_argument("--no-large-k", action="store_true", help="skip the k=63 reads section")
+    ap.add_argument("--large-k-scale", type=float, default=1.0, help="fraction of the 3 Gbp k=63 read set")
     ap.add_argument("--batch-samples", type=int, default=2000)
     ap.add_argument("--batch-scale", type=float, default=0.004,
                     help="genome sizes of the batched mix: log-uniform 10 kbp - 50 Mbp times this")
@@ -245,6 +248,116 @@ def batched_vs_plain(ctx, n_samples: int, scale: float):
             "speedup": t_plain / t_batch, "plain_s": t_plain, "batched_s": t_batch,
             "api": "tg_count_seq per sample vs tg_count_batch, pinned host buffers, results in host memory",
             "same_pairs_per_sample": bool(same_sizes), "bit_exact_checked_samples": bool(exact)}
+
+
+def output_drain(ctx, dev, n_stream: int):
+    """Device formatting of every pair of the 3.1 Gbp job (tg_job_drain) into a
+    sink that only counts bytes: TSV and KFF entries."""
+    import ctypes
+    import tuna_gb300 as T
+    L = T.library()
+    o = T._JobOpts(K, M, NPARTS, 1, (1 << 64) - 1, 0, 0)
+    j = ctypes.c_void_p()
+    ctx.check(L.tg_job_begin(ctx.h, ctypes.byref(o), ctypes.byref(j)))
+    out = {}
+    try:
+        ctx.check(L.tg_job_feed_seq_device(j, ctypes.c_void_p(dev.data_ptr()), n_stream))
+        ctx.check(L.tg_job_run(j))
+        n = int(L.tg_job_result_size(j))
+        tot = [0]
+
+        def sink(_data, nbytes, _np, _u):
+            tot[0] += nbytes
+            return 0
+
+        cb = T._SINK(sink)
+        for fmt, name in ((0, "tsv"), (1, "kff")):
+            ctx.check(L.tg_job_drain(j, fmt, cb, None))  # warm (buffers)
+            tot[0] = 0
+            t0 = time.perf_counter()
+            ctx.check(L.tg_job_drain(j, fmt, cb, None))
+            t = time.perf_counter() - t0
+            out[name] = {"seconds": t, "bytes": tot[0], "gbytes_s": tot[0] / t / 1e9, "mpairs_s": n / t / 1e6}
+    finally:
+        L.tg_job_end(j)
+    out["pairs"] = n
+    out["api"] = ("tg_job_drain (include/tuna_gpu.h): formatted on the device in 2^20-pair batches, "
+                  "copied to pinned host buffers, handed to a sink that counts bytes")
+    return out
+
+
+def large_k(ctx, scale: float, steps: int):
+    """The k=63 read set: a seeded 100 Mbp genome with 20% repeats (1 kbp
+    families, 5% divergence), 150 bp reads at 30x (3 Gbp), 0.5% substitutions;
+    k=63 m=21, ci=2 cx=10000. End to end from the FASTQ bytes (tg_count_fastx),
+    and the device-resident step; then the KFF drain."""
+    import ctypes
+    import torch
+    import tuna_gb300 as T
+    from tuna_gb300 import synth
+    fq, meta = synth.large_k_reads(scale=scale)
+    L = T.library()
+    k, m, ci, cx = meta["k"], meta["m"], meta["ci"], meta["cx"]
+    bases = meta["reads"] * 150
+    dev = torch.from_numpy(fq).cuda()
+    o = T._JobOpts(k, m, 16, ci, cx, 0, 0)
+    # device-resident: FASTQ bytes already in HBM, lexed and counted
+    res, _ = ctx.run(k, m, dev_fastx=dev.data_ptr(), dev_len=int(fq.size), ci=ci, cx=cx, want_results=False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        res, _ = ctx.run(k, m, dev_fastx=dev.data_ptr(), dev_len=int(fq.size), ci=ci, cx=cx, want_results=False)
+    t_dev = (time.perf_counter() - t0) / steps
+    st = res.stats
+    n_out = int(st["out"])
+    del dev
+    h_in = torch.from_numpy(fq).pin_memory()
+    cap = n_out + 1024
+    h_keys = torch.empty(cap * 2, dtype=torch.int64, pin_memory=True)
+    h_cnt = torch.empty(cap, dtype=torch.int32, pin_memory=True)
+    nout = ctypes.c_uint64()
+    sts = T._Stats()
+
+    def step():
+        ctx.check(L.tg_count_fastx(ctx.h, ctypes.byref(o), ctypes.c_void_p(h_in.data_ptr()), h_in.numel(),
+                                   ctypes.c_void_p(h_keys.data_ptr()), ctypes.c_void_p(h_cnt.data_ptr()), cap,
+                                   ctypes.byref(nout), ctypes.byref(sts)))
+
+    step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    t_e2e = (time.perf_counter() - t0) / steps
+    # the KFF file body of this result
+    tot = [0]
+
+    def sink(_d, nbytes, _np, _u):
+        tot[0] += nbytes
+        return 0
+
+    cb = T._SINK(sink)
+    j = ctypes.c_void_p()
+    ctx.check(L.tg_job_begin(ctx.h, ctypes.byref(o), ctypes.byref(j)))
+    try:
+        ctx.check(L.tg_job_feed_fastx(j, ctypes.c_void_p(h_in.data_ptr()), h_in.numel()))
+        ctx.check(L.tg_job_run(j))
+        t0 = time.perf_counter()
+        ctx.check(L.tg_job_drain(j, 1, cb, None))
+        t_kff = time.perf_counter() - t0
+    finally:
+        L.tg_job_end(j)
+    del h_in, h_keys, h_cnt
+    return {"workload": f"{meta['genome'] / 1e6:.0f} Mbp genome, 20% repeats (1 kbp families, 5% divergence), "
+                        f"{meta['reads']} reads of 150 bp (30x), 0.5% substitutions; k=63 m=21 ci=2 cx=10000",
+            "bases": bases, "fastq_bytes": int(fq.size),
+            "device_gbases_s": bases / t_dev / 1e9, "device_ms": t_dev * 1e3,
+            "e2e_gbases_s": bases / t_e2e / 1e9, "e2e_ms": t_e2e * 1e3,
+            "kmers": int(st["kmers"]), "distinct": int(st["distinct"]), "out": n_out,
+            "parts_ms": {f: float(st[f]) for f in ("lex_ms", "pack_ms", "phase1_ms", "phase2_keys_ms",
+                                                     "phase2_count_ms")},
+            "kff_drain_s": t_kff, "kff_bytes": tot[0],
+            "api": "device: tg_job_feed_fastx_device + tg_job_run; e2e: tg_count_fastx from pinned FASTQ bytes, "
+                   "pairs to pinned host buffers"}
 
 
 def served(seconds: float, scale: float):
@@ -470,6 +583,14 @@ def main():
     else:
         parity_full = None
 
+    output = None
+    if rank == 0 and not args.no_output:
+        output = output_drain(ctx, dev, n_stream)
+    del dev
+    large = None
+    if rank == 0 and not args.no_large_k:
+        large = large_k(ctx, args.large_k_scale, max(1, min(args.steps, 3)))
+
     batched = None
     if rank == 0 and not args.no_batch:
         batched = batched_vs_plain(ctx, args.batch_samples, args.batch_scale)
@@ -504,6 +625,8 @@ def main():
             "cpu_baseline": cpu,
             "e2e": e2e,
             "parity": parity_full,
+            "output": output,
+            "large_k": large,
             "batched": batched,
             "serve": serve,
             "gpu_launches": launches,
