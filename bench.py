@@ -56,6 +56,7 @@ def parse_args():
     ap.add_argument("--no-output", action="store_true", help="skip the output-formatting section")
     ap.add_argument("--no-large-k", action="store_true", help="skip the k=63 reads section")
     ap.add_argument("--large-k-scale", type=float, default=1.0, help="fraction of the 3 Gbp k=63 read set")
+    ap.add_argument("--no-gz", action="store_true", help="skip the gzip-input section")
     ap.add_argument("--batch-samples", type=int, default=2000)
     ap.add_argument("--batch-scale", type=float, default=0.004,
                     help="genome sizes of the batched mix: log-uniform 10 kbp - 50 Mbp times this")
@@ -360,6 +361,50 @@ def large_k(ctx, scale: float, steps: int):
                    "pairs to pinned host buffers"}
 
 
+def gz_input(fasta: np.ndarray, mbytes: float = 300.0):
+    """Reading gzip input on the host (tg_read_input): a BGZF file inflated on
+    1 and on all host threads, and the same bytes as one gzip member (one
+    stream, as the reference's GzInput reads every .gz file)."""
+    import gzip
+    import zlib
+    from concurrent.futures import ThreadPoolExecutor
+    import tuna_gb300 as T
+    raw = fasta[: int(mbytes * 1e6)].tobytes()
+    blk = 65280
+
+    def member(i):
+        chunk = raw[i:i + blk]
+        c = zlib.compressobj(1, zlib.DEFLATED, -15)
+        payload = c.compress(chunk) + c.flush()
+        bsize = 18 + len(payload) + 8
+        return (b"\x1f\x8b\x08\x04\x00\x00\x00\x00\x00\xff\x06\x00BC\x02\x00" + (bsize - 1).to_bytes(2, "little")
+                + payload + zlib.crc32(chunk).to_bytes(4, "little") + len(chunk).to_bytes(4, "little"))
+
+    with ThreadPoolExecutor(os.cpu_count() or 1) as ex:
+        bg = b"".join(ex.map(member, range(0, len(raw), blk)))
+    bg += bytes.fromhex("1f8b08040000000000ff0600424302001b0003000000000000000000")
+    d = tempfile.mkdtemp()
+    p_bg, p_one = os.path.join(d, "a.fa.gz"), os.path.join(d, "b.fa.gz")
+    with open(p_bg, "wb") as f:
+        f.write(bg)
+    with open(p_one, "wb") as f:
+        f.write(gzip.compress(raw, compresslevel=1))
+    res = {"bytes": len(raw), "bgzf_bytes": len(bg)}
+    cores = os.cpu_count() or 1
+    for name, path, th in (("bgzf_1_thread", p_bg, 1), ("bgzf_all_threads", p_bg, cores), ("one_member", p_one, cores)):
+        T.read_input(path, th, cap=len(raw) + 1024)  # page cache warm
+        t0 = time.perf_counter()
+        got = T.read_input(path, th, cap=len(raw) + 1024)
+        t = time.perf_counter() - t0
+        assert got == raw
+        res[name] = {"seconds": t, "gbytes_s": len(raw) / t / 1e9, "threads": th}
+    for p in (p_bg, p_one):
+        os.remove(p)
+    os.rmdir(d)
+    res["api"] = "tg_read_input (include/tuna_gpu.h), the reading step of tg_job_feed_file"
+    return res
+
+
 def served(seconds: float, scale: float):
     """Poisson arrivals at 50 requests/s replayed in real time against the
     continuous-batching server; latency from arrival to result in host memory."""
@@ -583,6 +628,9 @@ def main():
     else:
         parity_full = None
 
+    gz = None
+    if rank == 0 and not args.no_gz and fasta_h is not None:
+        gz = gz_input(fasta_h)
     output = None
     if rank == 0 and not args.no_output:
         output = output_drain(ctx, dev, n_stream)
@@ -626,6 +674,7 @@ def main():
             "e2e": e2e,
             "parity": parity_full,
             "output": output,
+            "gz": gz,
             "large_k": large,
             "batched": batched,
             "serve": serve,

@@ -216,6 +216,16 @@ tg_status tg_count_batch(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_sample
                          uint32_t* counts, uint64_t* sample_offsets, uint64_t cap, uint64_t* n_out,
                          tg_stats* stats);
 
+/* Reads one input file into out (capacity cap; *out_len receives its length,
+ * TG_ERR_ARG if it does not fit) exactly as tg_job_feed_file reads it: plain,
+ * or inflated when the name ends in ".gz" (SeqSource's choice,
+ * src/seq_source.hpp:196-204). BGZF files, whose members carry their sizes, are
+ * inflated on `threads` host threads (0 = all cores); any other gzip file as
+ * one stream, as the reference's GzInput (src/seq_source.hpp:48-141). Host
+ * work only; errbuf (may be NULL) receives the message of a failure. */
+tg_status tg_read_input(const char* path, uint32_t threads, uint8_t* out, size_t cap, size_t* out_len,
+                        char* errbuf, size_t errlen);
+
 /* ---- counting without device allocation --------------------------------
  * No counterpart in the reference: tuna allocates its partition buffers and
  * tables as it goes. This entry point is for callers that must not allocate

@@ -1,0 +1,95 @@
+"""gzip input (tg_read_input / tg_job_feed_file on ".gz" files): BGZF files
+are cut at the member sizes in their 'BC' extra fields and inflated on several
+host threads; any other gzip file is read as one stream, as the reference's
+GzInput does (src/seq_source.hpp:48-141). Either way the bytes are the file's
+inflated bytes, checked here against Python's gzip."""
+import gzip
+import os
+import zlib
+
+import numpy as np
+import pytest
+
+import tuna_gb300 as T
+
+BGZF_EOF = bytes.fromhex("1f8b08040000000000ff0600424302001b0003000000000000000000")
+
+
+def bgzf(data: bytes, block: int = 65280, level: int = 6) -> bytes:
+    """BGZF encoding: gzip members of at most `block` input bytes, each with
+    the 'BC' extra subfield holding its total size minus one, then the empty
+    end-of-file member."""
+    out = bytearray()
+    for i in range(0, len(data), block):
+        chunk = data[i:i + block]
+        c = zlib.compressobj(level, zlib.DEFLATED, -15)
+        payload = c.compress(chunk) + c.flush()
+        bsize = 18 + len(payload) + 8
+        out += b"\x1f\x8b\x08\x04\x00\x00\x00\x00\x00\xff" + (6).to_bytes(2, "little")
+        out += b"BC" + (2).to_bytes(2, "little") + (bsize - 1).to_bytes(2, "little")
+        out += payload + zlib.crc32(chunk).to_bytes(4, "little") + len(chunk).to_bytes(4, "little")
+    return bytes(out) + BGZF_EOF
+
+
+def _fastq(seed: int, n: int = 3000) -> bytes:
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        L = int(rng.integers(50, 200))
+        s = bytes(rng.choice(np.frombuffer(b"ACGTN", dtype=np.uint8), L, p=[.24, .25, .25, .25, .01]))
+        out.append(b"@r%d\n" % i + s + b"\n+\n" + b"I" * L + b"\n")
+    return b"".join(out)
+
+
+def _write(tmp_path, name, data):
+    p = os.path.join(tmp_path, name)
+    with open(p, "wb") as f:
+        f.write(data)
+    return p
+
+
+@pytest.mark.parametrize("threads", [1, 4, 16])
+def test_bgzf_inflates_on_threads(tmp_path, threads):
+    raw = _fastq(1, 6000)
+    p = _write(tmp_path, "a.fq.gz", bgzf(raw, block=10_000))
+    assert T.read_input(p, threads=threads) == raw
+
+
+def test_other_gzip_read_as_one_stream(tmp_path):
+    raw = _fastq(2)
+    half = len(raw) // 2
+    multi = gzip.compress(raw[:half]) + gzip.compress(raw[half:])  # two members, no size fields
+    assert T.read_input(_write(tmp_path, "m.fq.gz", multi)) == raw
+    assert T.read_input(_write(tmp_path, "s.fq.gz", gzip.compress(raw))) == raw
+
+
+def test_plain_and_errors(tmp_path):
+    raw = _fastq(3, 100)
+    assert T.read_input(_write(tmp_path, "p.fq", raw)) == raw
+    with pytest.raises(T.GpuError) as e:
+        T.read_input(_write(tmp_path, "empty.fq", b""))
+    assert "Empty file" in str(e.value)
+    bad = bytearray(bgzf(raw, block=2000))
+    bad[40] ^= 0xFF  # inside the first member's deflate data
+    with pytest.raises(T.GpuError) as e:
+        T.read_input(_write(tmp_path, "bad.fq.gz", bytes(bad)))
+    assert "Cannot read" in str(e.value)
+    with pytest.raises(T.GpuError):
+        T.read_input(os.path.join(tmp_path, "missing.fq.gz"))
+
+
+def test_bgzf_empty_members_only(tmp_path):
+    with pytest.raises(T.GpuError) as e:
+        T.read_input(_write(tmp_path, "eof.gz", BGZF_EOF))
+    assert "Cannot read" in str(e.value)
+
+
+@pytest.mark.gpu
+def test_count_bgzf_file(tmp_path):
+    from oracle import oracle as O
+    raw = _fastq(4, 20_000)
+    p = _write(tmp_path, "c.fq.gz", bgzf(raw))
+    with T.Context(0) as ctx:
+        got, _ = ctx.run(31, 21, files=[p])
+    want = O.count_fastx(raw, 31, 21, threads=4)
+    assert T.tsv_blob(got.keys, got.counts, 31) == O.tsv_blob(want)

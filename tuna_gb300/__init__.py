@@ -79,7 +79,7 @@ ABI_SYMBOLS = ["tg_ctx_create", "tg_ctx_destroy", "tg_last_error", "tg_ctx_strea
                "tg_job_result_copy", "tg_job_drain", "tg_job_write", "tg_job_export_partitions", "tg_job_end",
                "tg_count_seq", "tg_count_seq_device_noalloc", "tg_job_next_sample", "tg_job_sample_count",
                "tg_job_sample_offsets", "tg_count_batch", "tg_job_feed_fastx_device", "tg_count_fastx",
-               "tg_fastx_to_stream"]
+               "tg_fastx_to_stream", "tg_read_input"]
 
 
 def library(build_if_missing: bool = True) -> ctypes.CDLL:
@@ -111,6 +111,7 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
     L.tg_count_fastx.argtypes = [vp, ctypes.POINTER(_JobOpts), vp, sz, vp, vp, u64, ctypes.POINTER(u64),
                                  ctypes.POINTER(_Stats)]
     L.tg_fastx_to_stream.argtypes = [vp, vp, sz, vp, sz, ctypes.POINTER(sz)]
+    L.tg_read_input.argtypes = [ctypes.c_char_p, u32, vp, sz, ctypes.POINTER(sz), ctypes.c_char_p, sz]
     L.tg_job_run.argtypes = [vp]
     L.tg_job_stats.argtypes = [vp, ctypes.POINTER(_Stats)]
     L.tg_job_result_size.argtypes = [vp]
@@ -137,7 +138,7 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
                "tg_job_feed_fastx", "tg_job_feed_file", "tg_job_run", "tg_job_stats", "tg_job_result_copy",
                "tg_job_drain", "tg_job_write", "tg_job_export_partitions", "tg_job_end", "tg_count_seq",
                "tg_job_next_sample", "tg_job_sample_offsets", "tg_count_batch", "tg_job_feed_fastx_device",
-               "tg_count_fastx", "tg_fastx_to_stream"):
+               "tg_count_fastx", "tg_fastx_to_stream", "tg_read_input"):
         getattr(L, fn).restype = i32
     _lib = L
     return L
@@ -354,6 +355,21 @@ class Context:
             return st.as_dict()
         finally:
             L.tg_job_end(j)
+
+
+def read_input(path: str, threads: int = 0, cap: Optional[int] = None) -> bytes:
+    """The bytes of one input file as the library reads it (tg_read_input):
+    plain, or inflated for ".gz" (BGZF on `threads` host threads)."""
+    L = library()
+    if cap is None:
+        cap = max(1 << 20, 64 * os.path.getsize(path)) if os.path.exists(path) else 1 << 20
+    out = np.empty(cap, dtype=np.uint8)
+    n = ctypes.c_size_t()
+    err = ctypes.create_string_buffer(512)
+    rc = L.tg_read_input(os.fsencode(path), threads, out.ctypes.data, cap, ctypes.byref(n), err, 512)
+    if rc != 0:
+        raise GpuError(rc, err.value.decode(errors="replace"))
+    return out[: n.value].tobytes()
 
 
 _default_ctx: Optional[Context] = None

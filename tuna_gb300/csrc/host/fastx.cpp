@@ -20,8 +20,11 @@
 
 #include <dlfcn.h>
 
+#include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
+#include <thread>
 
 namespace tgh {
 
@@ -171,16 +174,45 @@ bool fastx_to_stream(const uint8_t* data, size_t len, std::vector<uint8_t>& out)
 // zlib is loaded at run time (libz.so.1), so the library builds without zlib
 // development headers; gzip input fails with a clear message if it is absent.
 namespace {
+// z_stream as zlib.h lays it out (LP64), for the raw-deflate calls below
+struct ZStream {
+    const uint8_t* next_in;
+    unsigned avail_in;
+    unsigned long total_in;
+    uint8_t* next_out;
+    unsigned avail_out;
+    unsigned long total_out;
+    const char* msg;
+    void* state;
+    void* zalloc;
+    void* zfree;
+    void* opaque;
+    int data_type;
+    unsigned long adler;
+    unsigned long reserved;
+};
 struct Zlib {
     using open_t = void* (*)(const char*, const char*);
     using read_t = int (*)(void*, void*, unsigned);
     using close_t = int (*)(void*);
     using buffer_t = int (*)(void*, unsigned);
+    using init2_t = int (*)(ZStream*, int, const char*, int);
+    using inflate_t = int (*)(ZStream*, int);
+    using end_t = int (*)(ZStream*);
+    using reset_t = int (*)(ZStream*);
+    using crc_t = unsigned long (*)(unsigned long, const uint8_t*, unsigned);
+    using version_t = const char* (*)();
     open_t gzopen = nullptr;
     read_t gzread = nullptr;
     close_t gzclose = nullptr;
     buffer_t gzbuffer = nullptr;
-    bool ok = false;
+    init2_t inflateInit2_ = nullptr;
+    inflate_t inflate = nullptr;
+    end_t inflateEnd = nullptr;
+    reset_t inflateReset = nullptr;
+    crc_t crc32 = nullptr;
+    version_t zlibVersion = nullptr;
+    bool ok = false, raw_ok = false;
     Zlib() {
         void* h = dlopen("libz.so.1", RTLD_NOW | RTLD_LOCAL);
         if (!h) h = dlopen("libz.so", RTLD_NOW | RTLD_LOCAL);
@@ -189,20 +221,129 @@ struct Zlib {
         gzread = reinterpret_cast<read_t>(dlsym(h, "gzread"));
         gzclose = reinterpret_cast<close_t>(dlsym(h, "gzclose"));
         gzbuffer = reinterpret_cast<buffer_t>(dlsym(h, "gzbuffer"));
+        inflateInit2_ = reinterpret_cast<init2_t>(dlsym(h, "inflateInit2_"));
+        inflate = reinterpret_cast<inflate_t>(dlsym(h, "inflate"));
+        inflateEnd = reinterpret_cast<end_t>(dlsym(h, "inflateEnd"));
+        inflateReset = reinterpret_cast<reset_t>(dlsym(h, "inflateReset"));
+        crc32 = reinterpret_cast<crc_t>(dlsym(h, "crc32"));
+        zlibVersion = reinterpret_cast<version_t>(dlsym(h, "zlibVersion"));
         ok = gzopen && gzread && gzclose;
+        raw_ok = inflateInit2_ && inflate && inflateEnd && inflateReset && crc32 && zlibVersion;
     }
 };
 const Zlib& zlib() {
     static Zlib z;
     return z;
 }
+
+inline uint32_t le16(const uint8_t* p) { return (uint32_t)p[0] | ((uint32_t)p[1] << 8); }
+inline uint32_t le32(const uint8_t* p) { return le16(p) | (le16(p + 2) << 16); }
+
+struct BgzfBlock {
+    size_t cdata, clen;  // raw deflate payload in the file
+    uint32_t isize, crc;
+    size_t out;          // offset of its bytes in the inflated file
+};
+
+// BGZF (the blocked gzip of SAM/BAM and bgzip): every member carries its own
+// size in the 'BC' extra subfield, so the members are found without
+// inflating. False if the file is not entirely such members.
+bool bgzf_blocks(const uint8_t* d, size_t n, std::vector<BgzfBlock>& out) {
+    size_t off = 0, o = 0;
+    while (off < n) {
+        if (n - off < 26 || d[off] != 0x1F || d[off + 1] != 0x8B || d[off + 2] != 8 || d[off + 3] != 4) return false;
+        const uint32_t xlen = le16(d + off + 10);
+        if (n - off < 12 + (size_t)xlen + 8) return false;
+        size_t bsize = 0;
+        for (size_t x = off + 12; x + 4 <= off + 12 + xlen;) {
+            const uint32_t slen = le16(d + x + 2);
+            if (d[x] == 'B' && d[x + 1] == 'C' && slen == 2 && x + 6 <= off + 12 + xlen) bsize = le16(d + x + 4) + 1;
+            x += 4 + slen;
+        }
+        if (bsize == 0 || bsize < 12 + (size_t)xlen + 8 || off + bsize > n) return false;
+        BgzfBlock b;
+        b.cdata = off + 12 + xlen;
+        b.clen = bsize - (12 + xlen) - 8;
+        b.crc = le32(d + off + bsize - 8);
+        b.isize = le32(d + off + bsize - 4);
+        b.out = o;
+        o += b.isize;
+        out.push_back(b);
+        off += bsize;
+    }
+    return !out.empty();
+}
+
+// Inflates the blocks on `threads` host threads into out; false on a corrupt block.
+bool bgzf_inflate(const Zlib& Z, const uint8_t* d, const std::vector<BgzfBlock>& blocks, unsigned threads,
+                  Bytes& out) {
+    const BgzfBlock& last = blocks.back();
+    out.resize(last.out + last.isize);
+    std::atomic<size_t> next{0};
+    std::atomic<bool> bad{false};
+    const size_t per = 64;  // blocks per claim (about 4 MiB of output)
+    auto work = [&]() {
+        ZStream zs{};
+        if (Z.inflateInit2_(&zs, -15, Z.zlibVersion(), (int)sizeof(ZStream)) != 0) {
+            bad = true;
+            return;
+        }
+        for (;;) {
+            const size_t b0 = next.fetch_add(per);
+            if (b0 >= blocks.size() || bad) break;
+            for (size_t i = b0; i < std::min(blocks.size(), b0 + per) && !bad; ++i) {
+                const BgzfBlock& b = blocks[i];
+                if (Z.inflateReset(&zs) != 0) { bad = true; break; }  // each block is its own raw stream
+                zs.next_in = d + b.cdata;
+                zs.avail_in = (unsigned)b.clen;
+                zs.next_out = out.data() + b.out;
+                zs.avail_out = b.isize;
+                const unsigned long before = zs.total_out;
+                const int r = Z.inflate(&zs, 4 /* Z_FINISH */);
+                const bool ended = r == 1 /* Z_STREAM_END */ || (b.isize == 0 && b.crc == 0 && r == -5);
+                if (!ended || zs.total_out - before != b.isize ||
+                    Z.crc32(0, out.data() + b.out, b.isize) != b.crc)
+                    bad = true;
+            }
+        }
+        Z.inflateEnd(&zs);
+    };
+    threads = std::max(1u, std::min<unsigned>(threads, (unsigned)((blocks.size() + per - 1) / per)));
+    std::vector<std::thread> th;
+    for (unsigned t = 1; t < threads; ++t) th.emplace_back(work);
+    work();
+    for (auto& t : th) t.join();
+    return !bad;
+}
 }  // namespace
 
-std::string read_input_file(const std::string& path, std::vector<uint8_t>& out) {
+std::string read_input_file(const std::string& path, Bytes& out, unsigned threads) {
     const bool gz = path.size() > 3 && path.compare(path.size() - 3, 3, ".gz") == 0;
     if (gz) {
         const Zlib& Z = zlib();
         if (!Z.ok) return "gzip input needs libz.so.1: " + path;
+        // BGZF: members found from their headers, inflated on all threads
+        if (Z.raw_ok) {
+            Bytes comp;
+            FILE* f = fopen(path.c_str(), "rb");
+            if (!f) return "Cannot open: " + path;
+            fseek(f, 0, SEEK_END);
+            const long sz = ftell(f);
+            fseek(f, 0, SEEK_SET);
+            if (sz > 0) {
+                comp.resize((size_t)sz);
+                const size_t r = fread(comp.data(), 1, comp.size(), f);
+                if (r != comp.size()) comp.clear();
+            }
+            fclose(f);
+            std::vector<BgzfBlock> blocks;
+            if (!comp.empty() && bgzf_blocks(comp.data(), comp.size(), blocks)) {
+                if (!bgzf_inflate(Z, comp.data(), blocks, threads, out)) return "Cannot read: " + path;
+                if (out.empty()) return "Cannot read: " + path;
+                return "";
+            }
+        }
+        // any other gzip file: one stream through gzread, as the reference reads it
         void* f = Z.gzopen(path.c_str(), "rb");
         if (!f) return "Cannot open: " + path;
         if (Z.gzbuffer) Z.gzbuffer(f, 1u << 20);

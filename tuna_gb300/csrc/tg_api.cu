@@ -421,13 +421,51 @@ tg_status tg_job_feed_fastx_device(tg_job* j, const uint8_t* ddata, size_t len) 
 
 tg_status tg_job_feed_file(tg_job* j, const char* path) {
     if (!j || !path) return TG_ERR_ARG;
-    std::vector<uint8_t> raw;
-    const std::string err = tgh::read_input_file(path, raw);
+    tgh::Bytes raw;
+    const std::string err = tgh::read_input_file(path, raw, j->ctx->host_threads);
     if (!err.empty()) {
         const bool empty = err.rfind("Empty file", 0) == 0;
         return j->ctx->fail(empty ? TG_ERR_PARSE : TG_ERR_IO, err);
     }
     return lex_append_host(j, raw.data(), raw.size());
+}
+
+tg_status tg_read_input(const char* path, uint32_t threads, uint8_t* out, size_t cap, size_t* out_len,
+                        char* errbuf, size_t errlen) {
+    if (!path || !out_len) return TG_ERR_ARG;
+    *out_len = 0;
+    auto set_err = [&](const std::string& m) {
+        if (errbuf && errlen) {
+            const size_t n = std::min(errlen - 1, m.size());
+            memcpy(errbuf, m.data(), n);
+            errbuf[n] = 0;
+        }
+    };
+    tgh::Bytes raw;
+    const std::string err =
+        tgh::read_input_file(path, raw, threads ? threads : std::max(1u, std::thread::hardware_concurrency()));
+    if (!err.empty()) {
+        set_err(err);
+        return err.rfind("Empty file", 0) == 0 ? TG_ERR_PARSE : TG_ERR_IO;
+    }
+    *out_len = raw.size();
+    if (raw.size() > cap) {
+        set_err("output buffer too small");
+        return TG_ERR_ARG;
+    }
+    // the copy out, on the same threads for large files
+    const unsigned nt = (unsigned)std::min<size_t>(threads ? threads : std::max(1u, std::thread::hardware_concurrency()),
+                                                   std::max<size_t>(1, raw.size() >> 24));
+    const size_t per = (raw.size() + nt - 1) / nt;
+    std::vector<std::thread> th;
+    for (unsigned t = 1; t < nt; ++t)
+        th.emplace_back([&, t] {
+            const size_t a = std::min(raw.size(), t * per), b = std::min(raw.size(), a + per);
+            if (b > a) memcpy(out + a, raw.data() + a, b - a);
+        });
+    if (!raw.empty()) memcpy(out, raw.data(), std::min(raw.size(), per));
+    for (auto& t : th) t.join();
+    return TG_OK;
 }
 
 tg_status tg_fastx_to_stream(tg_ctx* ctx, const uint8_t* data, size_t len, uint8_t* out, size_t cap,
