@@ -65,7 +65,10 @@ typedef struct tg_job tg_job;
 
 typedef struct {
     int device;                 /* CUDA device ordinal */
-    uint64_t hbm_budget_bytes;  /* 0 = free HBM minus a reserve */
+    uint64_t hbm_budget_bytes;  /* device memory phase 2 may hold at once (keys, pairs, groups);
+                                   0 = free HBM minus a reserve. A job whose keys and pairs do
+                                   not fit is counted in passes over ranges of bins, each pass's
+                                   pairs copied to host memory (results then stay on the host) */
     uint32_t host_threads;      /* host parser / formatter threads; 0 = all cores */
     uint32_t flags;             /* reserved, 0 */
 } tg_ctx_opts;
@@ -107,6 +110,8 @@ typedef struct {
     double lex_ms;            /* device time: FASTA/FASTQ lexing of the feeds */
     uint64_t fastx_bytes;     /* FASTA/FASTQ bytes fed (before lexing) */
     uint64_t host_parsed_bytes; /* of those, bytes parsed on the host (see tg_job_feed_fastx) */
+    uint64_t phase2_passes;   /* phase-2 passes over ranges of bins (more than 1 when the keys and
+                                 pairs of a job exceed the context's memory budget, hbm_budget_bytes) */
 } tg_stats;
 
 /* Output formats of tg_job_drain. */

@@ -97,6 +97,7 @@ struct tg_ctx {
     int device = 0;
     cudaStream_t st = nullptr;
     int n_sm = 0;
+    uint64_t hbm_budget = 0;  // tg_ctx_opts.hbm_budget_bytes
     size_t smem_optin = 0;
     unsigned host_threads = 1;
     std::string err;
@@ -154,6 +155,14 @@ struct tg_job {
     // samples: sample i starts at stream position sample_start[i]
     std::vector<unsigned long long> sample_start{0};
     int lex_launches = 0;  // lexer kernels of the feeds
+    // phase 2 in passes (memory budget): the pairs are in host memory, either
+    // the caller's buffers (sink_*, the one-call entry points) or host_keys/_counts
+    bool spilled = false;
+    std::vector<uint64_t> host_keys;
+    std::vector<uint32_t> host_counts;
+    uint64_t* sink_keys = nullptr;
+    uint32_t* sink_counts = nullptr;
+    uint64_t sink_cap = 0;
     const uint8_t* seq_ptr() const { return ext ? ext : ctx->seq.as<uint8_t>(); }
 };
 
@@ -183,6 +192,7 @@ tg_status tg_ctx_create(const tg_ctx_opts* opts, tg_ctx** out) {
     if (o.device < 0 || o.device >= ndev) return TG_ERR_ARG;
     tg_ctx* ctx = new tg_ctx();
     ctx->device = o.device;
+    ctx->hbm_budget = o.hbm_budget_bytes;
     ctx->host_threads = o.host_threads ? o.host_threads : std::max(1u, std::thread::hardware_concurrency());
     cudaError_t e = cudaSetDevice(o.device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking);
@@ -629,17 +639,10 @@ tg_status tg_job_run(tg_job* j) {
     CK(cudaMemcpyAsync(nd.data(), ctx->misc.as<uint8_t>() + MISC_NDESC, (size_t)C * 4, cudaMemcpyDeviceToHost,
                        ctx->st), "d2h");
     CK(cudaStreamSynchronize(ctx->st), "phase 1");
-    // ---- buffers: phase-2 scratch (keys included), output
+    // ---- phase 2: one run over all bins or, when their keys and pairs do not
+    // fit in the memory budget, passes over ranges of consecutive segments
+    // (bins), each pass's pairs going to host memory before the next
     const uint64_t n_kmers = cstats[0];
-    const uint64_t out_cap = std::max<uint64_t>(n_kmers, 1);
-    CK(ctx->ensure(ctx->okeys, out_cap * key_bytes(W)), "alloc output keys");
-    CK(ctx->ensure(ctx->ocnt, out_cap * 4), "alloc output counts");
-    if (ns > 1) {
-        CK(ctx->ensure(ctx->osamp, out_cap * 4), "alloc output samples");
-        CK(ctx->ensure(ctx->okeys2, out_cap * key_bytes(W)), "alloc output keys");
-        CK(ctx->ensure(ctx->ocnt2, out_cap * 4), "alloc output counts");
-        CK(ctx->ensure(ctx->osoff, 8 * ((size_t)ns + 1)), "alloc sample offsets");
-    }
     P2Input in{};
     in.W = W;
     in.k = k;
@@ -656,52 +659,157 @@ tg_status tg_job_run(tg_job* j) {
     in.ci = j->o.ci;
     in.cx = j->o.cx;
     in.n_samples = ns;
-    const size_t p2_bytes = phase2_scratch_bytes(in);
-    CK(ctx->ensure(ctx->scratch, p2_bytes), "alloc phase-2 scratch");
-    CK(cudaEventRecord(ctx->ev[6], ctx->st), "event");
-    // ---- phase 2
-    P2Output out{};
-    out.keys = ctx->okeys.p;
-    out.counts = ctx->ocnt.as<uint32_t>();
-    out.samples = ns > 1 ? ctx->osamp.as<uint32_t>() : nullptr;
-    out.n_samples = ns;
-    if (ns > 1) {
-        out.keys2 = ctx->okeys2.p;
-        out.counts2 = ctx->ocnt2.as<uint32_t>();
-        out.sample_off = ctx->osoff.as<unsigned long long>();
+    std::vector<std::pair<uint32_t, uint32_t>> passes;  // segment ranges
+    std::vector<uint64_t> seg_keys;
+    {
+        const uint64_t per_key = 2 * key_bytes(W) + 4 + 24;  // key, pair, groups and slack
+        size_t free_b = 0, total_b = 0;
+        CK(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+        const uint64_t have = free_b + ctx->scratch.cap + ctx->okeys.cap + ctx->ocnt.cap;
+        const uint64_t reserve = (2ull << 30) + total_b / 50;
+        const uint64_t budget = ctx->hbm_budget ? ctx->hbm_budget : (have > reserve ? have - reserve : 0);
+        if (ns == 1 && B.segs.size() > 1 && n_kmers * per_key > budget) {
+            std::vector<uint32_t> hist((size_t)1 << BIN_BITS);
+            CK(cudaMemcpy(hist.data(), ctx->hist.p, hist.size() * 4, cudaMemcpyDeviceToHost), "d2h");
+            const uint64_t max_keys = std::max<uint64_t>(1, budget / per_key);
+            uint32_t s0 = 0;
+            uint64_t acc = 0;
+            for (uint32_t sg = 0; sg < B.segs.size(); ++sg) {
+                uint64_t kk = 0;
+                for (uint32_t b = B.segs[sg].bin_lo; b < B.segs[sg].bin_hi; ++b) kk += hist[b];
+                seg_keys.push_back(kk);
+                if (sg > s0 && acc + kk > max_keys) {
+                    passes.emplace_back(s0, sg);
+                    s0 = sg;
+                    acc = 0;
+                }
+                acc += kk;
+            }
+            passes.emplace_back(s0, (uint32_t)B.segs.size());
+        }
     }
-    out.cap = out_cap;
+    CK(cudaEventRecord(ctx->ev[6], ctx->st), "event");
     std::string msg;
     auto fallback_table = [&](size_t bytes) -> void* {
         return ctx->ensure(ctx->fbtab, bytes) == cudaSuccess ? ctx->fbtab.p : nullptr;
     };
-    const tg_status ps = phase2_run(in, ctx->scratch.p, p2_bytes, out, fallback_table, ctx->st, ctx->ev[7],
-                                    &launches, msg, j->overlap ? *j->overlap : P2Overlap());
-    if (ps != TG_OK) return ctx->fail(ps, msg);
-    CK(cudaEventRecord(ctx->ev[8], ctx->st), "event");
-    CK(cudaEventSynchronize(ctx->ev[8]), "sync");
-    j->n_out = out.n_out;
-    // ---- stats
-    float ms = 0;
+    P2Output out{};
     tg_stats& S = j->st;
+    float ms = 0;
+    if (passes.size() <= 1) {
+        const uint64_t out_cap = std::max<uint64_t>(n_kmers, 1);
+        CK(ctx->ensure(ctx->okeys, out_cap * key_bytes(W)), "alloc output keys");
+        CK(ctx->ensure(ctx->ocnt, out_cap * 4), "alloc output counts");
+        if (ns > 1) {
+            CK(ctx->ensure(ctx->osamp, out_cap * 4), "alloc output samples");
+            CK(ctx->ensure(ctx->okeys2, out_cap * key_bytes(W)), "alloc output keys");
+            CK(ctx->ensure(ctx->ocnt2, out_cap * 4), "alloc output counts");
+            CK(ctx->ensure(ctx->osoff, 8 * ((size_t)ns + 1)), "alloc sample offsets");
+        }
+        const size_t p2_bytes = phase2_scratch_bytes(in);
+        CK(ctx->ensure(ctx->scratch, p2_bytes), "alloc phase-2 scratch");
+        out.keys = ctx->okeys.p;
+        out.counts = ctx->ocnt.as<uint32_t>();
+        out.samples = ns > 1 ? ctx->osamp.as<uint32_t>() : nullptr;
+        out.n_samples = ns;
+        if (ns > 1) {
+            out.keys2 = ctx->okeys2.p;
+            out.counts2 = ctx->ocnt2.as<uint32_t>();
+            out.sample_off = ctx->osoff.as<unsigned long long>();
+        }
+        out.cap = out_cap;
+        CK(cudaEventRecord(ctx->ev[6], ctx->st), "event");
+        const tg_status ps = phase2_run(in, ctx->scratch.p, p2_bytes, out, fallback_table, ctx->st, ctx->ev[7],
+                                        &launches, msg, j->overlap ? *j->overlap : P2Overlap());
+        if (ps != TG_OK) return ctx->fail(ps, msg);
+        CK(cudaEventRecord(ctx->ev[8], ctx->st), "event");
+        CK(cudaEventSynchronize(ctx->ev[8]), "sync");
+        j->n_out = out.n_out;
+        S.distinct = out.distinct;
+        S.fallback_groups = out.fallback_groups;
+        S.groups = out.groups;
+        S.heavy_groups = (uint32_t)out.heavy_groups;
+        cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[8]); S.phase2_ms = ms;
+        cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]); S.phase2_keys_ms = ms;
+        cudaEventElapsedTime(&ms, ctx->ev[7], ctx->ev[8]); S.phase2_count_ms = ms;
+        S.phase2_passes = 1;
+    } else {
+        // sizes of the largest pass
+        uint64_t max_keys = 0;
+        std::vector<P2Input> pin(passes.size(), in);
+        size_t p2_bytes = 0;
+        for (size_t p = 0; p < passes.size(); ++p) {
+            P2Input& ip = pin[p];
+            const uint32_t s0 = passes[p].first, s1 = passes[p].second;
+            ip.segs = B.segs.data() + s0;
+            ip.n_segs = s1 - s0;
+            ip.bin_lo = B.segs[s0].bin_lo;
+            ip.bin_hi = B.segs[s1 - 1].bin_hi;
+            ip.n_kmers = 0;
+            for (uint32_t sg = s0; sg < s1; ++sg) ip.n_kmers += seg_keys[sg];
+            max_keys = std::max(max_keys, ip.n_kmers);
+            p2_bytes = std::max(p2_bytes, phase2_scratch_bytes(ip));
+        }
+        const uint64_t out_cap = std::max<uint64_t>(max_keys, 1);
+        CK(ctx->ensure(ctx->okeys, out_cap * key_bytes(W)), "alloc output keys");
+        CK(ctx->ensure(ctx->ocnt, out_cap * 4), "alloc output counts");
+        CK(ctx->ensure(ctx->scratch, p2_bytes), "alloc phase-2 scratch");
+        j->spilled = true;
+        j->host_keys.clear();
+        j->host_counts.clear();
+        uint64_t acc = 0;
+        const double t0 = now_ms();
+        for (size_t p = 0; p < passes.size(); ++p) {
+            P2Output po{};
+            po.keys = ctx->okeys.p;
+            po.counts = ctx->ocnt.as<uint32_t>();
+            po.cap = out_cap;
+            CK(cudaEventRecord(ctx->ev[6], ctx->st), "event");
+            const tg_status ps = phase2_run(pin[p], ctx->scratch.p, p2_bytes, po, fallback_table, ctx->st,
+                                            ctx->ev[7], &launches, msg, P2Overlap());
+            if (ps != TG_OK) return ctx->fail(ps, msg);
+            CK(cudaEventRecord(ctx->ev[8], ctx->st), "event");
+            CK(cudaEventSynchronize(ctx->ev[8]), "sync");
+            cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]); S.phase2_keys_ms += ms;
+            cudaEventElapsedTime(&ms, ctx->ev[7], ctx->ev[8]); S.phase2_count_ms += ms;
+            const uint64_t n_p = po.n_out;
+            const double c0 = now_ms();
+            if (j->sink_keys || j->sink_counts) {  // straight into the caller's buffers, as far as they reach
+                const uint64_t m = acc < j->sink_cap ? std::min(n_p, j->sink_cap - acc) : 0;
+                if (m && j->sink_keys)
+                    CK(cudaMemcpy(j->sink_keys + acc * W, po.keys, m * key_bytes(W), cudaMemcpyDeviceToHost), "d2h");
+                if (m && j->sink_counts)
+                    CK(cudaMemcpy(j->sink_counts + acc, po.counts, m * 4, cudaMemcpyDeviceToHost), "d2h");
+            } else if (n_p) {
+                j->host_keys.resize((acc + n_p) * W);
+                j->host_counts.resize(acc + n_p);
+                CK(cudaMemcpy(j->host_keys.data() + acc * W, po.keys, n_p * key_bytes(W), cudaMemcpyDeviceToHost),
+                   "d2h");
+                CK(cudaMemcpy(j->host_counts.data() + acc, po.counts, n_p * 4, cudaMemcpyDeviceToHost), "d2h");
+            }
+            S.d2h_ms += now_ms() - c0;
+            acc += n_p;
+            S.distinct += po.distinct;
+            S.fallback_groups += po.fallback_groups;
+            S.groups += po.groups;
+            S.heavy_groups += (uint32_t)po.heavy_groups;
+        }
+        S.phase2_ms = now_ms() - t0;
+        S.phase2_passes = passes.size();
+        j->n_out = acc;
+    }
+    // ---- stats
     S.bases = n_bases;
     S.runs = cstats[2];
     S.kmers = cstats[0];
     S.superkmers = cstats[1];
-    S.distinct = out.distinct;
-    S.out = out.n_out;
+    S.out = j->n_out;
     S.gpu_parts = (uint32_t)B.segs.size();
-    S.fallback_groups = out.fallback_groups;
-    S.groups = out.groups;
-    S.heavy_groups = (uint32_t)out.heavy_groups;
     S.record_bytes = cstats[1] * 8;
     cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]); S.pack_ms = ms;
     cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]); S.phase1_cut_ms = ms;
     S.phase1_scatter_ms = 0;  // records stay in the cut's lists
     S.phase1_ms = S.phase1_cut_ms;
-    cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[8]); S.phase2_ms = ms;
-    cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]); S.phase2_keys_ms = ms;
-    cudaEventElapsedTime(&ms, ctx->ev[7], ctx->ev[8]); S.phase2_count_ms = ms;
     S.gpu_launches = (uint64_t)(launches + j->lex_launches);
     return TG_OK;
 }
@@ -721,6 +829,11 @@ tg_status tg_job_result_copy(tg_job* j, uint64_t* keys, uint32_t* counts, uint64
     if (!j->ran) return ctx->fail(TG_ERR_STATE, "result before run");
     if (first + n > j->n_out) return ctx->fail(TG_ERR_ARG, "result range out of bounds");
     if (!n) return TG_OK;
+    if (j->spilled) {  // phase 2 ran in passes: the pairs are in host memory
+        if (keys) memcpy(keys, j->host_keys.data() + first * j->W, n * 8 * (size_t)j->W);
+        if (counts) memcpy(counts, j->host_counts.data() + first, n * 4);
+        return TG_OK;
+    }
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
     const double t0 = now_ms();
     // jobs of several samples: the sample-major copy (each sample's pairs one range)
@@ -790,10 +903,23 @@ tg_status tg_job_drain(tg_job* j, tg_format fmt, tg_sink_fn sink, void* user) {
     int prev = -1;
     tg_status s = TG_OK;
     const uint64_t nb = (n + B - 1) / B;
+    if (j->spilled) {  // pairs in host memory: each batch is copied back to the device first
+        CK(ctx->ensure(ctx->okeys, B * key_bytes(W)), "alloc");
+        CK(ctx->ensure(ctx->ocnt, B * 4), "alloc");
+        keys = ctx->okeys.as<uint64_t>();
+        counts = ctx->ocnt.as<uint32_t>();
+    }
     for (uint64_t b = 0; b < nb && s == TG_OK; ++b) {
         const uint64_t first = b * B, m = std::min(B, n - first);
+        const uint64_t off = j->spilled ? 0 : first;
+        if (j->spilled) {
+            CK(cudaMemcpyAsync(ctx->okeys.p, j->host_keys.data() + first * W, m * key_bytes(W),
+                               cudaMemcpyHostToDevice, ctx->st), "h2d");
+            CK(cudaMemcpyAsync(ctx->ocnt.p, j->host_counts.data() + first, m * 4, cudaMemcpyHostToDevice, ctx->st),
+               "h2d");
+        }
         // the copy of batch b - 1 out of fbuf is ahead of this on the stream
-        CK(launch_format((int)fmt, k, keys + first * W, counts + first, m, ctx->fbuf.as<uint8_t>(), ctx->fscr.p,
+        CK(launch_format((int)fmt, k, keys + off * W, counts + off, m, ctx->fbuf.as<uint8_t>(), ctx->fscr.p,
                          ctx->n_sm, ctx->st, d_total, &launches),
            "format");
         CK(cudaStreamSynchronize(ctx->st), "format");
@@ -963,6 +1089,10 @@ static tg_status count_host(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_sam
     // several samples: the pairs are reordered sample-major at the end, so they
     // are copied once the run is over
     j->overlap = multi ? nullptr : &ov;
+    // a run in passes (memory budget) copies each pass's pairs here itself
+    j->sink_keys = keys;
+    j->sink_counts = counts;
+    j->sink_cap = cap;
     if (s == TG_OK) s = tg_job_run(j);
     if (s == TG_OK && multi) {
         const uint64_t h = std::min<uint64_t>(j->n_out, cap);

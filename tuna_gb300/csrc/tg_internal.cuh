@@ -131,6 +131,7 @@ struct KeysParams {
     Group* groups[2];                  // [0] normal, [1] heavy
     uint64_t groups_cap;
     unsigned long long* ctr;           // P2Counter
+    uint32_t bin_lo, bin_hi;           // k_keys: only records of bins in [bin_lo, bin_hi)
 };
 
 struct CountParams {

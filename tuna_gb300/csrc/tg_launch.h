@@ -74,6 +74,9 @@ struct P2Input {
     uint64_t n_kmers;                  // k-mer instances in all
     uint64_t ci, cx;
     uint32_t n_samples = 1;
+    // the bins counted by this run (all by default); segs must lie inside and
+    // n_kmers count only their keys
+    uint32_t bin_lo = 0, bin_hi = 1u << BIN_BITS;
 };
 struct P2Output {
     void* keys;                        // u64 x W per distinct k-mer

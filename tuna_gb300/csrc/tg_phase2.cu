@@ -217,20 +217,36 @@ __global__ void __launch_bounds__(PLAN_THREADS) k_plan(KeysParams P) {
 // its k-mers' places with one global atomic on its bin cursor, then the
 // warp's lanes take the batch's k-mers in order (consecutive lanes,
 // consecutive keys).
+//
+// A run restricted to a range of bins (the passes of a job larger than the
+// memory budget) keeps only the records of those bins, moved to the front of
+// the warp's batch so that every active lane still holds one record.
 template <int W>
 __global__ void __launch_bounds__(P2_THREADS) k_keys(KeysParams P) {
     using O = KeyOps<W>;
+    __shared__ uint64_t s_keep[P2_THREADS];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const Slice sl = P.slices[blockIdx.x];
     const uint64_t* d = P.desc + sl.r_lo;
     const uint32_t n = (uint32_t)(sl.r_hi - sl.r_lo);
     const int k = P.k;
+    const bool filt = P.bin_lo != 0 || P.bin_hi != (1u << BIN_BITS);
     uint64_t dnext = (uint32_t)wid * 32 + lane < n ? d[(uint32_t)wid * 32 + lane] : 0;
     for (uint32_t base = (uint32_t)wid * 32; base < n; base += P2_THREADS) {
-        const uint64_t dv = dnext;  // this batch; the next one is loaded while it is processed
+        uint64_t dv = dnext;  // this batch; the next one is loaded while it is processed
         {
             const uint32_t i = base + P2_THREADS + lane;
             dnext = i < n ? d[i] : 0;
+        }
+        if (filt) {
+            const uint32_t b = desc_bin(dv);
+            const bool keep = desc_nk(dv) && b >= P.bin_lo && b < P.bin_hi;
+            const unsigned m = __ballot_sync(0xffffffffu, keep);
+            if (keep) s_keep[wid * 32 + __popc(m & ((1u << lane) - 1u))] = dv;
+            __syncwarp();
+            dv = lane < __popc(m) ? s_keep[wid * 32 + lane] : 0;
+            __syncwarp();
+            if (m == 0) continue;
         }
         const uint32_t nk = desc_nk(dv);  // 0 past the slice; at least 1 otherwise
         unsigned long long koff = 0;
@@ -855,8 +871,10 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
         P2_CK(cudaMemcpyAsync(R.slices, L.slices.data(), L.n_slices * sizeof(Slice), cudaMemcpyHostToDevice, st),
               "h2d");
     P2_CK(cudaMemcpyAsync(R.segs, in.segs, (size_t)in.n_segs * sizeof(Segment), cudaMemcpyHostToDevice, st), "h2d");
-    // k-mer counts per bin -> first key of each bin
-    P2_CK(launch_scan(in.binhist, NBIN_ALL, R.kofs, R.sums, R.kofs + NBIN_ALL, st, launches), "scan");
+    // k-mer counts per bin -> first key of each bin (of this run's bins)
+    P2_CK(launch_scan(in.binhist + in.bin_lo, in.bin_hi - in.bin_lo, R.kofs + in.bin_lo, R.sums, R.kofs + in.bin_hi,
+                      st, launches),
+          "scan");
 
     KeysParams K{};
     K.packed = in.packed;
@@ -872,6 +890,8 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
     K.groups[1] = R.heavy;
     K.groups_cap = L.groups_cap;
     K.ctr = R.ctr;
+    K.bin_lo = in.bin_lo;
+    K.bin_hi = in.bin_hi;
     {
         const uint32_t warps = PLAN_THREADS / 32;
         k_plan<<<(in.n_segs + warps - 1) / warps, PLAN_THREADS, 0, st>>>(K);  // before k_keys moves the cursors
