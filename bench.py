@@ -57,6 +57,7 @@ def parse_args():
     ap.add_argument("--no-large-k", action="store_true", help="skip the k=63 reads section")
     ap.add_argument("--large-k-scale", type=float, default=1.0, help="fraction of the 3 Gbp k=63 read set")
     ap.add_argument("--no-gz", action="store_true", help="skip the gzip-input section")
+    ap.add_argument("--no-passes", action="store_true", help="skip the memory-budget (passes) section")
     ap.add_argument("--batch-samples", type=int, default=2000)
     ap.add_argument("--batch-scale", type=float, default=0.004,
                     help="genome sizes of the batched mix: log-uniform 10 kbp - 50 Mbp times this")
@@ -361,6 +362,27 @@ def large_k(ctx, scale: float, steps: int):
                    "pairs to pinned host buffers"}
 
 
+def passes_section(dev, n_stream: int, kmers: int, steps: int):
+    """The 3.1 Gbp job on a context whose memory budget holds a quarter of its
+    phase-2 keys and pairs: phase 2 in passes over ranges of bins, each pass's
+    pairs copied to host memory."""
+    import torch
+    import tuna_gb300 as T
+    per_key = 2 * 8 + 4 + 24
+    budget = kmers * per_key // 4
+    with T.Context(torch.cuda.current_device(), hbm_budget=budget) as c2:
+        r, _ = c2.run(K, M, dev_seq=dev.data_ptr(), dev_len=n_stream, n_parts=NPARTS, want_results=False)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            r, _ = c2.run(K, M, dev_seq=dev.data_ptr(), dev_len=n_stream, n_parts=NPARTS, want_results=False)
+        t = (time.perf_counter() - t0) / steps
+    st = r.stats
+    return {"budget_bytes": budget, "passes": int(st["phase2_passes"]), "ms_per_step": t * 1e3,
+            "gbases_s": n_stream / t / 1e9, "out": int(st["out"]),
+            "phase2_ms": st["phase2_ms"], "d2h_ms": st["d2h_ms"],
+            "api": "tg_ctx_opts.hbm_budget_bytes; device-resident input, every pass's pairs copied to host memory"}
+
+
 def gz_input(fasta: np.ndarray, mbytes: float = 300.0):
     """Reading gzip input on the host (tg_read_input): a BGZF file inflated on
     1 and on all host threads, and the same bytes as one gzip member (one
@@ -634,6 +656,9 @@ def main():
     output = None
     if rank == 0 and not args.no_output:
         output = output_drain(ctx, dev, n_stream)
+    passes = None
+    if rank == 0 and not args.no_passes:
+        passes = passes_section(dev, n_stream, int(st["kmers"]), 2)
     del dev
     large = None
     if rank == 0 and not args.no_large_k:
@@ -675,6 +700,7 @@ def main():
             "parity": parity_full,
             "output": output,
             "gz": gz,
+            "passes": passes,
             "large_k": large,
             "batched": batched,
             "serve": serve,
