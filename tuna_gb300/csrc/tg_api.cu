@@ -105,6 +105,7 @@ struct tg_ctx {
         misc, fbtab, tables, raw, lexs, fbuf, fscr;
     uint8_t* fhost[2] = {nullptr, nullptr};  // pinned host buffers of the output drain
     size_t fhost_cap = 0;
+    uint8_t* stage[2] = {nullptr, nullptr};  // pinned staging of copies to pageable host memory
     cudaEvent_t ev[12] = {};
     // results copied to the host while counting runs (tg_count_seq)
     cudaStream_t st_copy = nullptr;
@@ -158,8 +159,8 @@ struct tg_job {
     // phase 2 in passes (memory budget): the pairs are in host memory, either
     // the caller's buffers (sink_*, the one-call entry points) or host_keys/_counts
     bool spilled = false;
-    std::vector<uint64_t> host_keys;
-    std::vector<uint32_t> host_counts;
+    std::vector<uint64_t, tgh::NoInitAlloc<uint64_t>> host_keys;
+    std::vector<uint32_t, tgh::NoInitAlloc<uint32_t>> host_counts;
     uint64_t* sink_keys = nullptr;
     uint32_t* sink_counts = nullptr;
     uint64_t sink_cap = 0;
@@ -234,6 +235,8 @@ tg_status tg_ctx_destroy(tg_ctx* ctx) {
     }
     if (ctx->wave_out) cudaFreeHost(ctx->wave_out);
     for (uint8_t* h : ctx->fhost)
+        if (h) cudaFreeHost(h);
+    for (uint8_t* h : ctx->stage)
         if (h) cudaFreeHost(h);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
@@ -574,6 +577,40 @@ static tg_status run_cut(tg_job* j, bool exp, uint32_t p1_bits, int* launches, c
     return ctx->fail(TG_ERR_DEVICE, "descriptor capacity exceeded");
 }
 
+// Device memory to pageable host memory at the host link's rate: chunks are
+// copied into the context's two pinned staging buffers in turn, and the host
+// moves each one out with several threads while the next is copied.
+static tg_status d2h_pageable(tg_ctx* ctx, void* dst, const void* src, size_t bytes) {
+    constexpr size_t CH = 64u << 20;
+    for (uint8_t*& b : ctx->stage)
+        if (!b) CK(cudaHostAlloc(reinterpret_cast<void**>(&b), CH, cudaHostAllocDefault), "alloc pinned staging");
+    const size_t n_ch = (bytes + CH - 1) / CH;
+    const unsigned nt = std::max(1u, std::min(ctx->host_threads, 16u));
+    auto issue = [&](size_t c) -> cudaError_t {
+        const size_t off = c * CH, len = std::min(CH, bytes - off);
+        cudaError_t e = cudaMemcpyAsync(ctx->stage[c & 1], static_cast<const uint8_t*>(src) + off, len,
+                                        cudaMemcpyDeviceToHost, ctx->st);
+        if (e == cudaSuccess) e = cudaEventRecord(ctx->ev[4 + (c & 1)], ctx->st);
+        return e;
+    };
+    if (n_ch) CK(issue(0), "d2h");
+    for (size_t c = 0; c < n_ch; ++c) {
+        if (c + 1 < n_ch) CK(issue(c + 1), "d2h");  // the other buffer was emptied in the previous step
+        CK(cudaEventSynchronize(ctx->ev[4 + (c & 1)]), "d2h");
+        const size_t off = c * CH, len = std::min(CH, bytes - off);
+        const size_t per = (len + nt - 1) / nt;
+        std::vector<std::thread> th;
+        for (unsigned t = 1; t < nt; ++t)
+            th.emplace_back([&, t] {
+                const size_t a = std::min(len, t * per), b = std::min(len, a + per);
+                if (b > a) memcpy(static_cast<uint8_t*>(dst) + off + a, ctx->stage[c & 1] + a, b - a);
+            });
+        memcpy(static_cast<uint8_t*>(dst) + off, ctx->stage[c & 1], std::min(len, per));
+        for (auto& t : th) t.join();
+    }
+    return TG_OK;
+}
+
 tg_status tg_job_run(tg_job* j) {
     if (!j) return TG_ERR_ARG;
     tg_ctx* ctx = j->ctx;
@@ -757,6 +794,10 @@ tg_status tg_job_run(tg_job* j) {
         j->spilled = true;
         j->host_keys.clear();
         j->host_counts.clear();
+        if (!(j->sink_keys || j->sink_counts)) {  // at most one pair per k-mer: no reallocation between passes
+            j->host_keys.reserve(n_kmers * W);
+            j->host_counts.reserve(n_kmers);
+        }
         uint64_t acc = 0;
         const double t0 = now_ms();
         for (size_t p = 0; p < passes.size(); ++p) {
@@ -783,9 +824,9 @@ tg_status tg_job_run(tg_job* j) {
             } else if (n_p) {
                 j->host_keys.resize((acc + n_p) * W);
                 j->host_counts.resize(acc + n_p);
-                CK(cudaMemcpy(j->host_keys.data() + acc * W, po.keys, n_p * key_bytes(W), cudaMemcpyDeviceToHost),
-                   "d2h");
-                CK(cudaMemcpy(j->host_counts.data() + acc, po.counts, n_p * 4, cudaMemcpyDeviceToHost), "d2h");
+                tg_status cs = d2h_pageable(ctx, j->host_keys.data() + acc * W, po.keys, n_p * key_bytes(W));
+                if (cs == TG_OK) cs = d2h_pageable(ctx, j->host_counts.data() + acc, po.counts, n_p * 4);
+                if (cs != TG_OK) return cs;
             }
             S.d2h_ms += now_ms() - c0;
             acc += n_p;
