@@ -54,3 +54,28 @@ def test_passes_one_call_and_filter():
     got = T.Result(keys[: n.value].reshape(-1, 1), cnt[: n.value], {}, 31).sorted()
     w = want.sorted()
     assert np.array_equal(got.keys, w.keys) and np.array_equal(got.counts, w.counts)
+
+
+def _checksum(res) -> tuple:
+    """Order-independent digest of the (key, count) pairs."""
+    k = res.keys[:, 0].astype(np.uint64)
+    x = k ^ (res.counts.astype(np.uint64) * np.uint64(0x9E3779B97F4A7C15))
+    x ^= x >> np.uint64(31)
+    x *= np.uint64(0xBF58476D1CE4E5B9)
+    x ^= x >> np.uint64(29)
+    return len(res), int(x.sum(dtype=np.uint64)), int(res.counts.astype(np.uint64).sum())
+
+
+def test_large_job_key_launches_match_passes():
+    """Above 2^28 k-mers k_keys writes the keys in two launches (half of the bins
+    each); passes under a budget stay below that and use one. Same pairs."""
+    import tuna_gb300 as T
+    seq = _stream(9, 300_000_000)
+    with T.Context(0) as big:
+        one, _ = big.run(31, 21, seq=seq)
+        assert one.stats["kmers"] > (1 << 28) and one.stats["phase2_passes"] == 1
+    with T.Context(0, hbm_budget=6 << 30) as small:
+        parts, _ = small.run(31, 21, seq=seq)
+        assert parts.stats["phase2_passes"] >= 2
+    assert _checksum(one) == _checksum(parts)
+    assert _checksum(one)[2] == one.stats["kmers"]
