@@ -355,6 +355,7 @@ def large_k(ctx, scale: float, steps: int):
             "device_gbases_s": bases / t_dev / 1e9, "device_ms": t_dev * 1e3,
             "e2e_gbases_s": bases / t_e2e / 1e9, "e2e_ms": t_e2e * 1e3,
             "kmers": int(st["kmers"]), "distinct": int(st["distinct"]), "out": n_out,
+            "group_load_pct": int(st["group_load_pct"]),
             "parts_ms": {f: float(st[f]) for f in ("lex_ms", "pack_ms", "phase1_ms", "phase2_keys_ms",
                                                      "phase2_count_ms")},
             "kff_drain_s": t_kff, "kff_bytes": tot[0],
@@ -515,7 +516,7 @@ def main():
 
     stream_h, bases, lens, fasta_h = workload(args.scale, want_fasta=not args.no_e2e)
     dev = torch.from_numpy(stream_h).to(f"cuda:{local}")
-    ctx = T.Context(local)
+    ctx = T.Context(local, autotune=True)  # the first warm-up step times the group sizes
     ext = torch.cuda.ExternalStream(ctx.stream_ptr, device=f"cuda:{local}")
     torch.cuda.synchronize()
 
@@ -685,6 +686,8 @@ def main():
             "config": {"workload": f"{bases / 1e9:.2f} Gbp repetitive assembly, 24 contigs, k=31 m=23 n=4096",
                        "k": K, "m": M, "n_parts": NPARTS, "bases": bases, "stream_bytes": n_stream,
                        "gpu_parts": int(st["gpu_parts"]), "l2": "inputs larger than L2 (3.1 GB), no flush",
+                       "group_load_pct": int(st["group_load_pct"]),
+                       "autotune": "TG_CTX_AUTOTUNE: group size timed on the first warm-up step (35/50/65 % of the table)",
                        "parallelism": f"replicas x{world}"},
             "stats": {"kmers": int(st["kmers"]), "superkmers": int(st["superkmers"]),
                       "distinct": int(st["distinct"]), "fallback_groups": int(st["fallback_groups"])},

@@ -70,8 +70,15 @@ typedef struct {
                                    not fit is counted in passes over ranges of bins, each pass's
                                    pairs copied to host memory (results then stay on the host) */
     uint32_t host_threads;      /* host parser / formatter threads; 0 = all cores */
-    uint32_t flags;             /* reserved, 0 */
+    uint32_t flags;             /* TG_CTX_* bits */
 } tg_ctx_opts;
+
+/* tg_ctx_opts.flags: the first job of each key width (k <= 31, k >= 32) with at
+ * least 2^26 k-mers times its counting pass with several group sizes (the load
+ * of the shared-memory table when a group's keys are all distinct) on its own
+ * keys and keeps the fastest for itself and every later job of the context
+ * (tg_stats.group_load_pct). Without it the group size is half the table. */
+#define TG_CTX_AUTOTUNE 1u
 
 typedef struct {
     uint16_t k;          /* 2..63 on this path */
@@ -112,6 +119,8 @@ typedef struct {
     uint64_t host_parsed_bytes; /* of those, bytes parsed on the host (see tg_job_feed_fastx) */
     uint64_t phase2_passes;   /* phase-2 passes over ranges of bins (more than 1 when the keys and
                                  pairs of a job exceed the context's memory budget, hbm_budget_bytes) */
+    uint32_t group_load_pct;  /* keys per counting group, % of the shared-memory table's slots */
+    uint32_t autotune_trials; /* counting passes this job timed for TG_CTX_AUTOTUNE */
 } tg_stats;
 
 /* Output formats of tg_job_drain. */

@@ -60,7 +60,8 @@ class _Stats(ctypes.Structure):
                 ("record_bytes", ctypes.c_uint64), ("gpu_launches", ctypes.c_uint64),
                 ("phase2_count_ms", ctypes.c_double), ("phase2_keys_ms", ctypes.c_double),
                 ("groups", ctypes.c_uint64), ("lex_ms", ctypes.c_double), ("fastx_bytes", ctypes.c_uint64),
-                ("host_parsed_bytes", ctypes.c_uint64), ("phase2_passes", ctypes.c_uint64)]
+                ("host_parsed_bytes", ctypes.c_uint64), ("phase2_passes", ctypes.c_uint64),
+                ("group_load_pct", ctypes.c_uint32), ("autotune_trials", ctypes.c_uint32)]
 
     def as_dict(self) -> Dict[str, float]:
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -207,15 +208,16 @@ class Context:
     """One device context (tg_ctx): a stream and grow-only device buffers that
     consecutive jobs reuse."""
 
-    def __init__(self, device: int = 0, host_threads: int = 0, hbm_budget: int = 0):
+    def __init__(self, device: int = 0, host_threads: int = 0, hbm_budget: int = 0, autotune: bool = False):
         """hbm_budget: device bytes phase 2 may hold at once (0 = free HBM minus
         a reserve); a job whose keys and pairs exceed it runs in passes over
-        ranges of bins."""
+        ranges of bins. autotune: TG_CTX_AUTOTUNE (group size timed on the
+        first large job of each key width)."""
         L = library()
         if L.tg_device_count() <= device:
             raise GpuError(2, "no CUDA device available for the GPU k-mer counter")
         self._L = L
-        o = _CtxOpts(device, hbm_budget, host_threads, 0)
+        o = _CtxOpts(device, hbm_budget, host_threads, 1 if autotune else 0)
         h = ctypes.c_void_p()
         rc = L.tg_ctx_create(ctypes.byref(o), ctypes.byref(h))
         if rc != 0:

@@ -98,6 +98,8 @@ struct tg_ctx {
     cudaStream_t st = nullptr;
     int n_sm = 0;
     uint64_t hbm_budget = 0;  // tg_ctx_opts.hbm_budget_bytes
+    uint32_t flags = 0;       // tg_ctx_opts.flags
+    uint32_t tuned_pct[2] = {0, 0};  // TG_CTX_AUTOTUNE: group size chosen per key width (0: not yet)
     size_t smem_optin = 0;
     unsigned host_threads = 1;
     std::string err;
@@ -194,6 +196,7 @@ tg_status tg_ctx_create(const tg_ctx_opts* opts, tg_ctx** out) {
     tg_ctx* ctx = new tg_ctx();
     ctx->device = o.device;
     ctx->hbm_budget = o.hbm_budget_bytes;
+    ctx->flags = o.flags;
     ctx->host_threads = o.host_threads ? o.host_threads : std::max(1u, std::thread::hardware_concurrency());
     cudaError_t e = cudaSetDevice(o.device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking);
@@ -743,8 +746,6 @@ tg_status tg_job_run(tg_job* j) {
             CK(ctx->ensure(ctx->ocnt2, out_cap * 4), "alloc output counts");
             CK(ctx->ensure(ctx->osoff, 8 * ((size_t)ns + 1)), "alloc sample offsets");
         }
-        const size_t p2_bytes = phase2_scratch_bytes(in);
-        CK(ctx->ensure(ctx->scratch, p2_bytes), "alloc phase-2 scratch");
         out.keys = ctx->okeys.p;
         out.counts = ctx->ocnt.as<uint32_t>();
         out.samples = ns > 1 ? ctx->osamp.as<uint32_t>() : nullptr;
@@ -755,6 +756,34 @@ tg_status tg_job_run(tg_job* j) {
             out.sample_off = ctx->osoff.as<unsigned long long>();
         }
         out.cap = out_cap;
+        // group size: the context's tuned one, else half the table; with
+        // TG_CTX_AUTOTUNE the first large job of a key width times the counting
+        // pass at each candidate on its own keys and keeps the fastest
+        uint32_t pct = ctx->tuned_pct[W - 1] ? ctx->tuned_pct[W - 1] : 50;
+        if ((ctx->flags & TG_CTX_AUTOTUNE) && !ctx->tuned_pct[W - 1] && n_kmers >= (1ull << 26)) {
+            static const uint32_t cand[] = {35, 50, 65};
+            float best = 0;
+            for (uint32_t cp : cand) {
+                P2Input ti = in;
+                ti.group_pct = cp;
+                const size_t tb = phase2_scratch_bytes(ti);
+                CK(ctx->ensure(ctx->scratch, tb), "alloc phase-2 scratch");
+                P2Output to = out;
+                const tg_status ts = phase2_run(ti, ctx->scratch.p, tb, to, fallback_table, ctx->st, ctx->ev[7],
+                                                &launches, msg, P2Overlap());
+                if (ts != TG_OK) return ctx->fail(ts, msg);
+                CK(cudaEventRecord(ctx->ev[8], ctx->st), "event");
+                CK(cudaEventSynchronize(ctx->ev[8]), "sync");
+                cudaEventElapsedTime(&ms, ctx->ev[7], ctx->ev[8]);  // the counting pass (keys come before ev[7])
+                if (S.autotune_trials == 0 || ms < best) { best = ms; pct = cp; }
+                ++S.autotune_trials;
+            }
+            ctx->tuned_pct[W - 1] = pct;
+        }
+        in.group_pct = pct;
+        S.group_load_pct = pct;
+        const size_t p2_bytes = phase2_scratch_bytes(in);
+        CK(ctx->ensure(ctx->scratch, p2_bytes), "alloc phase-2 scratch");
         CK(cudaEventRecord(ctx->ev[6], ctx->st), "event");
         const tg_status ps = phase2_run(in, ctx->scratch.p, p2_bytes, out, fallback_table, ctx->st, ctx->ev[7],
                                         &launches, msg, j->overlap ? *j->overlap : P2Overlap());
@@ -773,6 +802,8 @@ tg_status tg_job_run(tg_job* j) {
     } else {
         // sizes of the largest pass
         uint64_t max_keys = 0;
+        in.group_pct = ctx->tuned_pct[W - 1] ? ctx->tuned_pct[W - 1] : 50;
+        S.group_load_pct = in.group_pct;
         std::vector<P2Input> pin(passes.size(), in);
         size_t p2_bytes = 0;
         for (size_t p = 0; p < passes.size(); ++p) {

@@ -77,6 +77,7 @@ struct P2Input {
     // the bins counted by this run (all by default); segs must lie inside and
     // n_kmers count only their keys
     uint32_t bin_lo = 0, bin_hi = 1u << BIN_BITS;
+    uint32_t group_pct = 50;  // keys per group, % of the table's slots
 };
 struct P2Output {
     void* keys;                        // u64 x W per distinct k-mer

@@ -775,7 +775,7 @@ P2Plan make_plan(const P2Input& in) {
     L.n_slices = L.slices.size();
     // a segment of K keys has fewer than 2 K / target + 1 groups (two neighbouring
     // groups of k_plan hold more than `target` keys together)
-    const uint64_t target = count_slots(in.W) * 5 / 10;
+    const uint64_t target = std::max<uint64_t>(1, (uint64_t)count_slots(in.W) * in.group_pct / 100);
     L.groups_cap = 2 * in.n_kmers / target + in.n_segs + 1;
     L.retry_cap = std::max<uint64_t>(4096, 2 * L.groups_cap);
     L.n_keys_alloc = in.n_kmers + 1;
@@ -929,7 +929,7 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
     K.kofs = R.kofs;
     K.segs = R.segs;
     K.n_segs = in.n_segs;
-    K.target = slots * 5 / 10;  // as in make_plan
+    K.target = std::max<uint32_t>(1, slots * in.group_pct / 100);  // as in make_plan
     K.k = in.k;
     K.keys = R.keys;
     K.groups[0] = R.normal;

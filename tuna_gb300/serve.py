@@ -122,7 +122,7 @@ class Server:
 
     def _work(self, device: int, host_threads: int) -> None:
         T, L = self._T, self._L
-        ctx = T.Context(device, host_threads)
+        ctx = T.Context(device, host_threads, autotune=True)
         try:
             while True:
                 with self._cv:
