@@ -57,6 +57,7 @@ def parse_args():
     ap.add_argument("--no-large-k", action="store_true", help="skip the k=63 reads section")
     ap.add_argument("--large-k-scale", type=float, default=1.0, help="fraction of the 3 Gbp k=63 read set")
     ap.add_argument("--no-gz", action="store_true", help="skip the gzip-input section")
+    ap.add_argument("--no-small", action="store_true", help="skip the small read-set section")
     ap.add_argument("--no-passes", action="store_true", help="skip the memory-budget (passes) section")
     ap.add_argument("--batch-samples", type=int, default=2000)
     ap.add_argument("--batch-scale", type=float, default=0.004,
@@ -384,6 +385,51 @@ def passes_section(dev, n_stream: int, kmers: int, steps: int):
             "api": "tg_ctx_opts.hbm_budget_bytes; device-resident input, every pass's pairs copied to host memory"}
 
 
+def small_reads(ctx, steps: int):
+    """The small read set: a seeded 4.6 Mbp genome (i.i.d., GC 50 %), 150 bp reads
+    from both strands at 30x (138 Mbp), 0.5 % substitutions, 0.01 % N, as FASTQ;
+    k=31 m=21. End to end from the FASTQ bytes (tg_count_fastx), and the CPU
+    reference path (the oracle port) on the same bytes with all host cores."""
+    import ctypes
+    import torch
+    import tuna_gb300 as T
+    from oracle import oracle as O
+    from tuna_gb300 import synth
+    fq, meta = synth.reads_workload(scale=1.0, seed=1)
+    bases = int(meta["reads"]) * 150
+    L = T.library()
+    h = torch.from_numpy(fq).pin_memory()
+    cap = bases
+    hk = torch.empty(cap, dtype=torch.int64, pin_memory=True)
+    hc = torch.empty(cap, dtype=torch.int32, pin_memory=True)
+    o = T._JobOpts(31, 21, 16, 1, (1 << 64) - 1, 0, 0)
+    n = ctypes.c_uint64()
+    st = T._Stats()
+
+    def step():
+        ctx.check(L.tg_count_fastx(ctx.h, ctypes.byref(o), ctypes.c_void_p(h.data_ptr()), h.numel(),
+                                   ctypes.c_void_p(hk.data_ptr()), ctypes.c_void_p(hc.data_ptr()), cap,
+                                   ctypes.byref(n), ctypes.byref(st)))
+
+    for _ in range(3):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    t = (time.perf_counter() - t0) / steps
+    cores = os.cpu_count() or 1
+    O.count_fastx(fq[:1_000_000], 31, 21, threads=cores)  # load, warm
+    c0 = time.perf_counter()
+    ref = O.count_fastx(fq, 31, 21, threads=cores)
+    tc = time.perf_counter() - c0
+    return {"workload": "4.6 Mbp genome, 920 k reads of 150 bp (30x, both strands), 0.5 % substitutions, "
+                        "0.01 % N, FASTQ; k=31 m=21", "bases": bases, "fastq_bytes": int(fq.size),
+            "e2e_gbases_s": bases / t / 1e9, "e2e_ms": t * 1e3, "distinct": int(n.value),
+            "cpu_port_gbases_s": bases / tc / 1e9, "cpu_port_s": tc, "cpu_cores": cores,
+            "same_distinct": int(n.value) == len(ref),
+            "api": "tg_count_fastx from pinned FASTQ bytes; CPU: the oracle port (tor_count_fastx)"}
+
+
 def gz_input(fasta: np.ndarray, mbytes: float = 300.0):
     """Reading gzip input on the host (tg_read_input): a BGZF file inflated on
     1 and on all host threads, and the same bytes as one gzip member (one
@@ -651,6 +697,9 @@ def main():
     else:
         parity_full = None
 
+    small = None
+    if rank == 0 and not args.no_small:
+        small = small_reads(ctx, args.steps)
     gz = None
     if rank == 0 and not args.no_gz and fasta_h is not None:
         gz = gz_input(fasta_h)
@@ -702,6 +751,7 @@ def main():
             "e2e": e2e,
             "parity": parity_full,
             "output": output,
+            "small_reads": small,
             "gz": gz,
             "passes": passes,
             "large_k": large,
