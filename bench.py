@@ -580,13 +580,12 @@ def main():
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(ext)
     launches = 0
-    kern = {"pack": [], "cut": [], "scatter": [], "keys": [], "count": [], "phase1": [], "phase2": []}
+    kern = {"pack": [], "cut": [], "keys": [], "count": [], "phase1": [], "phase2": []}
     for _ in range(args.steps):
         st = step()
         launches += int(st["gpu_launches"])
         kern["pack"].append(st["pack_ms"])
         kern["cut"].append(st["phase1_cut_ms"])
-        kern["scatter"].append(st["phase1_scatter_ms"])
         kern["keys"].append(st["phase2_keys_ms"])
         kern["count"].append(st["phase2_count_ms"])
         kern["phase1"].append(st["phase1_ms"])
@@ -607,15 +606,13 @@ def main():
     rec_bases = st["kmers"] + recs * (K - 1)
     alg = {
         "cut": n_stream / 4 + n_stream / 8 + 8 * recs,            # packed + validity in, descriptors out
-        "scatter": 16 * recs,                                     # descriptors in, bucket-ordered descriptors out
         "keys": 8 * recs + rec_bases / 4 + 8 * st["kmers"],       # descriptors + record bases in, keys out
         "count": 8 * st["kmers"] + st["out"] * 12,                # keys in, (key, count) out
         "pack": n_stream + n_stream / 4 + n_stream / 8,           # ASCII in, packed + validity out
     }
-    dom = max(("cut", "scatter", "keys", "count", "pack"), key=lambda x: avg[x])
+    dom = max(("cut", "keys", "count", "pack"), key=lambda x: avg[x])
     achieved = alg[dom] / (avg[dom] / 1e3) / 1e9
-    kernel_names = {"cut": "k_cut", "scatter": "k_bucket", "keys": "k_binhist+k_binscan+k_keys",
-                    "count": "k_count", "pack": "k_pack"}
+    kernel_names = {"cut": "k_cut_seq", "keys": "k_scan+k_plan+k_keys", "count": "k_count", "pack": "k_pack"}
     # phase 1 against the reference's algorithmic bytes B1 = N/4 + record bytes (~1.82 B/base)
     ref_record_bytes = 2 * recs + (st["kmers"] + recs * (K - 1)) / 4
     b1 = bases / 4 + ref_record_bytes

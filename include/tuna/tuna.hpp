@@ -13,8 +13,8 @@
 // only (the reference allows concurrent calls, so every reference callback is
 // also correct here). Differences from the reference, by design of this path:
 //   k is in [2, 63] (two 64-bit key words) and m in [1, min(k - 1, 32)];
-//   Options::partitions only names the partition count (the GPU picks its own
-//   internal buckets); Options::ram_gb is not used (the device budget is HBM);
+//   Options::partitions only names the partition count (the GPU bins k-mers its
+//   own way); Options::ram_gb is not used (the device budget is HBM);
 //   Options::device selects the CUDA device.
 //
 // Build: g++ -std=c++17 -I<repo>/include app.cpp -L<dir of libtuna_gpu.so> -ltuna_gpu

@@ -104,7 +104,7 @@ typedef struct {
     uint64_t fallback_groups; /* key ranges counted in a global-memory table */
     double h2d_ms;            /* host->device copy time of the input */
     double pack_ms;           /* device time: 2-bit packing */
-    double phase1_ms;         /* device time: minimizers, superkmers, buckets */
+    double phase1_ms;         /* device time: minimizers, superkmers, bin histogram */
     double phase2_ms;         /* device time: counting, filter, compaction */
     double d2h_ms;            /* device->host time of results (copy / drain) */
     double phase1_cut_ms;     /* part of phase1_ms: the superkmer cut kernel */

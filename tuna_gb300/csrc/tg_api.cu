@@ -3,14 +3,16 @@
 //
 // A job runs, on the context's stream:
 //   k_pack      ASCII stream -> 2-bit codes + validity bits
+//   (k_lex_*    FASTA/FASTQ bytes -> the stream, when fed as files)
 //   k_cut_seq   minimizers, chain starts, forced splits -> record descriptors
-//               per CTA, k-mer instances per (bucket, bin) (one host sync here)
-//   k_scan_*    (bucket, bin) counts -> key offsets
-//   k_plan      groups of whole bins per bucket
+//               per CTA, k-mer instances per bin (one host sync here)
+//   k_scan_*    bin counts -> key offsets
+//   k_plan      groups of whole bins per segment (a run of bins of one sample)
 //   k_keys      every canonical k-mer key at its bin's cursor
 //   k_count     per group: keys into a shared-memory table, ci/cx, compaction
 //               (again for groups split by key hash)
 //   k_fb_*      (rare) key ranges that overflowed shared memory, global tables
+//   k_fmt*      (tg_job_drain / tg_job_write) pairs -> TSV / KFF / raw bytes
 // The export of partition files runs the tile cut k_cut<true> instead, which
 // also yields each record's exact minimizer position.
 #include <cuda_runtime.h>

@@ -26,7 +26,7 @@ constexpr int CUT_TILE = 1024;      // k-mer start positions per tile of the exp
 constexpr int CUT_SPAN = 16384;     // the most positions any cut tile covers (array slack)
 constexpr int CUT_THREADS = 256;
 constexpr int MAX_W = 255;          // w = k - m
-constexpr int P1_MAX = 4096;        // max internal buckets (smem histogram, >= 8 bin bits)
+constexpr int P1_MAX = 4096;        // max segments of bins (gpu_parts), and partitions of the export cut
 constexpr uint32_t NONE32 = 0xFFFFFFFFu;
 
 // Event types of the Phase-1 tile event list.
@@ -90,8 +90,8 @@ struct CutParams {
 };
 
 // Phase 2 works on slices of the phase-1 descriptor lists and on groups: runs
-// of whole minimizer bins of one bucket, whose keys are contiguous in the key
-// array (the keys are laid out bucket-major, bin-major inside a bucket).
+// of whole bins of one segment, whose keys are contiguous in the key array
+// (the keys are laid out bin-major).
 struct Slice {
     uint64_t r_lo, r_hi;  // descriptor range in the phase-1 lists
 };

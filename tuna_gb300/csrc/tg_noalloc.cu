@@ -8,7 +8,7 @@
 // pre-reserved pool), or a latency-critical loop where an allocation would
 // synchronise the device. tg_count_seq_device_noalloc takes the input and the
 // output buffers from the caller and keeps every intermediate array (packed
-// bases, superkmer descriptors, the (bucket, bin) histogram and key offsets,
+// bases, superkmer descriptors, the bin histogram and key offsets,
 // k-mer keys, group lists, fallback table) in one file-scope device array of
 // TG_NOALLOC_SCRATCH_BYTES that the CUDA runtime reserves when the library is
 // loaded on a device and that stays reserved until the process exits.

@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(PLAN_THREADS) k_plan(KeysParams P) {
 // ---------------------------------------------------------------- k_keys
 // Every k-mer of a slice of the phase-1 descriptor lists (in stream order, so
 // the packed bases are read front to back): canonical key written at its
-// (bucket, bin) cursor. A warp takes 32 descriptors at a time; each reserves
+// bin's cursor. A warp takes 32 descriptors at a time; each reserves
 // its k-mers' places with one global atomic on its bin cursor, then the
 // warp's lanes take the batch's k-mers in order (consecutive lanes,
 // consecutive keys).
