@@ -23,7 +23,7 @@ namespace tg {
 
 constexpr int TG_PAD = 32;          // leading invalid bases in packed/valid
 constexpr int CUT_TILE = 1024;      // k-mer start positions per tile of the export cut
-constexpr int CUT_SPAN = 16384;     // the most positions any cut tile covers (array slack)
+constexpr int CUT_SPAN = 32768;     // the most positions any cut tile covers (array slack)
 constexpr int CUT_THREADS = 256;
 constexpr int MAX_W = 255;          // w = k - m
 constexpr int P1_MAX = 4096;        // max segments of bins (gpu_parts), and partitions of the export cut

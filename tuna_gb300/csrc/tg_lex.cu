@@ -339,12 +339,14 @@ __global__ void __launch_bounds__(LEX_THREADS, LEX_CTAS_PER_SM)
             if (na) atomicMax(&s_na, (long long)(c * LEX_CHUNK + threadIdx.x * 64 + 63 - __clzll(na)));
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
+        if (warp == 0) {  // the warps' summaries in order, by a shuffle tree over lanes 0..7
+            LexFn<uint32_t> g = lane < LEX_THREADS / 32 ? s_w[lane] : lex_identity<uint32_t>();
 #pragma unroll
-            for (int i = 0; i < LEX_THREADS / 32; ++i) {
-                const LexFn<uint32_t> g = s_w[i];
-                carry = lex_then(carry, LexFn<ull>{g.e, g.c0, g.c1, g.c2, g.c3});
+            for (int d = 1; d < LEX_THREADS / 32; d <<= 1) {
+                const LexFn<uint32_t> o = lex_shfl_down(g, d);
+                if ((lane & (2 * d - 1)) == 0) g = lex_then(g, o);
             }
+            if (lane == 0) carry = lex_then(carry, LexFn<ull>{g.e, g.c0, g.c1, g.c2, g.c3});
         }
         fence_proxy_async();  // this buffer's reads before the next bulk copy into it
         __syncthreads();      // buffer it & 1 and s_w free for reuse

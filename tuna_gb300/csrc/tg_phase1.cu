@@ -494,7 +494,13 @@ k_cut(CutParams P, const HashTables* __restrict__ gT) {
 // position (for the forced split every L k-mers) and the next cut after its
 // last one, which close the records that cross segments. A record that is open
 // at the tile's end is carried to the next tile.
-constexpr int SEG = 64;
+// 128 positions per thread: a thread walks SEG + w m-mers for SEG k-mers, so
+// longer segments spend less on the window's warm-up (k=31 m=23: 7.43 ->
+// 7.12 ms for 0.93 Gbp; k=63 m=21 reads: 13.35 -> 11.86 ms against 64). The
+// forced split period L = 256 - k stays above SEG for every k <= 63, so a
+// segment holds at most one forced split.
+constexpr int SEG = 128;
+static_assert(SEG * 256 <= CUT_SPAN, "a cut tile must fit the packed arrays' slack");
 
 struct SeqSmem {
     size_t tables, pk, vb, vh, vs, sum, total;
@@ -664,7 +670,7 @@ k_cut_seq(CutParams P, const HashTables* __restrict__ gT) {
 
         // ---- pass 1: walk positions [ps, ps + SEG) (m-mers from ps - 1 on).
         // Positions inside the walk are relative to pb = ps - 1 (32-bit). The
-        // segments start 64 bases apart, so every thread crosses a packed word
+        // segments start SEG bases apart, so every thread crosses a packed word
         // (16 bases) or validity word (32) at the same step: the bases come
         // from register copies of the words, shifted once per step.
         const int64_t ps = t0 + (int64_t)tid * SEG;
