@@ -215,6 +215,12 @@ tg_status tg_count_seq(tg_ctx* ctx, const tg_job_opts* opts, const uint8_t* seq,
 tg_status tg_count_fastx(tg_ctx* ctx, const tg_job_opts* opts, const uint8_t* data, size_t len,
                          uint64_t* keys, uint32_t* counts, uint64_t cap, uint64_t* n_out,
                          tg_stats* stats);
+/* The same from the bytes of n_samples FASTA/FASTQ files in host memory, each
+ * lexed on the device into its own sample (an empty one gives no pairs). */
+tg_status tg_count_batch_fastx(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_samples,
+                               const uint8_t* const* datas, const size_t* lens, uint64_t* keys,
+                               uint32_t* counts, uint64_t* sample_offsets, uint64_t cap, uint64_t* n_out,
+                               tg_stats* stats);
 /* FASTA/FASTQ bytes to the sequence stream on the device, copied back to out
  * (capacity cap; *out_len receives the stream length, TG_ERR_ARG if it does not
  * fit). The stream holds the reference parser's ACGT runs in order, separated

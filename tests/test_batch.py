@@ -102,3 +102,42 @@ def test_export_needs_one_sample():
     with T.Context(0) as ctx:
         with pytest.raises(T.GpuError):
             ctx.run(31, 21, samples=smp, export=True, want_results=False)
+
+
+def test_count_batch_fastx_matches_alone():
+    """tg_count_batch_fastx: FASTA and FASTQ files, one empty, lexed on the device
+    into separate samples; each sample's pairs are its pairs alone."""
+    import ctypes
+    import tuna_gb300 as T
+    from tuna_gb300 import synth
+    files = []
+    for i in range(6):
+        g = synth.genome(30_000 + 10_000 * i, 300 + i, 0.45)
+        if i == 3:
+            files.append(np.zeros(0, dtype=np.uint8))
+        elif i % 2:
+            files.append(synth.fasta(g, [g.size // 2, g.size - g.size // 2]))
+        else:
+            files.append(synth.reads_fastq(g, 300, (100, 250), 0.005, 0.001, 70 + i))
+    L = T.library()
+    ptrs = (ctypes.c_void_p * len(files))(*[f.ctypes.data if f.size else None for f in files])
+    lens = (ctypes.c_size_t * len(files))(*[int(f.size) for f in files])
+    cap = sum(int(f.size) for f in files)
+    keys = np.zeros(cap, dtype=np.uint64)
+    cnt = np.zeros(cap, dtype=np.uint32)
+    off = np.zeros(len(files) + 1, dtype=np.uint64)
+    o = T._JobOpts(31, 21, 16, 1, (1 << 64) - 1, 0, 0)
+    n = ctypes.c_uint64()
+    st = T._Stats()
+    with T.Context(0) as ctx:
+        rc = L.tg_count_batch_fastx(ctx.h, ctypes.byref(o), len(files), ptrs, lens, keys.ctypes.data, cnt.ctypes.data,
+                                    off.ctypes.data, cap, ctypes.byref(n), ctypes.byref(st))
+        assert rc == 0, L.tg_last_error(ctx.h)
+        for i, f in enumerate(files):
+            a, b = int(off[i]), int(off[i + 1])
+            if f.size == 0:
+                assert a == b
+                continue
+            want = ctx.run(31, 21, fastx=f)[0].sorted()
+            got = T.Result(keys[a:b].reshape(-1, 1).copy(), cnt[a:b].copy(), {}, 31).sorted()
+            assert np.array_equal(got.keys, want.keys) and np.array_equal(got.counts, want.counts)

@@ -50,3 +50,25 @@ def test_served_answers_match_alone():
             assert np.array_equal(got.keys, want.keys) and np.array_equal(got.counts, want.counts)
             assert a.latency_s >= 0
     assert max(a.batch for a in answers) >= 1
+
+
+def test_served_fastq_requests_match_alone():
+    """Requests given as FASTQ bytes (lexed on the device, tg_count_batch_fastx),
+    mixed with stream requests of the same k: each answer is the request's
+    result alone."""
+    import tuna_gb300 as T
+    from tuna_gb300 import synth
+    from tuna_gb300.serve import Server
+    reqs = []
+    for i in range(10):
+        g = synth.genome(20_000 + 7_000 * i, 900 + i, 0.45)
+        fq = synth.reads_fastq(g, 200 + 40 * i, (100, 250), 0.005, 0.001, 60 + i)
+        reqs.append((fq, i % 2 == 0))  # even: FASTQ bytes, odd: the parsed stream
+    with Server(0, workers=2) as srv:
+        futs = [srv.submit(fq if fx else synth.fastq_sequence_stream(fq), 31, 21, fastx=fx) for fq, fx in reqs]
+        answers = [f.result(timeout=300) for f in futs]
+    with T.Context(0) as ctx:
+        for (fq, _), a in zip(reqs, answers):
+            want = ctx.run(31, 21, fastx=fq)[0].sorted()
+            got = T.Result(a.keys.copy(), a.counts.copy(), {}, 31).sorted()
+            assert np.array_equal(got.keys, want.keys) and np.array_equal(got.counts, want.counts)

@@ -80,7 +80,7 @@ ABI_SYMBOLS = ["tg_ctx_create", "tg_ctx_destroy", "tg_last_error", "tg_ctx_strea
                "tg_job_result_copy", "tg_job_drain", "tg_job_write", "tg_job_export_partitions", "tg_job_end",
                "tg_count_seq", "tg_count_seq_device_noalloc", "tg_job_next_sample", "tg_job_sample_count",
                "tg_job_sample_offsets", "tg_count_batch", "tg_job_feed_fastx_device", "tg_count_fastx",
-               "tg_fastx_to_stream", "tg_read_input"]
+               "tg_fastx_to_stream", "tg_read_input", "tg_count_batch_fastx"]
 
 
 def library(build_if_missing: bool = True) -> ctypes.CDLL:
@@ -113,6 +113,8 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
                                  ctypes.POINTER(_Stats)]
     L.tg_fastx_to_stream.argtypes = [vp, vp, sz, vp, sz, ctypes.POINTER(sz)]
     L.tg_read_input.argtypes = [ctypes.c_char_p, u32, vp, sz, ctypes.POINTER(sz), ctypes.c_char_p, sz]
+    L.tg_count_batch_fastx.argtypes = [vp, ctypes.POINTER(_JobOpts), u32, ctypes.POINTER(vp), ctypes.POINTER(sz), vp,
+                                       vp, vp, u64, ctypes.POINTER(u64), ctypes.POINTER(_Stats)]
     L.tg_job_run.argtypes = [vp]
     L.tg_job_stats.argtypes = [vp, ctypes.POINTER(_Stats)]
     L.tg_job_result_size.argtypes = [vp]
@@ -139,7 +141,7 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
                "tg_job_feed_fastx", "tg_job_feed_file", "tg_job_run", "tg_job_stats", "tg_job_result_copy",
                "tg_job_drain", "tg_job_write", "tg_job_export_partitions", "tg_job_end", "tg_count_seq",
                "tg_job_next_sample", "tg_job_sample_offsets", "tg_count_batch", "tg_job_feed_fastx_device",
-               "tg_count_fastx", "tg_fastx_to_stream", "tg_read_input"):
+               "tg_count_fastx", "tg_fastx_to_stream", "tg_read_input", "tg_count_batch_fastx"):
         getattr(L, fn).restype = i32
     _lib = L
     return L

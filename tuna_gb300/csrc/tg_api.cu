@@ -1120,7 +1120,12 @@ static tg_status count_host(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_sam
         total += lens[i] + 1;
     }
     if (s == TG_OK && fastx) {
-        s = n_samples == 1 ? lex_append_host(j, seqs[0], lens[0]) : TG_ERR_ARG;
+        // each sample's FASTA/FASTQ bytes lexed on the device into its own sample
+        // (an empty sample stays empty)
+        for (uint32_t i = 0; i < n_samples && s == TG_OK; ++i) {
+            if (i > 0) s = tg_job_next_sample(j);
+            if (s == TG_OK && lens[i]) s = lex_append_host(j, seqs[i], lens[i]);
+        }
     } else if (s == TG_OK && total) {
         const double t0 = now_ms();
         cudaError_t e = cudaSetDevice(ctx->device);
@@ -1199,6 +1204,13 @@ tg_status tg_count_fastx(tg_ctx* ctx, const tg_job_opts* opts, const uint8_t* da
                          uint32_t* counts, uint64_t cap, uint64_t* n_out, tg_stats* stats) {
     if (!data && len) return TG_ERR_ARG;
     return count_host(ctx, opts, 1, &data, &len, keys, counts, nullptr, cap, n_out, stats, true);
+}
+
+tg_status tg_count_batch_fastx(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_samples,
+                               const uint8_t* const* datas, const size_t* lens, uint64_t* keys, uint32_t* counts,
+                               uint64_t* sample_offsets, uint64_t cap, uint64_t* n_out, tg_stats* stats) {
+    if (n_samples == 0) return TG_ERR_ARG;
+    return count_host(ctx, opts, n_samples, datas, lens, keys, counts, sample_offsets, cap, n_out, stats, true);
 }
 
 tg_status tg_count_batch(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_samples, const uint8_t* const* seqs,

@@ -2,10 +2,12 @@
 (tg_count_batch, include/tuna_gpu.h).
 
 A request is one count job: a sequence stream (non-ACGT bytes separate runs,
-as tg_job_feed_seq takes it) and its k, m, ci, cx. Requests are queued as they
-arrive. Each of `workers` worker threads owns a device context (its own CUDA
-stream and device buffers); whenever a worker is free it takes every waiting
-request with the same (k, m, ci, cx) as the oldest one, up to a budget of
+as tg_job_feed_seq takes it) or the bytes of a FASTA/FASTQ file (lexed on the
+device, tg_count_batch_fastx), and its k, m, ci, cx. Requests are queued as
+they arrive. Each of `workers` worker threads owns a device context (its own
+CUDA stream and device buffers); whenever a worker is free it takes every
+waiting request of the same kind with the same (k, m, ci, cx) as the oldest
+one, up to a budget of
 bases sized from the free device memory, and counts them as the samples of one
 job. Requests that arrive while a batch is on the device join a later batch
 as soon as a worker frees up; with two workers two batches are in flight, so
@@ -46,7 +48,7 @@ class Answer:
 @dataclass
 class _Req:
     seq: np.ndarray
-    key: Tuple[int, int, int, int]
+    key: Tuple[int, int, int, int, bool]  # k, m, ci, cx, FASTA/FASTQ bytes
     arrival: float
     future: Future = field(default_factory=Future)
 
@@ -82,9 +84,13 @@ class Server:
             t.start()
 
     # ------------------------------------------------------------------ API
-    def submit(self, seq: np.ndarray, k: int, m: int, ci: int = 1, cx: int = U64_MAX) -> Future:
-        """Queue one count job; the future's result is an Answer."""
-        r = _Req(np.ascontiguousarray(seq, dtype=np.uint8), (k, m, ci, min(cx, U64_MAX)), time.perf_counter())
+    def submit(self, seq: np.ndarray, k: int, m: int, ci: int = 1, cx: int = U64_MAX, fastx: bool = False) -> Future:
+        """Queue one count job; the future's result is an Answer. fastx: seq is
+        the bytes of a FASTA/FASTQ file (lexed on the device), not a stream."""
+        if fastx and np.asarray(seq).size == 0:
+            raise ValueError("Empty file")
+        r = _Req(np.ascontiguousarray(seq, dtype=np.uint8), (k, m, ci, min(cx, U64_MAX), bool(fastx)),
+                 time.perf_counter())
         with self._cv:
             if self._stop:
                 raise RuntimeError("server is closed")
@@ -143,7 +149,7 @@ class Server:
 
     def _run(self, ctx, batch: List[_Req]) -> None:
         T, L = self._T, self._L
-        k, m, ci, cx = batch[0].key
+        k, m, ci, cx, fastx = batch[0].key
         W = 1 if k <= 31 else 2
         n = len(batch)
         ptrs = (ctypes.c_void_p * n)(*[r.seq.ctypes.data if r.seq.size else None for r in batch])
@@ -155,9 +161,10 @@ class Server:
         o = T._JobOpts(k, m, 16, ci, cx, 0, 0)
         n_out = ctypes.c_uint64()
         st = T._Stats()
-        rc = L.tg_count_batch(ctx.h, ctypes.byref(o), n, ptrs, lens, ctypes.c_void_p(keys.ctypes.data),
-                              ctypes.c_void_p(cnt.ctypes.data), ctypes.c_void_p(off.ctypes.data), cap,
-                              ctypes.byref(n_out), ctypes.byref(st))
+        fn = L.tg_count_batch_fastx if fastx else L.tg_count_batch
+        rc = fn(ctx.h, ctypes.byref(o), n, ptrs, lens, ctypes.c_void_p(keys.ctypes.data),
+                ctypes.c_void_p(cnt.ctypes.data), ctypes.c_void_p(off.ctypes.data), cap,
+                ctypes.byref(n_out), ctypes.byref(st))
         ctx.check(rc)
         done = time.perf_counter()
         kk = keys[: int(n_out.value) * W].reshape(-1, W)
