@@ -509,6 +509,24 @@ def served(seconds: float, scale: float):
 
 
 # ------------------------------------------------------------------ reference arm
+def rank_barrier(world: int) -> None:
+    """Barrier across the replicas (no-op for one process)."""
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def rank_max(x: float, world: int, device: str) -> float:
+    """The maximum of x over the replicas: a step's time is the slowest rank's."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args, rank: int):
     if rank != 0:
         return
@@ -548,17 +566,10 @@ def main():
     torch.cuda.set_device(local)
 
     def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+        rank_barrier(world)
 
     def max_over_ranks(x: float) -> float:
-        if world == 1:
-            return x
-        import torch.distributed as dist
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return rank_max(x, world, "cuda")
 
     stream_h, bases, lens, fasta_h = workload(args.scale, want_fasta=not args.no_e2e)
     dev = torch.from_numpy(stream_h).to(f"cuda:{local}")
