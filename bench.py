@@ -107,24 +107,33 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm, mx, reasons = [], None, set()
-        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         with open(self.path) as f:
-            for line in f:
-                parts = [p.strip() for p in line.split(",")]
-                if len(parts) < 9:
-                    continue
-                try:
-                    sm.append(float(parts[1]))
-                    mx = float(parts[2])
-                except ValueError:
-                    continue
-                for nm, v in zip(names[1:], parts[5:9]):
-                    if v.lower() in ("active", "yes", "1"):
-                        reasons.add(nm)
+            out = parse_clock_lines(f)
         os.remove(self.path)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
-                "reasons": sorted(reasons), "samples": len(sm)}
+        return out
+
+
+def parse_clock_lines(lines):
+    """Median SM clock, maximum clock and throttle reasons seen in nvidia-smi
+    samples (ClockSampler.FIELDS, csv, noheader, nounits)."""
+    sm, mx, reasons = [], None, set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for line in lines:
+        parts = [p.strip() for p in line.split(",")]
+        if len(parts) < 9:
+            continue
+        try:
+            clk = float(parts[1])
+            top = float(parts[2])
+        except ValueError:
+            continue
+        sm.append(clk)
+        mx = top
+        for nm, v in zip(names, parts[5:9]):
+            if v.lower() in ("active", "yes", "1"):
+                reasons.add(nm)
+    return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+            "reasons": sorted(reasons), "samples": len(sm)}
 
 
 # ------------------------------------------------------------------ workload

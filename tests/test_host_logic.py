@@ -1,0 +1,42 @@
+"""Host-side logic that needs no GPU: the server's batching policy
+(tuna_gb300.serve.take_batch) and the bench's clock-sample parsing
+(bench.parse_clock_lines), whose throttle reasons decide whether a bench
+number is kept."""
+import os
+import sys
+from collections import deque
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+
+def _req(n, key):
+    from tuna_gb300.serve import _Req
+    return _Req(np.zeros(n, dtype=np.uint8), key, 0.0)
+
+
+def test_take_batch_groups_by_kind_within_budget():
+    from tuna_gb300.serve import take_batch
+    a, b, fq = (31, 21, 1, 2**64 - 1, False), (21, 17, 1, 2**64 - 1, False), (31, 21, 1, 2**64 - 1, True)
+    q = deque([_req(100, a), _req(50, b), _req(300, a), _req(700, a), _req(10, fq), _req(500, a)])
+    batch, rest = take_batch(q, max_bases=1000)
+    assert [r.seq.size for r in batch] == [100, 300, 500]  # 700 would pass the budget; 500 still fits
+    assert [(r.seq.size, r.key) for r in rest] == [(50, b), (700, a), (10, fq)]
+    batch2, rest2 = take_batch(rest, max_bases=10)
+    assert [r.seq.size for r in batch2] == [50]  # the oldest goes whatever its size
+    assert [r.seq.size for r in rest2] == [700, 10]
+    assert take_batch(deque(), 10) == ([], deque())
+
+
+def test_parse_clock_lines():
+    import bench
+    ok = "0, 2070, 2070, 900.5, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active\n"
+    cap = "0, 1980, 2070, 1390.0, 0x0000000000000004, Not Active, Not Active, Not Active, Active\n"
+    hot = "0, 1500, 2070, 1200.0, 0x0000000000000040, Not Active, Active, Not Active, Not Active\n"
+    out = bench.parse_clock_lines([ok, ok, cap, "garbage\n", "0, [N/A], 2070, 1, 0, a, b, c, d\n"])
+    assert out == {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
+    out = bench.parse_clock_lines([hot, ok])
+    assert out["reasons"] == ["hw_thermal_slowdown"] and out["sm_mhz"] == (1500.0 + 2070.0) / 2
+    assert bench.parse_clock_lines([])["sm_mhz"] is None

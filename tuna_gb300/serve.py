@@ -113,17 +113,7 @@ class Server:
 
     # ------------------------------------------------------------------ worker
     def _take(self) -> List[_Req]:
-        """The oldest request and every waiting one with its parameters, up to
-        the base budget (the oldest always goes, whatever its size)."""
-        head = self._q[0]
-        batch, rest, bases = [], deque(), 0
-        for r in self._q:
-            if r.key == head.key and (not batch or bases + r.seq.size <= self.max_batch_bases):
-                batch.append(r)
-                bases += r.seq.size
-            else:
-                rest.append(r)
-        self._q = rest
+        batch, self._q = take_batch(self._q, self.max_batch_bases)
         return batch
 
     def _work(self, device: int, host_threads: int) -> None:
@@ -171,6 +161,24 @@ class Server:
         for i, r in enumerate(batch):
             a, b = int(off[i]), int(off[i + 1])
             r.future.set_result(Answer(kk[a:b], cnt[a:b], r.arrival, done, n))
+
+
+def take_batch(queue, max_bases: int):
+    """The next batch and the requests left waiting: the oldest request and every
+    waiting one of the same kind and parameters, in arrival order, while the
+    batch stays within max_bases bases (the oldest always goes, whatever its
+    size); the others keep their order."""
+    if not queue:
+        return [], deque()
+    head = queue[0]
+    batch, rest, bases = [], deque(), 0
+    for r in queue:
+        if r.key == head.key and (not batch or bases + r.seq.size <= max_bases):
+            batch.append(r)
+            bases += r.seq.size
+        else:
+            rest.append(r)
+    return batch, rest
 
 
 def _free_device_bytes(device: int) -> int:
