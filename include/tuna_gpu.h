@@ -10,7 +10,11 @@
  *                                    src/partition_hash.hpp:259-338
  *   tg_job_begin                     Config (src/Config.hpp:10-26) + the
  *                                    partition count of include/tuna/tuna.hpp:116-119
- *   tg_job_feed_fastx / _file        SeqSource::process (src/seq_source.hpp:190-205)
+ *   tg_job_feed_fastx / _file /      SeqSource::process (src/seq_source.hpp:190-205) and
+ *     _fastx_device                    the helicase parsers (lexed on the device)
+ *   tg_read_input                    the file reading of SeqSource and GzInput
+ *                                    (src/seq_source.hpp:48-141, :196-204)
+ *   tg_fastx_to_stream               the helicase parsers alone (include/helicase_cpp/)
  *   tg_job_feed_seq / _seq_device    the ACTG chunks handed to
  *                                    extract_superkmers_from_actg (src/partition_hash.hpp:48)
  *   tg_job_run                       run<k,m> / run_callback<k,m> phases 1+2
@@ -22,6 +26,11 @@
  *                                    pipeline (src/superkmer_io.hpp:3-19, -tp -kt)
  *   tg_job_stats                     the phase1:/phase2:/superkmers:/unique_kmers:
  *                                    stderr lines (src/pipeline.hpp:174-178)
+ *   tg_count_seq / tg_count_fastx    one call: feed, run_callback, count_to_raw
+ *   tg_count_batch / _batch_fastx,   no counterpart (the reference counts one input
+ *     tg_job_next_sample             set per run): several samples in one pass
+ *   hbm_budget_bytes (phase 2 in     the disk mode of src/pipeline.hpp:186-263
+ *     passes)
  *
  * Conventions: every function returns a tg_status (0 = ok); no exception
  * crosses the ABI; tg_last_error() gives the message of the last failure on a
