@@ -124,6 +124,22 @@ def test_ci_cx_filter(ctx):
         assert T.tsv_blob(got.keys, got.counts, 31) == O.tsv_blob(want), (ci, cx)
 
 
+def test_filter_equals_post_filter(ctx):
+    """-ci/-cx inside the count kernel keep exactly the pairs that filtering the
+    unfiltered output afterwards keeps (the reference applies the bounds as each
+    bin's table is drained, src/count.hpp:270-287)."""
+    import tuna_gb300 as T
+    from tuna_gb300 import synth
+    fq, _ = synth.reads_workload(scale=0.003, seed=21)
+    full, _ = ctx.run(31, 21, fastx=fq)
+    assert len(full) > 0
+    for ci, cx in [(2, 40), (1, 1), (4, U64_MAX), (7, 9)]:
+        got, _ = ctx.run(31, 21, fastx=fq, ci=ci, cx=cx)
+        keep = (full.counts >= ci) & (full.counts.astype(np.uint64) <= np.uint64(cx))
+        assert T.tsv_blob(got.keys, got.counts, 31) == \
+            T.tsv_blob(full.keys[keep], full.counts[keep], 31), (ci, cx)
+
+
 def test_empty_and_separator_only(ctx):
     r, _ = ctx.run(31, 21, seq=b"NNNN\n\n\r")
     assert len(r) == 0
