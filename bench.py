@@ -7,8 +7,9 @@ GC 41%, 45% of the sequence from 300 bp / 6 kbp repeat families at 10-20%
 divergence, 3% microsatellites — the largest single-GPU workload of the
 benchmark set. Inputs (3.1 GB) are larger than L2, so no flush is needed.
 
-  value   Gbases/s with the input already resident in HBM: k_pack -> k_cut ->
-          scans -> k_scatter -> k_count, results left on the device
+  value   Gbases/s with the input already resident in HBM: k_pack -> k_cut_seq
+          -> k_scan -> k_plan -> k_keys -> k_count, results left on the device
+          (stats also give distinct k-mers/s and k-mer updates/s)
   e2e     the same through the public C ABI from the FASTA file's bytes
           (tg_count_fastx) with pinned host buffers: H2D of the FASTA, lexing
           on the device, both phases, D2H of every counted (k-mer, count) pair;
@@ -756,7 +757,9 @@ def main():
                        "autotune": "TG_CTX_AUTOTUNE: group size timed on the first warm-up step (35/50/65 % of the table)",
                        "parallelism": f"replicas x{world}"},
             "stats": {"kmers": int(st["kmers"]), "superkmers": int(st["superkmers"]),
-                      "distinct": int(st["distinct"]), "fallback_groups": int(st["fallback_groups"])},
+                      "distinct": int(st["distinct"]), "fallback_groups": int(st["fallback_groups"]),
+                      "distinct_kmers_per_s": int(st["distinct"]) / (ms / 1e3),
+                      "kmer_updates_per_s": int(st["kmers"]) / (ms / 1e3)},
             "kernels_ms": {kernel_names.get(k2, k2): round(v, 4) for k2, v in avg.items()},
             "roofline": {"bound": "hbm", "kernel": kernel_names[dom],
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
