@@ -18,8 +18,8 @@ benchmark set. Inputs (3.1 GB) are larger than L2, so no flush is needed.
   cpu_baseline  the CPU oracle (a port of the reference path) on a bounded
           sample of the same workload, all host cores
 
---impl reference times the CPU port alone (the reference sources do not exist
-on the GPU box) and prints the same line with "impl": "reference".
+--impl reference times the CPU port alone (the reference's own sources and
+binaries are not present where the bench runs) and prints the same line with "impl": "reference".
 Multi-GPU (--gpus N under torchrun): replicas, each rank counts its own copy.
 """
 from __future__ import annotations

@@ -1,7 +1,7 @@
 """ctypes front end of the CPU oracle (oracle/tuna_oracle.c).
 
 Test infrastructure, not the product: tests/, __graft_entry__.smoke() and the
-CPU-baseline leg of bench.py use it as the checker. It restates the reference
+CPU-baseline leg of bench.py use it to verify and to time. It restates the reference
 tuna counting path (see tuna_oracle.h for the file:line map) and is pinned
 against the reference's own outputs in tests/golden/.
 """

@@ -1,8 +1,8 @@
 /*
  * tuna_oracle.c — CPU restatement of the reference tuna counting path.
  *
- * TEST INFRASTRUCTURE, NOT THE PRODUCT: the checker for the GPU library and
- * the CPU baseline that bench.py times. See tuna_oracle.h for the map from each
+ * TEST INFRASTRUCTURE, NOT THE PRODUCT: what the GPU library's results are
+ * compared with, and the CPU baseline that bench.py times. See tuna_oracle.h for the map from each
  * stage to the reference file it follows. The restatement is pinned against the
  * reference's own binaries (oracle/build_ref.sh) and the fixtures they produced
  * (tests/golden/).

@@ -2,8 +2,8 @@
  * tuna_oracle.h — CPU restatement of the reference tuna counting path.
  *
  * TEST INFRASTRUCTURE, NOT THE PRODUCT. Only tests/, __graft_entry__.smoke()
- * and bench.py's CPU-baseline leg load this library, and only as the checker
- * (or as the timed CPU baseline). The GPU library never links or calls it.
+ * and bench.py's CPU-baseline leg load this library, and only to verify
+ * results (or as the timed CPU baseline). The GPU library never links or calls it.
  *
  * Every stage follows one function of the reference (paths are relative to
  * the reference project root):

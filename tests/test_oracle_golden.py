@@ -1,6 +1,6 @@
 """The CPU oracle against the reference's own outputs (tests/golden/).
 
-The oracle is the checker of every GPU parity test, so it is pinned here
+Every GPU parity test compares against the oracle, so it is pinned here
 first: same sorted (k-mer, count) lines, same superkmer count, and the same
 Phase 1 partition contents (record multisets) as the reference binaries.
 """
