@@ -31,6 +31,9 @@
  *     tg_job_next_sample             set per run): several samples in one pass
  *   hbm_budget_bytes (phase 2 in     the disk mode of src/pipeline.hpp:186-263
  *     passes)
+ *   tg_job_set_shard                 the partitions one worker takes in phase 2
+ *                                    (src/count.hpp:322-336), as a static share per
+ *                                    device: the partition -> device map
  *
  * Conventions: every function returns a tg_status (0 = ok); no exception
  * crosses the ABI; tg_last_error() gives the message of the last failure on a
@@ -210,6 +213,21 @@ tg_status tg_job_end(tg_job* job);
 tg_status tg_job_next_sample(tg_job* job);
 uint32_t tg_job_sample_count(const tg_job* job);
 tg_status tg_job_sample_offsets(tg_job* job, uint64_t* offsets);
+
+/* ---- shards: one job's partitions spread over devices ---------------------
+ * Every instance of a canonical k-mer has the same minimizer, so the same bin
+ * (partition): the pairs of different bins are disjoint. A job set to shard s
+ * of n runs Phase 1 over its whole input and Phase 2 over the s-th of n equal
+ * runs of consecutive bins only; its result is that shard's pairs, and the n
+ * shards' results together are exactly the job's result. Device d of n counting
+ * shard d of the same input is the partition -> device map of a multi-device
+ * job, with no exchange between devices. n is a power of two, at most
+ * TG_MAX_SHARDS (and at most tg_job_opts.gpu_parts when that is set); a job of
+ * several samples cannot be sharded (TG_ERR_UNSUPPORTED from tg_job_run).
+ * Call before tg_job_run. tg_stats.kmers, superkmers and bases describe the
+ * whole input; distinct and out the shard. */
+#define TG_MAX_SHARDS 1024u
+tg_status tg_job_set_shard(tg_job* job, uint32_t shard, uint32_t n_shards);
 
 /* ---- one-call helpers --------------------------------------------------- */
 /* Count a host sequence stream end to end: H2D, both phases, D2H of the

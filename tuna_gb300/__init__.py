@@ -80,7 +80,7 @@ ABI_SYMBOLS = ["tg_ctx_create", "tg_ctx_destroy", "tg_last_error", "tg_ctx_strea
                "tg_job_result_copy", "tg_job_drain", "tg_job_write", "tg_job_export_partitions", "tg_job_end",
                "tg_count_seq", "tg_count_seq_device_noalloc", "tg_job_next_sample", "tg_job_sample_count",
                "tg_job_sample_offsets", "tg_count_batch", "tg_job_feed_fastx_device", "tg_count_fastx",
-               "tg_fastx_to_stream", "tg_read_input", "tg_count_batch_fastx"]
+               "tg_fastx_to_stream", "tg_read_input", "tg_count_batch_fastx", "tg_job_set_shard"]
 
 
 def library(build_if_missing: bool = True) -> ctypes.CDLL:
@@ -135,13 +135,15 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
     L.tg_job_sample_count.argtypes = [vp]
     L.tg_job_sample_count.restype = u32
     L.tg_job_sample_offsets.argtypes = [vp, vp]
+    L.tg_job_set_shard.argtypes = [vp, u32, u32]
     L.tg_count_batch.argtypes = [vp, ctypes.POINTER(_JobOpts), u32, ctypes.POINTER(vp), ctypes.POINTER(sz), vp, vp,
                                  vp, u64, ctypes.POINTER(u64), ctypes.POINTER(_Stats)]
     for fn in ("tg_ctx_create", "tg_ctx_destroy", "tg_job_begin", "tg_job_feed_seq", "tg_job_feed_seq_device",
                "tg_job_feed_fastx", "tg_job_feed_file", "tg_job_run", "tg_job_stats", "tg_job_result_copy",
                "tg_job_drain", "tg_job_write", "tg_job_export_partitions", "tg_job_end", "tg_count_seq",
                "tg_job_next_sample", "tg_job_sample_offsets", "tg_count_batch", "tg_job_feed_fastx_device",
-               "tg_count_fastx", "tg_fastx_to_stream", "tg_read_input", "tg_count_batch_fastx"):
+               "tg_count_fastx", "tg_fastx_to_stream", "tg_read_input", "tg_count_batch_fastx",
+               "tg_job_set_shard"):
         getattr(L, fn).restype = i32
     _lib = L
     return L
@@ -269,20 +271,24 @@ class Context:
 
     def run(self, k: int, m: int, *, seq=None, dev_seq=None, dev_len: int = 0, fastx=None, files=(),
             dev_fastx=None, samples=None, n_parts: int = 16, ci: int = 1, cx: int = _U64_MAX, gpu_parts: int = 0,
-            export: bool = False, want_results: bool = True, drain: Optional[int] = None):
+            export: bool = False, want_results: bool = True, drain: Optional[int] = None,
+            shard: Optional[tuple] = None):
         """Run one job. seq: host stream (bytes / uint8 array); dev_seq: device
         pointer (int) of dev_len bytes; fastx: FASTA/FASTQ bytes; dev_fastx: device
         pointer of dev_len FASTA/FASTQ bytes; files: paths;
         samples: host streams counted as separate samples of the job (the
         Result then carries the sample of each pair); drain: a tg_format (0 TSV,
         1 KFF entries, 2 RAW) whose bytes tg_job_drain hands back in
-        Result.formatted.
+        Result.formatted; shard: (s, n) counts only shard s of n of the bins
+        (tg_job_set_shard), whose pairs the n shards' results split between them.
         Returns (Result, partitions or None)."""
         L = self._L
         o = self._opts(k, m, n_parts, ci, cx, gpu_parts)
         j = ctypes.c_void_p()
         self.check(L.tg_job_begin(self.h, ctypes.byref(o), ctypes.byref(j)))
         try:
+            if shard is not None:
+                self.check(L.tg_job_set_shard(j, int(shard[0]), int(shard[1])))
             for i, smp in enumerate(samples or ()):
                 if i:
                     self.check(L.tg_job_next_sample(j))

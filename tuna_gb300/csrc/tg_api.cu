@@ -168,6 +168,8 @@ struct tg_job {
     uint64_t* sink_keys = nullptr;
     uint32_t* sink_counts = nullptr;
     uint64_t sink_cap = 0;
+    // phase 2 over shard `shard` of `n_shards` runs of consecutive segments only
+    uint32_t shard = 0, n_shards = 1;
     const uint8_t* seq_ptr() const { return ext ? ext : ctx->seq.as<uint8_t>(); }
 };
 
@@ -418,6 +420,19 @@ tg_status tg_job_next_sample(tg_job* j) {
 
 uint32_t tg_job_sample_count(const tg_job* j) { return j ? (uint32_t)j->sample_start.size() : 0; }
 
+tg_status tg_job_set_shard(tg_job* j, uint32_t shard, uint32_t n_shards) {
+    if (!j) return TG_ERR_ARG;
+    if (j->ran) return j->ctx->fail(TG_ERR_STATE, "shard set after run");
+    if (!n_shards || (n_shards & (n_shards - 1)) || n_shards > TG_MAX_SHARDS)
+        return j->ctx->fail(TG_ERR_ARG, "n_shards must be a power of two <= 1024");
+    if (shard >= n_shards) return j->ctx->fail(TG_ERR_ARG, "shard must be < n_shards");
+    if (j->o.gpu_parts && j->o.gpu_parts < n_shards)
+        return j->ctx->fail(TG_ERR_ARG, "n_shards must be <= gpu_parts");
+    j->shard = shard;
+    j->n_shards = n_shards;
+    return TG_OK;
+}
+
 tg_status tg_job_feed_fastx(tg_job* j, const uint8_t* data, size_t len) {
     if (!j || (!data && len)) return TG_ERR_ARG;
     return lex_append_host(j, data, len);
@@ -650,7 +665,7 @@ tg_status tg_job_run(tg_job* j) {
     CK(cudaMemcpyAsync(&n_bases, ctx->misc.as<uint8_t>() + MISC_BASES, 8, cudaMemcpyDeviceToHost, ctx->st), "d2h");
     // ---- phase 1: cut
     uint32_t p1 = j->o.gpu_parts;
-    if (!p1) p1 = std::min<uint32_t>(1024, std::max<uint32_t>(16, next_pow2_u32(n / 32768)));
+    if (!p1) p1 = std::max(j->n_shards, std::min<uint32_t>(1024, std::max<uint32_t>(16, next_pow2_u32(n / 32768))));
     uint32_t p1_bits = 0;
     while ((1u << p1_bits) < p1) ++p1_bits;
     // the bins of the samples (2^20 in all, cut into p1 segments for one sample)
@@ -658,6 +673,7 @@ tg_status tg_job_run(tg_job* j) {
     starts.push_back(n);
     const SampleBins B = layout_bins(starts, (1u << BIN_BITS) >> p1_bits);
     const uint32_t ns = (uint32_t)B.base.size();
+    if (j->n_shards > 1 && ns > 1) return ctx->fail(TG_ERR_UNSUPPORTED, "a job of several samples cannot be sharded");
     {
         const size_t bytes = 8 * (size_t)(ns + 1) + 4 * (size_t)ns + ns + 64;
         CK(ctx->ensure(ctx->samp, bytes), "alloc samples");
@@ -684,12 +700,32 @@ tg_status tg_job_run(tg_job* j) {
     // ---- phase 2: one run over all bins or, when their keys and pairs do not
     // fit in the memory budget, passes over ranges of consecutive segments
     // (bins), each pass's pairs going to host memory before the next
-    const uint64_t n_kmers = cstats[0];
+    // the segments this run counts: all of them, or the job's shard of them
+    std::vector<Segment> segs = B.segs;
+    std::vector<uint32_t> hist;  // k-mers per bin, downloaded when a shard or the passes need it
+    auto load_hist = [&]() -> cudaError_t {
+        if (!hist.empty()) return cudaSuccess;
+        hist.resize((size_t)1 << BIN_BITS);
+        return cudaMemcpy(hist.data(), ctx->hist.p, hist.size() * 4, cudaMemcpyDeviceToHost);
+    };
+    uint64_t n_kmers = cstats[0];
+    if (j->n_shards > 1) {  // one sample: 2^p1_bits >= n_shards segments of consecutive bins
+        const size_t P = B.segs.size();
+        segs.assign(B.segs.begin() + P * j->shard / j->n_shards, B.segs.begin() + P * (j->shard + 1) / j->n_shards);
+        CK(load_hist(), "d2h");
+        n_kmers = 0;
+        for (const Segment& g : segs)
+            for (uint32_t b = g.bin_lo; b < g.bin_hi; ++b) n_kmers += hist[b];
+    }
     P2Input in{};
     in.W = W;
     in.k = k;
-    in.segs = B.segs.data();
-    in.n_segs = (uint32_t)B.segs.size();
+    in.segs = segs.data();
+    in.n_segs = (uint32_t)segs.size();
+    if (j->n_shards > 1) {
+        in.bin_lo = segs.front().bin_lo;
+        in.bin_hi = segs.back().bin_hi;
+    }
     in.n_sm = (uint32_t)ctx->n_sm;
     in.packed = ctx->packed.as<uint32_t>();
     in.desc = ctx->desc.as<uint64_t>();
@@ -710,15 +746,14 @@ tg_status tg_job_run(tg_job* j) {
         const uint64_t have = free_b + ctx->scratch.cap + ctx->okeys.cap + ctx->ocnt.cap;
         const uint64_t reserve = (2ull << 30) + total_b / 50;
         const uint64_t budget = ctx->hbm_budget ? ctx->hbm_budget : (have > reserve ? have - reserve : 0);
-        if (ns == 1 && B.segs.size() > 1 && n_kmers * per_key > budget) {
-            std::vector<uint32_t> hist((size_t)1 << BIN_BITS);
-            CK(cudaMemcpy(hist.data(), ctx->hist.p, hist.size() * 4, cudaMemcpyDeviceToHost), "d2h");
+        if (ns == 1 && segs.size() > 1 && n_kmers * per_key > budget) {
+            CK(load_hist(), "d2h");
             const uint64_t max_keys = std::max<uint64_t>(1, budget / per_key);
             uint32_t s0 = 0;
             uint64_t acc = 0;
-            for (uint32_t sg = 0; sg < B.segs.size(); ++sg) {
+            for (uint32_t sg = 0; sg < segs.size(); ++sg) {
                 uint64_t kk = 0;
-                for (uint32_t b = B.segs[sg].bin_lo; b < B.segs[sg].bin_hi; ++b) kk += hist[b];
+                for (uint32_t b = segs[sg].bin_lo; b < segs[sg].bin_hi; ++b) kk += hist[b];
                 seg_keys.push_back(kk);
                 if (sg > s0 && acc + kk > max_keys) {
                     passes.emplace_back(s0, sg);
@@ -727,7 +762,7 @@ tg_status tg_job_run(tg_job* j) {
                 }
                 acc += kk;
             }
-            passes.emplace_back(s0, (uint32_t)B.segs.size());
+            passes.emplace_back(s0, (uint32_t)segs.size());
         }
     }
     CK(cudaEventRecord(ctx->ev[6], ctx->st), "event");
@@ -811,10 +846,10 @@ tg_status tg_job_run(tg_job* j) {
         for (size_t p = 0; p < passes.size(); ++p) {
             P2Input& ip = pin[p];
             const uint32_t s0 = passes[p].first, s1 = passes[p].second;
-            ip.segs = B.segs.data() + s0;
+            ip.segs = segs.data() + s0;
             ip.n_segs = s1 - s0;
-            ip.bin_lo = B.segs[s0].bin_lo;
-            ip.bin_hi = B.segs[s1 - 1].bin_hi;
+            ip.bin_lo = segs[s0].bin_lo;
+            ip.bin_hi = segs[s1 - 1].bin_hi;
             ip.n_kmers = 0;
             for (uint32_t sg = s0; sg < s1; ++sg) ip.n_kmers += seg_keys[sg];
             max_keys = std::max(max_keys, ip.n_kmers);
