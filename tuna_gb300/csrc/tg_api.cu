@@ -120,10 +120,15 @@ struct tg_ctx {
     int prepared_m = -1;
 
     tg_status fail(tg_status s, const std::string& msg) {
+        if (s == TG_ERR_CUDA || s == TG_ERR_OOM) (void)cudaGetLastError();
         err = msg;
         return s;
     }
+    // A failed runtime call also leaves its error as the thread's "last error",
+    // which the next launch check would read: reset it once reported, so the
+    // context's next job starts clean (a device fault stays sticky regardless).
     tg_status cuda_fail(cudaError_t e, const char* what) {
+        (void)cudaGetLastError();
         err = std::string(what) + ": " + cudaGetErrorString(e);
         return e == cudaErrorMemoryAllocation ? TG_ERR_OOM : TG_ERR_CUDA;
     }
@@ -132,7 +137,7 @@ struct tg_ctx {
         if (b.p) { cudaFree(b.p); b.p = nullptr; b.cap = 0; }
         const size_t want = std::max<size_t>(bytes, 256);
         cudaError_t e = cudaMalloc(&b.p, want);
-        if (e != cudaSuccess) { b.p = nullptr; return e; }
+        if (e != cudaSuccess) { b.p = nullptr; (void)cudaGetLastError(); return e; }
         b.cap = want;
         return cudaSuccess;
     }
@@ -215,8 +220,9 @@ tg_status tg_ctx_create(const tg_ctx_opts* opts, tg_ctx** out) {
     if (e == cudaSuccess) e = cudaHostGetDevicePointer(reinterpret_cast<void**>(&ctx->wave_out_dev), ctx->wave_out, 0);
     for (int i = 0; i < 16 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&ctx->wave_ev[i], cudaEventDisableTiming);
     if (e != cudaSuccess) {
-        delete ctx;
-        return TG_ERR_CUDA;
+        tg_ctx_destroy(ctx);  // whatever was created so far
+        (void)cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? TG_ERR_OOM : TG_ERR_CUDA;
     }
     *out = ctx;
     return TG_OK;
