@@ -1,7 +1,7 @@
 """Host-side logic that needs no GPU: the server's batching policy
-(tuna_gb300.serve.take_batch) and the bench's clock-sample parsing
-(bench.parse_clock_lines), whose throttle reasons decide whether a bench
-number is kept."""
+(tuna_gb300.serve.take_batch), what the server does when no worker can open a
+device context, and the bench's clock-sample parsing (bench.parse_clock_lines),
+whose throttle reasons decide whether a bench number is kept."""
 import os
 import sys
 from collections import deque
@@ -40,3 +40,29 @@ def test_parse_clock_lines():
     out = bench.parse_clock_lines([hot, ok])
     assert out["reasons"] == ["hw_thermal_slowdown"] and out["sm_mhz"] == (1500.0 + 2070.0) / 2
     assert bench.parse_clock_lines([])["sm_mhz"] is None
+
+
+def test_server_without_a_device_fails_requests():
+    """When no worker can open a device context, waiting requests fail instead
+    of waiting forever, and later submits raise (run where there is no GPU)."""
+    import time
+
+    import pytest
+    import tuna_gb300 as T
+    from tuna_gb300 import serve
+    if T.library().tg_device_count() > 0:
+        pytest.skip("a CUDA device is present: the workers would serve the request")
+    seq = np.frombuffer(b"ACGTTGCAAC" * 20, dtype=np.uint8)
+    with serve.Server(0, workers=2, max_batch_bases=1 << 20) as srv:
+        try:
+            f = srv.submit(seq, 31, 21)
+        except RuntimeError:  # both workers were already gone
+            f = None
+        if f is not None:
+            with pytest.raises(T.GpuError):
+                f.result(timeout=60)
+        deadline = time.time() + 60
+        while srv._error is None and time.time() < deadline:
+            time.sleep(0.02)
+        with pytest.raises(RuntimeError, match="no worker could open a device context"):
+            srv.submit(seq, 31, 21)

@@ -77,6 +77,8 @@ class Server:
         self._q: Deque[_Req] = deque()
         self._cv = threading.Condition()
         self._stop = False
+        self._alive = workers       # workers that hold a device context
+        self._error: Optional[BaseException] = None  # why no worker is left
         self.batches = 0
         self._threads = [threading.Thread(target=self._work, args=(device, host_threads), daemon=True)
                          for _ in range(workers)]
@@ -94,6 +96,8 @@ class Server:
         with self._cv:
             if self._stop:
                 raise RuntimeError("server is closed")
+            if self._error is not None:
+                raise RuntimeError(f"no worker could open a device context: {self._error}")
             self._q.append(r)
             self._cv.notify()
         return r.future
@@ -118,7 +122,11 @@ class Server:
 
     def _work(self, device: int, host_threads: int) -> None:
         T, L = self._T, self._L
-        ctx = T.Context(device, host_threads, autotune=True)
+        try:
+            ctx = T.Context(device, host_threads, autotune=True)
+        except Exception as e:  # noqa: BLE001 - the last worker lost fails every waiting request
+            self._worker_lost(e)
+            return
         try:
             while True:
                 with self._cv:
@@ -136,6 +144,18 @@ class Server:
                             r.future.set_exception(e)
         finally:
             ctx.close()
+
+    def _worker_lost(self, e: BaseException) -> None:
+        with self._cv:
+            self._alive -= 1
+            if self._alive > 0:
+                return
+            self._error = e
+            while self._q:
+                r = self._q.popleft()
+                if not r.future.done():
+                    r.future.set_exception(e)
+            self._cv.notify_all()
 
     def _run(self, ctx, batch: List[_Req]) -> None:
         T, L = self._T, self._L
