@@ -63,7 +63,8 @@ typedef enum {
     TG_OK = 0,
     TG_ERR_ARG = 1,        /* bad parameter (k, m, n, sizes, null pointers) */
     TG_ERR_CUDA = 2,       /* a CUDA call failed; see tg_last_error */
-    TG_ERR_OOM = 3,        /* device or pinned memory exhausted */
+    TG_ERR_OOM = 3,        /* device, pinned or host memory (or host threads) exhausted;
+                              a host-side C++ failure is reported as this, "host: ..." */
     TG_ERR_STATE = 4,      /* call out of order (e.g. feed after run) */
     TG_ERR_IO = 5,         /* file could not be opened / read / written */
     TG_ERR_PARSE = 6,      /* empty input file ("Empty file") */

@@ -93,3 +93,18 @@ def test_count_bgzf_file(tmp_path):
         got, _ = ctx.run(31, 21, files=[p])
     want = O.count_fastx(raw, 31, 21, threads=4)
     assert T.tsv_blob(got.keys, got.counts, 31) == O.tsv_blob(want)
+
+
+def test_bgzf_claiming_more_than_memory_fails_cleanly(tmp_path):
+    """Members whose sizes add up to ~800 TB: the reservation of the output
+    fails on the host and comes back as a status with a message (no C++
+    exception crosses the C ABI, the process goes on)."""
+    member = (b"\x1f\x8b\x08\x04\x00\x00\x00\x00\x00\xff" + (6).to_bytes(2, "little") + b"BC"
+              + (2).to_bytes(2, "little") + (27).to_bytes(2, "little") + b"\x03\x00"
+              + (0).to_bytes(4, "little") + (0xFFFFFFFF).to_bytes(4, "little"))
+    assert len(member) == 28
+    p = _write(tmp_path, "huge.gz", member * 200_000)
+    with pytest.raises(T.GpuError) as e:
+        T.read_input(p, threads=4, cap=1 << 20)
+    assert "host:" in str(e.value) or "Cannot read" in str(e.value)
+    assert T.read_input(_write(tmp_path, "ok.gz", bgzf(b"ACGT\n"))) == b"ACGT\n"  # still usable

@@ -184,6 +184,35 @@ struct tg_job {
         if (e_ != cudaSuccess) return ctx->cuda_fail(e_, what); \
     } while (0)
 
+// Ends a job the library opened itself, however the call leaves.
+struct JobEnd {
+    tg_job* j;
+    ~JobEnd() { tg_job_end(j); }
+};
+
+static void note_host_failure(tg_ctx* ctx, const char* what) noexcept {
+    if (!ctx) return;
+    try {
+        ctx->err = std::string("host: ") + what;
+    } catch (...) {
+    }
+}
+
+// Host-side C++ failures below the C ABI (allocation, thread creation, an
+// exception from a caller's sink) become a status and a message: no exception
+// crosses the ABI.
+template <typename F>
+static tg_status guarded(tg_ctx* ctx, F&& body) noexcept {
+    try {
+        return body();
+    } catch (const std::exception& x) {
+        note_host_failure(ctx, x.what());
+    } catch (...) {
+        note_host_failure(ctx, "unknown exception");
+    }
+    return TG_ERR_OOM;
+}
+
 extern "C" {
 
 const char* tg_version(void) { return "tuna-gb300 0.1 (sm_103a)"; }
@@ -194,7 +223,7 @@ int tg_device_count(void) {
     return n;
 }
 
-tg_status tg_ctx_create(const tg_ctx_opts* opts, tg_ctx** out) {
+static tg_status tg_ctx_create_impl(const tg_ctx_opts* opts, tg_ctx** out) {
     if (!out) return TG_ERR_ARG;
     *out = nullptr;
     tg_ctx_opts o{};
@@ -226,6 +255,10 @@ tg_status tg_ctx_create(const tg_ctx_opts* opts, tg_ctx** out) {
     }
     *out = ctx;
     return TG_OK;
+}
+
+tg_status tg_ctx_create(const tg_ctx_opts* opts, tg_ctx** out) {
+    return guarded(nullptr, [&] { return tg_ctx_create_impl(opts, out); });
 }
 
 tg_status tg_ctx_destroy(tg_ctx* ctx) {
@@ -260,7 +293,7 @@ const char* tg_last_error(const tg_ctx* ctx) { return ctx ? ctx->err.c_str() : "
 
 void* tg_ctx_stream(const tg_ctx* ctx) { return ctx ? (void*)ctx->st : nullptr; }
 
-tg_status tg_job_begin(tg_ctx* ctx, const tg_job_opts* opts, tg_job** out) {
+static tg_status tg_job_begin_impl(tg_ctx* ctx, const tg_job_opts* opts, tg_job** out) {
     if (!ctx || !opts || !out) return TG_ERR_ARG;
     *out = nullptr;
     const tg_job_opts& o = *opts;
@@ -283,6 +316,10 @@ tg_status tg_job_begin(tg_ctx* ctx, const tg_job_opts* opts, tg_job** out) {
     ctx->active = j;
     *out = j;
     return TG_OK;
+}
+
+tg_status tg_job_begin(tg_ctx* ctx, const tg_job_opts* opts, tg_job** out) {
+    return guarded(ctx, [&] { return tg_job_begin_impl(ctx, opts, out); });
 }
 
 // Room for `extra` more stream bytes in ctx->seq (a device feed used in place
@@ -395,12 +432,16 @@ static tg_status lex_append_host(tg_job* j, const uint8_t* data, size_t len) {
     return lex_append(j, ctx->raw.as<uint8_t>(), len, data);
 }
 
-tg_status tg_job_feed_seq(tg_job* j, const uint8_t* seq, size_t len) {
+static tg_status tg_job_feed_seq_impl(tg_job* j, const uint8_t* seq, size_t len) {
     if (!j || (!seq && len)) return TG_ERR_ARG;
     return append_stream(j, seq, len, cudaMemcpyHostToDevice);
 }
 
-tg_status tg_job_feed_seq_device(tg_job* j, const uint8_t* dseq, size_t len) {
+tg_status tg_job_feed_seq(tg_job* j, const uint8_t* seq, size_t len) {
+    return guarded(j ? j->ctx : nullptr, [&] { return tg_job_feed_seq_impl(j, seq, len); });
+}
+
+static tg_status tg_job_feed_seq_device_impl(tg_job* j, const uint8_t* dseq, size_t len) {
     if (!j || (!dseq && len)) return TG_ERR_ARG;
     if (j->ran) return j->ctx->fail(TG_ERR_STATE, "feed after run");
     if (j->n == 0 && !j->used_ctx_seq) {
@@ -412,7 +453,11 @@ tg_status tg_job_feed_seq_device(tg_job* j, const uint8_t* dseq, size_t len) {
     return append_stream(j, dseq, len, cudaMemcpyDeviceToDevice);
 }
 
-tg_status tg_job_next_sample(tg_job* j) {
+tg_status tg_job_feed_seq_device(tg_job* j, const uint8_t* dseq, size_t len) {
+    return guarded(j ? j->ctx : nullptr, [&] { return tg_job_feed_seq_device_impl(j, dseq, len); });
+}
+
+static tg_status tg_job_next_sample_impl(tg_job* j) {
     if (!j) return TG_ERR_ARG;
     if (j->ran) return j->ctx->fail(TG_ERR_STATE, "feed after run");
     if (j->sample_start.size() >= TG_MAX_SAMPLES) return j->ctx->fail(TG_ERR_ARG, "too many samples in one job");
@@ -422,6 +467,10 @@ tg_status tg_job_next_sample(tg_job* j) {
     }
     j->sample_start.push_back(j->n);
     return TG_OK;
+}
+
+tg_status tg_job_next_sample(tg_job* j) {
+    return guarded(j ? j->ctx : nullptr, [&] { return tg_job_next_sample_impl(j); });
 }
 
 uint32_t tg_job_sample_count(const tg_job* j) { return j ? (uint32_t)j->sample_start.size() : 0; }
@@ -439,12 +488,16 @@ tg_status tg_job_set_shard(tg_job* j, uint32_t shard, uint32_t n_shards) {
     return TG_OK;
 }
 
-tg_status tg_job_feed_fastx(tg_job* j, const uint8_t* data, size_t len) {
+static tg_status tg_job_feed_fastx_impl(tg_job* j, const uint8_t* data, size_t len) {
     if (!j || (!data && len)) return TG_ERR_ARG;
     return lex_append_host(j, data, len);
 }
 
-tg_status tg_job_feed_fastx_device(tg_job* j, const uint8_t* ddata, size_t len) {
+tg_status tg_job_feed_fastx(tg_job* j, const uint8_t* data, size_t len) {
+    return guarded(j ? j->ctx : nullptr, [&] { return tg_job_feed_fastx_impl(j, data, len); });
+}
+
+static tg_status tg_job_feed_fastx_device_impl(tg_job* j, const uint8_t* ddata, size_t len) {
     if (!j || (!ddata && len)) return TG_ERR_ARG;
     tg_ctx* ctx = j->ctx;
     if (j->ran) return ctx->fail(TG_ERR_STATE, "feed after run");
@@ -458,7 +511,11 @@ tg_status tg_job_feed_fastx_device(tg_job* j, const uint8_t* ddata, size_t len) 
     return lex_append(j, ddata, len, nullptr);
 }
 
-tg_status tg_job_feed_file(tg_job* j, const char* path) {
+tg_status tg_job_feed_fastx_device(tg_job* j, const uint8_t* ddata, size_t len) {
+    return guarded(j ? j->ctx : nullptr, [&] { return tg_job_feed_fastx_device_impl(j, ddata, len); });
+}
+
+static tg_status tg_job_feed_file_impl(tg_job* j, const char* path) {
     if (!j || !path) return TG_ERR_ARG;
     tgh::Bytes raw;
     const std::string err = tgh::read_input_file(path, raw, j->ctx->host_threads);
@@ -469,7 +526,11 @@ tg_status tg_job_feed_file(tg_job* j, const char* path) {
     return lex_append_host(j, raw.data(), raw.size());
 }
 
-tg_status tg_read_input(const char* path, uint32_t threads, uint8_t* out, size_t cap, size_t* out_len,
+tg_status tg_job_feed_file(tg_job* j, const char* path) {
+    return guarded(j ? j->ctx : nullptr, [&] { return tg_job_feed_file_impl(j, path); });
+}
+
+static tg_status tg_read_input_impl(const char* path, uint32_t threads, uint8_t* out, size_t cap, size_t* out_len,
                         char* errbuf, size_t errlen) {
     if (!path || !out_len) return TG_ERR_ARG;
     *out_len = 0;
@@ -507,7 +568,19 @@ tg_status tg_read_input(const char* path, uint32_t threads, uint8_t* out, size_t
     return TG_OK;
 }
 
-tg_status tg_fastx_to_stream(tg_ctx* ctx, const uint8_t* data, size_t len, uint8_t* out, size_t cap,
+tg_status tg_read_input(const char* path, uint32_t threads, uint8_t* out, size_t cap, size_t* out_len,
+                        char* errbuf, size_t errlen) {
+    try {
+        return tg_read_input_impl(path, threads, out, cap, out_len, errbuf, errlen);
+    } catch (const std::exception& x) {
+        if (errbuf && errlen) snprintf(errbuf, errlen, "host: %s", x.what());
+    } catch (...) {
+        if (errbuf && errlen) snprintf(errbuf, errlen, "host: unknown exception");
+    }
+    return TG_ERR_OOM;
+}
+
+static tg_status tg_fastx_to_stream_impl(tg_ctx* ctx, const uint8_t* data, size_t len, uint8_t* out, size_t cap,
                              size_t* out_len) {
     if (!ctx || (!data && len) || !out_len) return TG_ERR_ARG;
     *out_len = 0;
@@ -517,6 +590,7 @@ tg_status tg_fastx_to_stream(tg_ctx* ctx, const uint8_t* data, size_t len, uint8
     tg_job* j = nullptr;
     tg_status s = tg_job_begin(ctx, &o, &j);
     if (s != TG_OK) return s;
+    const JobEnd end_job{j};
     s = tg_job_feed_fastx(j, data, len);
     if (s == TG_OK) {
         const size_t n = j->n ? j->n - 1 : 0;  // without the closing separator
@@ -527,8 +601,12 @@ tg_status tg_fastx_to_stream(tg_ctx* ctx, const uint8_t* data, size_t len, uint8
             if (e != cudaSuccess) s = ctx->cuda_fail(e, "d2h");
         }
     }
-    tg_job_end(j);
     return s;
+}
+
+tg_status tg_fastx_to_stream(tg_ctx* ctx, const uint8_t* data, size_t len, uint8_t* out, size_t cap,
+                             size_t* out_len) {
+    return guarded(ctx, [&] { return tg_fastx_to_stream_impl(ctx, data, len, out, cap, out_len); });
 }
 
 // Phase 1 cut (optionally the export variant) over the current stream.
@@ -637,7 +715,7 @@ static tg_status d2h_pageable(tg_ctx* ctx, void* dst, const void* src, size_t by
     return TG_OK;
 }
 
-tg_status tg_job_run(tg_job* j) {
+static tg_status tg_job_run_impl(tg_job* j) {
     if (!j) return TG_ERR_ARG;
     tg_ctx* ctx = j->ctx;
     if (j->ran) return ctx->fail(TG_ERR_STATE, "job already ran");
@@ -929,6 +1007,10 @@ tg_status tg_job_run(tg_job* j) {
     return TG_OK;
 }
 
+tg_status tg_job_run(tg_job* j) {
+    return guarded(j ? j->ctx : nullptr, [&] { return tg_job_run_impl(j); });
+}
+
 tg_status tg_job_stats(const tg_job* j, tg_stats* out) {
     if (!j || !out) return TG_ERR_ARG;
     *out = j->st;
@@ -986,7 +1068,7 @@ tg_status tg_job_sample_offsets(tg_job* j, uint64_t* offsets) {
 // handed to the sink while this one copies.
 constexpr uint64_t DRAIN_PAIRS = 1ull << 20;
 
-tg_status tg_job_drain(tg_job* j, tg_format fmt, tg_sink_fn sink, void* user) {
+static tg_status tg_job_drain_impl(tg_job* j, tg_format fmt, tg_sink_fn sink, void* user) {
     if (!j || !sink || (int)fmt < 0 || (int)fmt > 2) return TG_ERR_ARG;
     tg_ctx* ctx = j->ctx;
     if (!j->ran) return ctx->fail(TG_ERR_STATE, "drain before run");
@@ -1055,6 +1137,10 @@ tg_status tg_job_drain(tg_job* j, tg_format fmt, tg_sink_fn sink, void* user) {
     return s;
 }
 
+tg_status tg_job_drain(tg_job* j, tg_format fmt, tg_sink_fn sink, void* user) {
+    return guarded(j ? j->ctx : nullptr, [&] { return tg_job_drain_impl(j, fmt, sink, user); });
+}
+
 struct FileSink {
     FILE* f;
 };
@@ -1063,7 +1149,7 @@ static int file_sink(const void* data, size_t bytes, uint64_t, void* u) {
     return fwrite(data, 1, bytes, fs->f) == bytes ? 0 : 1;
 }
 
-tg_status tg_job_write(tg_job* j, tg_format fmt, const char* path) {
+static tg_status tg_job_write_impl(tg_job* j, tg_format fmt, const char* path) {
     if (!j || !path) return TG_ERR_ARG;
     FILE* f = fopen(path, "wb");
     if (!f) return j->ctx->fail(TG_ERR_IO, std::string("cannot open output file: ") + path);
@@ -1083,7 +1169,11 @@ tg_status tg_job_write(tg_job* j, tg_format fmt, const char* path) {
     return s;
 }
 
-tg_status tg_job_export_partitions(tg_job* j, tg_part_sink_fn sink, void* user) {
+tg_status tg_job_write(tg_job* j, tg_format fmt, const char* path) {
+    return guarded(j ? j->ctx : nullptr, [&] { return tg_job_write_impl(j, fmt, path); });
+}
+
+static tg_status tg_job_export_partitions_impl(tg_job* j, tg_part_sink_fn sink, void* user) {
     if (!j || !sink) return TG_ERR_ARG;
     tg_ctx* ctx = j->ctx;
     if (!j->ran) return ctx->fail(TG_ERR_STATE, "export before run");
@@ -1135,6 +1225,10 @@ tg_status tg_job_export_partitions(tg_job* j, tg_part_sink_fn sink, void* user) 
     return TG_OK;
 }
 
+tg_status tg_job_export_partitions(tg_job* j, tg_part_sink_fn sink, void* user) {
+    return guarded(j ? j->ctx : nullptr, [&] { return tg_job_export_partitions_impl(j, sink, user); });
+}
+
 tg_status tg_job_end(tg_job* j) {
     if (!j) return TG_ERR_ARG;
     if (j->ctx->active == j) j->ctx->active = nullptr;
@@ -1154,6 +1248,7 @@ static tg_status count_host(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_sam
     tg_job* j = nullptr;
     tg_status s = tg_job_begin(ctx, opts, &j);
     if (s != TG_OK) return s;
+    const JobEnd end_job{j};
     // one buffer, separators everywhere, then every sample copied to its place
     uint64_t total = 0;
     for (uint32_t i = 0; i < n_samples; ++i) {
@@ -1231,34 +1326,33 @@ static tg_status count_host(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_sam
         else if (sample_off && !multi) { sample_off[0] = 0; sample_off[1] = j->n_out; }
     }
     if (stats) *stats = j->st;
-    tg_job_end(j);
     return s;
 }
 
 tg_status tg_count_seq(tg_ctx* ctx, const tg_job_opts* opts, const uint8_t* seq, size_t len, uint64_t* keys,
                        uint32_t* counts, uint64_t cap, uint64_t* n_out, tg_stats* stats) {
     if (!seq && len) return TG_ERR_ARG;
-    return count_host(ctx, opts, 1, &seq, &len, keys, counts, nullptr, cap, n_out, stats);
+    return guarded(ctx, [&] { return count_host(ctx, opts, 1, &seq, &len, keys, counts, nullptr, cap, n_out, stats); });
 }
 
 tg_status tg_count_fastx(tg_ctx* ctx, const tg_job_opts* opts, const uint8_t* data, size_t len, uint64_t* keys,
                          uint32_t* counts, uint64_t cap, uint64_t* n_out, tg_stats* stats) {
     if (!data && len) return TG_ERR_ARG;
-    return count_host(ctx, opts, 1, &data, &len, keys, counts, nullptr, cap, n_out, stats, true);
+    return guarded(ctx, [&] { return count_host(ctx, opts, 1, &data, &len, keys, counts, nullptr, cap, n_out, stats, true); });
 }
 
 tg_status tg_count_batch_fastx(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_samples,
                                const uint8_t* const* datas, const size_t* lens, uint64_t* keys, uint32_t* counts,
                                uint64_t* sample_offsets, uint64_t cap, uint64_t* n_out, tg_stats* stats) {
     if (n_samples == 0) return TG_ERR_ARG;
-    return count_host(ctx, opts, n_samples, datas, lens, keys, counts, sample_offsets, cap, n_out, stats, true);
+    return guarded(ctx, [&] { return count_host(ctx, opts, n_samples, datas, lens, keys, counts, sample_offsets, cap, n_out, stats, true); });
 }
 
 tg_status tg_count_batch(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_samples, const uint8_t* const* seqs,
                          const size_t* lens, uint64_t* keys, uint32_t* counts, uint64_t* sample_offsets, uint64_t cap,
                          uint64_t* n_out, tg_stats* stats) {
     if (n_samples == 0) return TG_ERR_ARG;
-    return count_host(ctx, opts, n_samples, seqs, lens, keys, counts, sample_offsets, cap, n_out, stats);
+    return guarded(ctx, [&] { return count_host(ctx, opts, n_samples, seqs, lens, keys, counts, sample_offsets, cap, n_out, stats); });
 }
 
 }  // extern "C"
