@@ -58,6 +58,28 @@ def test_argument_errors(cli, args, tmp_path):
         assert _err_line(ref.stderr) == _err_line(r.stderr)
 
 
+def _header_n(stderr: str) -> str:
+    for ln in stderr.splitlines():
+        if ln.startswith("tuna  k="):
+            return [f for f in ln.split() if f.startswith("n=")][0]
+    return ""
+
+
+@pytest.mark.parametrize("n,want", [("1", "n=1"), ("3", "n=4"), ("1000", "n=1024"), ("4096", "n=4096"),
+                                    ("5000", "n=8192"), ("2147483648", "n=2147483648"),
+                                    ("2147483649", "n=0")])
+def test_partition_count_rounding(cli, tmp_path, n, want):
+    """-n is rounded up to a power of two as the reference's main does (the
+    header line is printed before any device work); against the reference
+    binary for the counts it can run quickly."""
+    (tmp_path / "a.fa").write_bytes(b">s\nACGTACGTTGCAACGTAGCTAGCTAGGATCCATGCATGCA\n")
+    r = subprocess.run([cli, "-n", n, "a.fa", "out.tsv"], capture_output=True, text=True, cwd=tmp_path)
+    assert _header_n(r.stderr) == want
+    if os.path.exists(REF_BIN) and int(n) <= 8192:
+        ref = subprocess.run([REF_BIN, "-n", n, "a.fa", "ref.tsv"], capture_output=True, text=True, cwd=tmp_path)
+        assert _header_n(ref.stderr) == want
+
+
 def _write_case(tmp_path, name):
     data = G.case_input(name)
     path = tmp_path / ("in.fq" if data[:1] == b"@" else "in.fa")

@@ -211,11 +211,13 @@ static uint32_t auto_partitions(const std::vector<std::string>& files) {
     return (uint32_t)n;
 }
 
+// -n rounded up to a power of two (the reference's -n semantics, main.cpp:52):
+// the smallest 2^j >= n, 1 for n <= 1, and 0 where 2^j would not fit in 32 bits.
 static uint32_t round_pow2(uint32_t n) {
-    if (n <= 1) return 1;
-    if ((n & (n - 1)) == 0) return n;
-    while (n & (n - 1)) n &= n - 1;
-    return n << 1;
+    if (n > (1u << 31)) return 0;
+    uint32_t p = 1;
+    while (p < n) p <<= 1;
+    return p;
 }
 
 static double secs(std::chrono::steady_clock::time_point t0) {
