@@ -16,6 +16,7 @@
 // The export of partition files runs the tile cut k_cut<true> instead, which
 // also yields each record's exact minimizer position.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <chrono>
@@ -183,6 +184,16 @@ struct tg_job {
         cudaError_t e_ = (call);                         \
         if (e_ != cudaSuccess) return ctx->cuda_fail(e_, what); \
     } while (0)
+
+// NVTX range over one library call on the host thread (a profiler's timeline
+// shows tg_job_run, its phase marks, the lexer and the drain); header-only
+// NVTX does nothing unless a tool is attached.
+struct TraceRange {
+    explicit TraceRange(const char* name) { nvtxRangePushA(name); }
+    ~TraceRange() { nvtxRangePop(); }
+    TraceRange(const TraceRange&) = delete;
+    TraceRange& operator=(const TraceRange&) = delete;
+};
 
 // Ends a job the library opened itself, however the call leaves.
 struct JobEnd {
@@ -370,6 +381,7 @@ static tg_status append_stream(tg_job* j, const uint8_t* src, size_t len, cudaMe
 // offset 63 mod 64, where the reference's block walk departs from line
 // counting) is parsed by the host parser instead.
 static tg_status lex_append(tg_job* j, const uint8_t* draw, size_t len, const uint8_t* host_raw) {
+    const TraceRange tr("tuna.lex");
     tg_ctx* ctx = j->ctx;
     if (j->ran) return ctx->fail(TG_ERR_STATE, "feed after run");
     if (len == 0) return ctx->fail(TG_ERR_PARSE, "Empty file");
@@ -717,6 +729,7 @@ static tg_status d2h_pageable(tg_ctx* ctx, void* dst, const void* src, size_t by
 
 static tg_status tg_job_run_impl(tg_job* j) {
     if (!j) return TG_ERR_ARG;
+    const TraceRange tr("tuna.job_run");
     tg_ctx* ctx = j->ctx;
     if (j->ran) return ctx->fail(TG_ERR_STATE, "job already ran");
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
@@ -748,6 +761,7 @@ static tg_status tg_job_run_impl(tg_job* j) {
     unsigned long long n_bases = 0;
     CK(cudaMemcpyAsync(&n_bases, ctx->misc.as<uint8_t>() + MISC_BASES, 8, cudaMemcpyDeviceToHost, ctx->st), "d2h");
     // ---- phase 1: cut
+    nvtxMarkA("tuna.phase1");
     uint32_t p1 = j->o.gpu_parts;
     if (!p1) p1 = std::max(j->n_shards, std::min<uint32_t>(1024, std::max<uint32_t>(16, next_pow2_u32(n / 32768))));
     uint32_t p1_bits = 0;
@@ -781,6 +795,7 @@ static tg_status tg_job_run_impl(tg_job* j) {
     CK(cudaMemcpyAsync(nd.data(), ctx->misc.as<uint8_t>() + MISC_NDESC, (size_t)C * 4, cudaMemcpyDeviceToHost,
                        ctx->st), "d2h");
     CK(cudaStreamSynchronize(ctx->st), "phase 1");
+    nvtxMarkA("tuna.phase2");
     // ---- phase 2: one run over all bins or, when their keys and pairs do not
     // fit in the memory budget, passes over ranges of consecutive segments
     // (bins), each pass's pairs going to host memory before the next
@@ -1070,6 +1085,7 @@ constexpr uint64_t DRAIN_PAIRS = 1ull << 20;
 
 static tg_status tg_job_drain_impl(tg_job* j, tg_format fmt, tg_sink_fn sink, void* user) {
     if (!j || !sink || (int)fmt < 0 || (int)fmt > 2) return TG_ERR_ARG;
+    const TraceRange tr("tuna.drain");
     tg_ctx* ctx = j->ctx;
     if (!j->ran) return ctx->fail(TG_ERR_STATE, "drain before run");
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
@@ -1175,6 +1191,7 @@ tg_status tg_job_write(tg_job* j, tg_format fmt, const char* path) {
 
 static tg_status tg_job_export_partitions_impl(tg_job* j, tg_part_sink_fn sink, void* user) {
     if (!j || !sink) return TG_ERR_ARG;
+    const TraceRange tr("tuna.export_partitions");
     tg_ctx* ctx = j->ctx;
     if (!j->ran) return ctx->fail(TG_ERR_STATE, "export before run");
     if (j->sample_start.size() > 1) return ctx->fail(TG_ERR_UNSUPPORTED, "partition export of a job of several samples");
