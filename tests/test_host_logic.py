@@ -1,7 +1,8 @@
 """Host-side logic that needs no GPU: the server's batching policy
 (tuna_gb300.serve.take_batch), what the server does when no worker can open a
-device context, and the bench's clock-sample parsing (bench.parse_clock_lines),
-whose throttle reasons decide whether a bench number is kept."""
+device context, the bench's clock-sample parsing (bench.parse_clock_lines),
+whose throttle reasons decide whether a bench number is kept, and the
+library's host-side planning (launch shapes, buffer bounds, bin layout)."""
 import os
 import sys
 from collections import deque
@@ -66,3 +67,30 @@ def test_server_without_a_device_fails_requests():
             time.sleep(0.02)
         with pytest.raises(RuntimeError, match="no worker could open a device context"):
             srv.submit(seq, 31, 21)
+
+
+def test_host_planning_invariants(tmp_path):
+    """The library's host-side planning (tests/cpp/host_plan_check.cu, linked
+    against libtuna_gpu.so, run without a GPU): the phase-1 cut fits in shared
+    memory for every (k, m) the GPU path takes, buffer and output size bounds,
+    the record-descriptor packing, and the sharing of the 2^20 bins among a
+    job's samples (powers of two, contiguous, proportional, segments covering
+    each sample's bins)."""
+    import shutil
+    import subprocess
+
+    import pytest
+    import tuna_gb300.build as B
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not found")
+    lib = B.gpu_lib()
+    exe = str(tmp_path / "host_plan_check")
+    src = os.path.join(ROOT, "tests", "cpp", "host_plan_check.cu")
+    r = subprocess.run([nvcc, *B.ARCH, "-std=c++17", "-O2", "--expt-relaxed-constexpr",
+                        "-I", os.path.join(ROOT, "tuna_gb300", "csrc"), "-I", os.path.join(ROOT, "include"),
+                        src, "-o", exe, "-L", os.path.dirname(lib), "-ltuna_gpu",
+                        "-Xlinker", "-rpath," + os.path.dirname(lib)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and r.stdout.strip().endswith("OK"), r.stdout + r.stderr
