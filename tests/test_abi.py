@@ -33,3 +33,27 @@ def test_version_and_device_count_without_gpu():
     assert b"tuna-gb300" in lib.tg_version()
     lib.tg_device_count.restype = ctypes.c_int
     assert lib.tg_device_count() >= 0
+
+
+def test_c_program_against_the_abi(tmp_path):
+    """tests/cpp/abi_check.c: the header compiles as C11 (-pedantic -Werror),
+    links against the library, and every entry point answers null or
+    out-of-range arguments with its documented status without a device;
+    tg_read_input reads a file and reports a short buffer and a missing file."""
+    import shutil
+    import subprocess
+
+    import pytest
+    if not shutil.which("gcc"):
+        pytest.skip("gcc not found")
+    lib = B.gpu_lib()
+    exe = str(tmp_path / "abi_check")
+    r = subprocess.run(["gcc", "-std=c11", "-Wall", "-Wextra", "-pedantic", "-Werror",
+                        "-I", os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "cpp", "abi_check.c"),
+                        "-o", exe, "-L", os.path.dirname(lib), "-ltuna_gpu", "-Wl,-rpath," + os.path.dirname(lib)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    inp = tmp_path / "in.fa"
+    inp.write_bytes(b">a\nACGTA\n")
+    r = subprocess.run([exe, str(inp)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.strip().endswith("OK"), r.stdout + r.stderr

@@ -82,9 +82,9 @@ struct Carve {
 
 }  // namespace
 
-extern "C" tg_status tg_count_seq_device_noalloc(const tg_job_opts* opts, const uint8_t* d_seq, size_t len,
-                                                 uint64_t* d_keys, uint32_t* d_counts, uint64_t cap,
-                                                 uint64_t* n_out, void* stream, char* errbuf, size_t errlen) {
+static tg_status count_noalloc(const tg_job_opts* opts, const uint8_t* d_seq, size_t len, uint64_t* d_keys,
+                               uint32_t* d_counts, uint64_t cap, uint64_t* n_out, void* stream, char* errbuf,
+                               size_t errlen) {
     if (!opts || !n_out || (!d_seq && len)) { set_err(errbuf, errlen, "null argument"); return TG_ERR_ARG; }
     *n_out = 0;
     const tg_job_opts& o = *opts;
@@ -204,4 +204,19 @@ extern "C" tg_status tg_count_seq_device_noalloc(const tg_job_opts* opts, const 
     }
 #undef NA_CK
     return TG_OK;
+}
+
+// Host-side C++ failures (the bin layout's vectors, messages) become a status:
+// no exception crosses the C ABI.
+extern "C" tg_status tg_count_seq_device_noalloc(const tg_job_opts* opts, const uint8_t* d_seq, size_t len,
+                                                 uint64_t* d_keys, uint32_t* d_counts, uint64_t cap,
+                                                 uint64_t* n_out, void* stream, char* errbuf, size_t errlen) {
+    try {
+        return count_noalloc(opts, d_seq, len, d_keys, d_counts, cap, n_out, stream, errbuf, errlen);
+    } catch (const std::exception& x) {
+        if (errbuf && errlen) snprintf(errbuf, errlen, "host: %s", x.what());
+    } catch (...) {
+        if (errbuf && errlen) snprintf(errbuf, errlen, "host: unknown exception");
+    }
+    return TG_ERR_OOM;
 }
