@@ -15,6 +15,17 @@
 //   k_fmt*      (tg_job_drain / tg_job_write) pairs -> TSV / KFF / raw bytes
 // The export of partition files runs the tile cut k_cut<true> instead, which
 // also yields each record's exact minimizer position.
+//
+// Reference counterparts (paths relative to the reference project root): a
+// job is run<k,m> / run_callback<k,m> (src/pipeline.hpp:64-264, :273-330) with
+// the input of SeqSource::process (src/seq_source.hpp:190-205); tg_job_stats
+// carries what the stderr lines report (src/pipeline.hpp:174-178); the drain
+// and tg_job_write are write_counts / write_counts_kff (src/count.hpp:180-265,
+// src/kff_output.hpp:42-57); tg_job_export_partitions writes the disk
+// pipeline's hash_<p>.superkmers (src/pipeline.hpp:186-201,
+// src/superkmer_io.hpp:154-172); the one-call entry points are count_to_raw
+// (include/tuna/tuna.hpp:181-195); passes over ranges of bins take the place
+// of the disk mode (src/pipeline.hpp:77-98, :186-263).
 #include <cuda_runtime.h>
 #include <nvtx3/nvToolsExt.h>
 

@@ -15,6 +15,13 @@
 //   keys    u64 x W [K]      every canonical k-mer instance, grouped by bin
 //                            (W = 1 for k <= 31)
 //   out     keys + u32 counts of the distinct k-mers that pass ci/cx
+//
+// Reference counterparts (paths relative to the reference project root):
+// kache codes src/partition_hash.hpp:68-70; the record byte layout the packed
+// bases mirror src/superkmer_io.hpp:3-19; ntHash seeds and roll terms of
+// HashTables include/nt_hash.hpp:26-124; the per-partition buckets the bins
+// replace src/partition_hash.hpp:550-552; keys in the word layout of
+// include/kache-hash/Kmer.hpp:38-48.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -33,6 +40,7 @@ constexpr uint32_t NONE32 = 0xFFFFFFFFu;
 constexpr uint32_t EV_OWNED = 1u;   // record start owned by this CTA
 constexpr uint32_t EV_CUT = 2u;     // cut (record start of any owner or run end)
 
+// ntHash tables for one m (include/nt_hash.hpp:26-40 seeds, :71-72 roll).
 struct HashTables {
     // indexed by kache codes: FW[b] = FWD[nt(b)], RV[b] = REV[nt(b)]
     uint64_t FW[4], RV[4];

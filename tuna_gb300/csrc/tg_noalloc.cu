@@ -14,7 +14,8 @@
 // loaded on a device and that stays reserved until the process exits.
 //
 // It runs the same kernels as tg_job_run on the same parameters, so its output
-// is the same set of (k-mer, count) pairs. Inputs longer than
+// is the same set of (k-mer, count) pairs: the counting of run_callback<k,m>
+// (src/pipeline.hpp:273-330 of the reference) over a sequence stream. Inputs longer than
 // TG_NOALLOC_MAX_LEN bytes are rejected; so is an input whose intermediate
 // arrays would not fit in the scratch array.
 #include <cuda_runtime.h>
