@@ -108,3 +108,14 @@ def test_bgzf_claiming_more_than_memory_fails_cleanly(tmp_path):
         T.read_input(p, threads=4, cap=1 << 20)
     assert "host:" in str(e.value) or "Cannot read" in str(e.value)
     assert T.read_input(_write(tmp_path, "ok.gz", bgzf(b"ACGT\n"))) == b"ACGT\n"  # still usable
+
+
+def test_inflated_far_beyond_the_first_guess(tmp_path):
+    """A file that inflates to far more than the first buffer guess (64 x the
+    compressed size) is read again at the size the library reports."""
+    import gzip
+    data = b">a\n" + b"A" * 20_000_000 + b"\n"
+    p = _write(tmp_path, "big.fa.gz", gzip.compress(data, 9))
+    assert os.path.getsize(p) * 64 < len(data)
+    assert T.read_input(p) == data
+    assert T.read_input(_write(tmp_path, "big_bgzf.fa.gz", bgzf(data)), threads=4) == data

@@ -376,10 +376,15 @@ def read_input(path: str, threads: int = 0, cap: Optional[int] = None) -> bytes:
     L = library()
     if cap is None:
         cap = max(1 << 20, 64 * os.path.getsize(path)) if os.path.exists(path) else 1 << 20
-    out = np.empty(cap, dtype=np.uint8)
     n = ctypes.c_size_t()
     err = ctypes.create_string_buffer(512)
-    rc = L.tg_read_input(os.fsencode(path), threads, out.ctypes.data, cap, ctypes.byref(n), err, 512)
+    for _ in range(2):  # a short buffer is answered with the size needed: read again once
+        out = np.empty(cap, dtype=np.uint8)
+        rc = L.tg_read_input(os.fsencode(path), threads, out.ctypes.data, cap, ctypes.byref(n), err, 512)
+        if rc == 1 and n.value > cap:
+            cap = n.value
+            continue
+        break
     if rc != 0:
         raise GpuError(rc, err.value.decode(errors="replace"))
     return out[: n.value].tobytes()
