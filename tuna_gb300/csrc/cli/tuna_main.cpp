@@ -49,7 +49,8 @@ static void print_usage(const char* prog) {
                  "  -t  <int>   host threads                [default: 1]\n"
                  "  -ci <int>   minimum k-mer count         [default: 1]\n"
                  "  -cx <int>   maximum k-mer count         [default: max]\n"
-                 "  -ram <int>  RAM budget in GB            [default: auto-detect available RAM]\n"
+                 "  -ram <int>  RAM budget in GB            [accepted; phase 2 budgets device memory\n"
+                 "              and runs in passes when a job does not fit]\n"
                  "  -w  <dir>   working directory for temp files\n"
                  "              [default: tuna_tmp/ next to output file]\n\n"
                  "  -hp         hide progress messages\n"
