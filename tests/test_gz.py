@@ -119,3 +119,37 @@ def test_inflated_far_beyond_the_first_guess(tmp_path):
     assert os.path.getsize(p) * 64 < len(data)
     assert T.read_input(p) == data
     assert T.read_input(_write(tmp_path, "big_bgzf.fa.gz", bgzf(data)), threads=4) == data
+
+
+def _member(chunk: bytes, pre_sub: bytes = b"") -> bytes:
+    """One BGZF member whose extra field holds `pre_sub` before the BC subfield."""
+    c = zlib.compressobj(6, zlib.DEFLATED, -15)
+    payload = c.compress(chunk) + c.flush()
+    xlen = len(pre_sub) + 6
+    bsize = 12 + xlen + len(payload) + 8
+    out = b"\x1f\x8b\x08\x04\x00\x00\x00\x00\x00\xff" + xlen.to_bytes(2, "little") + pre_sub
+    out += b"BC" + (2).to_bytes(2, "little") + (bsize - 1).to_bytes(2, "little")
+    return out + payload + zlib.crc32(chunk).to_bytes(4, "little") + len(chunk).to_bytes(4, "little")
+
+
+def test_bgzf_edge_cases(tmp_path):
+    """Other extra subfields before BC are skipped; a file that is not entirely
+    BGZF members (truncated, or with bytes after the last member) is read as one
+    gzip stream, as the reference's gzread loop reads every .gz file: a truncated
+    file gives the bytes that inflate, trailing bytes are ignored. A member whose
+    CRC does not match fails ("Cannot read"), where the reference's loop stops
+    at the error and counts what it read before."""
+    data = b">s\n" + b"ACGT" * 50000 + b"\n"
+    chunks = [data[i:i + 30000] for i in range(0, len(data), 30000)]
+    sub = b"RA" + (4).to_bytes(2, "little") + b"abcd"
+    p = _write(tmp_path, "sub.gz", b"".join(_member(c, sub) for c in chunks) + BGZF_EOF)
+    assert T.read_input(p, threads=4) == data
+    full = bgzf(data, block=30000)
+    got = T.read_input(_write(tmp_path, "trunc.gz", full[:-40]), threads=4)
+    assert 0 < len(got) < len(data) and data.startswith(got)
+    assert T.read_input(_write(tmp_path, "tail.gz", full + b"garbage!"), threads=4) == data
+    bad = bytearray(full)
+    bad[-len(BGZF_EOF) - 8] ^= 1  # the last data member's CRC
+    with pytest.raises(T.GpuError) as e:
+        T.read_input(_write(tmp_path, "crc.gz", bytes(bad)), threads=4)
+    assert "Cannot read" in str(e.value)
