@@ -153,3 +153,13 @@ def test_bgzf_edge_cases(tmp_path):
     with pytest.raises(T.GpuError) as e:
         T.read_input(_write(tmp_path, "crc.gz", bytes(bad)), threads=4)
     assert "Cannot read" in str(e.value)
+
+
+@pytest.mark.parametrize("threads", [1, 3, 8])
+def test_large_plain_file_copied_out_on_threads(tmp_path, threads):
+    """tg_read_input hands a 100 MB file back through its multi-threaded copy
+    (shares of at least 16 MiB), byte for byte."""
+    rng = np.random.default_rng(threads)
+    data = b">s\n" + bytes(rng.choice(np.frombuffer(b"ACGTN\n", dtype=np.uint8), 100_000_000)) + b"\n"
+    p = _write(tmp_path, "big.fa", data)
+    assert T.read_input(p, threads=threads) == data

@@ -105,6 +105,31 @@ double now_ms() {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+// Host memcpy of n bytes on up to `threads` threads, each taking at least
+// min_share bytes; the calling thread copies the first share. A share whose
+// thread cannot be started is copied by the caller, so no joinable thread is
+// ever left behind by an exception.
+void parallel_copy(void* dst, const void* src, size_t n, unsigned threads, size_t min_share) {
+    const size_t most = std::max<size_t>(1, n / std::max<size_t>(1, min_share));
+    const unsigned nt = (unsigned)std::max<size_t>(1, std::min<size_t>(std::max(1u, threads), most));
+    const size_t per = (n + nt - 1) / nt;
+    auto part = [dst, src, n, per](unsigned t) {
+        const size_t a = std::min(n, (size_t)t * per), b = std::min(n, a + per);
+        if (b > a) memcpy(static_cast<uint8_t*>(dst) + a, static_cast<const uint8_t*>(src) + a, b - a);
+    };
+    std::vector<std::thread> th;
+    th.reserve(nt);
+    for (unsigned t = 1; t < nt; ++t) {
+        try {
+            th.emplace_back(part, t);
+        } catch (...) {
+            part(t);
+        }
+    }
+    part(0);
+    for (auto& t : th) t.join();
+}
+
 }  // namespace
 
 struct tg_ctx {
@@ -577,17 +602,8 @@ static tg_status tg_read_input_impl(const char* path, uint32_t threads, uint8_t*
         return TG_ERR_ARG;
     }
     // the copy out, on the same threads for large files
-    const unsigned nt = (unsigned)std::min<size_t>(threads ? threads : std::max(1u, std::thread::hardware_concurrency()),
-                                                   std::max<size_t>(1, raw.size() >> 24));
-    const size_t per = (raw.size() + nt - 1) / nt;
-    std::vector<std::thread> th;
-    for (unsigned t = 1; t < nt; ++t)
-        th.emplace_back([&, t] {
-            const size_t a = std::min(raw.size(), t * per), b = std::min(raw.size(), a + per);
-            if (b > a) memcpy(out + a, raw.data() + a, b - a);
-        });
-    if (!raw.empty()) memcpy(out, raw.data(), std::min(raw.size(), per));
-    for (auto& t : th) t.join();
+    parallel_copy(out, raw.data(), raw.size(), threads ? threads : std::max(1u, std::thread::hardware_concurrency()),
+                  16u << 20);
     return TG_OK;
 }
 
@@ -725,15 +741,7 @@ static tg_status d2h_pageable(tg_ctx* ctx, void* dst, const void* src, size_t by
         if (c + 1 < n_ch) CK(issue(c + 1), "d2h");  // the other buffer was emptied in the previous step
         CK(cudaEventSynchronize(ctx->ev[4 + (c & 1)]), "d2h");
         const size_t off = c * CH, len = std::min(CH, bytes - off);
-        const size_t per = (len + nt - 1) / nt;
-        std::vector<std::thread> th;
-        for (unsigned t = 1; t < nt; ++t)
-            th.emplace_back([&, t] {
-                const size_t a = std::min(len, t * per), b = std::min(len, a + per);
-                if (b > a) memcpy(static_cast<uint8_t*>(dst) + off + a, ctx->stage[c & 1] + a, b - a);
-            });
-        memcpy(static_cast<uint8_t*>(dst) + off, ctx->stage[c & 1], std::min(len, per));
-        for (auto& t : th) t.join();
+        parallel_copy(static_cast<uint8_t*>(dst) + off, ctx->stage[c & 1], len, nt, 1u << 20);
     }
     return TG_OK;
 }
@@ -1053,8 +1061,8 @@ tg_status tg_job_result_copy(tg_job* j, uint64_t* keys, uint32_t* counts, uint64
     if (first + n > j->n_out) return ctx->fail(TG_ERR_ARG, "result range out of bounds");
     if (!n) return TG_OK;
     if (j->spilled) {  // phase 2 ran in passes: the pairs are in host memory
-        if (keys) memcpy(keys, j->host_keys.data() + first * j->W, n * 8 * (size_t)j->W);
-        if (counts) memcpy(counts, j->host_counts.data() + first, n * 4);
+        if (keys) parallel_copy(keys, j->host_keys.data() + first * j->W, n * 8 * (size_t)j->W, ctx->host_threads, 16u << 20);
+        if (counts) parallel_copy(counts, j->host_counts.data() + first, n * 4, ctx->host_threads, 16u << 20);
         return TG_OK;
     }
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
