@@ -310,7 +310,14 @@ bool bgzf_inflate(const Zlib& Z, const uint8_t* d, const std::vector<BgzfBlock>&
     };
     threads = std::max(1u, std::min<unsigned>(threads, (unsigned)((blocks.size() + per - 1) / per)));
     std::vector<std::thread> th;
-    for (unsigned t = 1; t < threads; ++t) th.emplace_back(work);
+    th.reserve(threads);
+    for (unsigned t = 1; t < threads; ++t) {
+        try {
+            th.emplace_back(work);
+        } catch (...) {
+            break;  // blocks are claimed from a shared counter: fewer threads take them all
+        }
+    }
     work();
     for (auto& t : th) t.join();
     return !bad;
