@@ -555,6 +555,19 @@ static void p1_rec_cb(uint64_t pid, const uint8_t* rec, size_t nb, uint64_t mh, 
     j->n_sk++;
 }
 
+/* fn(args[t]) for t < threads, on threads th[t]; a worker whose thread cannot
+ * be started runs on the calling thread instead. */
+static void run_workers(void* (*fn)(void*), void* args, size_t arg_size, int threads, pthread_t* th) {
+    unsigned char started[256] = {0}; /* threads <= 256 (clamp_threads) */
+    for (int t = 0; t < threads; ++t) {
+        void* a = (char*)args + (size_t)t * arg_size;
+        if (t < 256 && pthread_create(&th[t], NULL, fn, a) == 0) started[t] = 1;
+        else fn(a);
+    }
+    for (int t = 0; t < threads && t < 256; ++t)
+        if (started[t]) pthread_join(th[t], NULL);
+}
+
 static void* p1_worker(void* arg) {
     p1_job* j = (p1_job*)arg;
     for (size_t r = j->r0; r < j->r1; ++r) {
@@ -702,8 +715,7 @@ static p1_job* run_phase1(const uint8_t* seq, size_t len, int k, int m, uint64_t
         while (r < n_runs && (acc < goal || t == threads - 1)) { acc += runs[r].len; ++r; }
         jobs[t].r1 = r;
     }
-    for (int t = 0; t < threads; ++t) pthread_create(&th[t], NULL, p1_worker, &jobs[t]);
-    for (int t = 0; t < threads; ++t) pthread_join(th[t], NULL);
+    run_workers(p1_worker, jobs, sizeof(p1_job), threads, th);
     free(th);
     /* spans no longer needed after phase 1 */
     bb_free(&sp);
@@ -750,8 +762,8 @@ static tor_result* count_stream_impl(const uint8_t* seq, size_t len, int k, int 
     atomic_store(&c.next, 0);
     p2_job* pj = (p2_job*)calloc((size_t)threads, sizeof(p2_job));
     pthread_t* th = (pthread_t*)calloc((size_t)threads, sizeof(pthread_t));
-    for (int t = 0; t < threads; ++t) { pj[t].c = &c; pthread_create(&th[t], NULL, p2_worker, &pj[t]); }
-    for (int t = 0; t < threads; ++t) pthread_join(th[t], NULL);
+    for (int t = 0; t < threads; ++t) pj[t].c = &c;
+    run_workers(p2_worker, pj, sizeof(p2_job), threads, th);
     free(th);
     const int nw = (k + 31) / 32;
     tor_result* r = (tor_result*)calloc(1, sizeof(tor_result));

@@ -163,12 +163,21 @@ static void* genome_worker(void* arg) {
     return NULL;
 }
 
+/* fn pulls chunks from the job's shared counter: if a thread cannot be
+ * started, the calling thread runs fn too and the started ones share the rest. */
 static void run_threads(void* (*fn)(void*), void* job, int threads) {
     if (threads < 1) threads = 1;
     if (threads > 256) threads = 256;
     pthread_t th[256];
-    for (int i = 0; i < threads; ++i) pthread_create(&th[i], NULL, fn, job);
-    for (int i = 0; i < threads; ++i) pthread_join(th[i], NULL);
+    int started[256];
+    int missing = 0;
+    for (int i = 0; i < threads; ++i) {
+        started[i] = pthread_create(&th[i], NULL, fn, job) == 0;
+        missing |= !started[i];
+    }
+    if (missing) fn(job);
+    for (int i = 0; i < threads; ++i)
+        if (started[i]) pthread_join(th[i], NULL);
 }
 
 /* Returns 0. out must hold len bytes. Repeat parameters of zero disable. */
