@@ -57,3 +57,36 @@ def test_c_program_against_the_abi(tmp_path):
     inp.write_bytes(b">a\nACGTA\n")
     r = subprocess.run([exe, str(inp)], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0 and r.stdout.strip().endswith("OK"), r.stdout + r.stderr
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """The ctypes mirrors of tg_ctx_opts, tg_job_opts and tg_stats have the C
+    header's size and field offsets (a C program prints them; a field name the
+    header lacks does not compile)."""
+    import json
+    import shutil
+    import subprocess
+
+    import pytest
+    import tuna_gb300 as T
+    if not shutil.which("gcc"):
+        pytest.skip("gcc not found")
+    structs = {"tg_ctx_opts": T._CtxOpts, "tg_job_opts": T._JobOpts, "tg_stats": T._Stats}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "tuna_gpu.h"', "int main(void) {",
+             '    printf("{");']
+    for i, (name, cls) in enumerate(structs.items()):
+        lines.append(f'    printf("{"," if i else ""}\\"{name}\\": [%zu", sizeof({name}));')
+        for f, _ in cls._fields_:
+            lines.append(f'    printf(", %zu", offsetof({name}, {f}));')
+        lines.append('    printf("]");')
+    lines += ['    printf("}\\n");', "    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = str(tmp_path / "layout")
+    r = subprocess.run(["gcc", "-std=c11", "-Wall", "-I", os.path.join(ROOT, "include"), str(src), "-o", exe],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = json.loads(subprocess.run([exe], capture_output=True, text=True, check=True).stdout)
+    for name, cls in structs.items():
+        want = [ctypes.sizeof(cls)] + [getattr(cls, f).offset for f, _ in cls._fields_]
+        assert got[name] == want, name
