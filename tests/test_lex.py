@@ -109,6 +109,50 @@ def test_lexer_rules_match_block_walk():
     assert flagged < 60
 
 
+def test_host_parser_matches_oracle(tmp_path):
+    """The library's host parser (tgh::fastx_to_stream, the path of the FASTQ
+    files the device lexer flags), driven on CPU by tests/cpp/host_parser_check.cpp
+    over fuzzed files, plain and gzip: the same runs as the oracle's parser,
+    including the block-walk cases the lexer hands over."""
+    import gzip
+    import os
+    import shutil
+    import subprocess
+
+    import tuna_gb300.build as B
+    if not shutil.which("g++"):
+        pytest.skip("g++ not found")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    lib = B.gpu_lib()
+    exe = str(tmp_path / "host_parser_check")
+    r = subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(root, "tuna_gb300", "csrc"),
+                        "-I", os.path.join(root, "include"), os.path.join(root, "tests", "cpp", "host_parser_check.cpp"),
+                        "-o", exe, "-L", os.path.dirname(lib), "-ltuna_gpu", "-Wl,-rpath," + os.path.dirname(lib)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    rng = random.Random(23)
+    cases, paths = [], []
+    for i in range(1500):
+        s = fuzz_case(rng)
+        if i % 10 == 0:  # a FASTQ record in front: the rest is read with FASTQ rules
+            s = b"@r\nACGT\n+\nIIII\n" + s
+        name = str(tmp_path / (f"c{i}.fq.gz" if i % 7 == 0 else f"c{i}.fa"))
+        with open(name, "wb") as f:
+            f.write(gzip.compress(s) if name.endswith(".gz") else s)
+        cases.append(s)
+        paths.append(name)
+    for i in range(0, len(paths), 500):
+        r = subprocess.run([exe, *paths[i:i + 500]], capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr
+    flagged = 0
+    for s, name in zip(cases, paths):
+        _, irregular = lexer_rules(s)
+        flagged += irregular
+        with open(name + ".stream", "rb") as f:
+            assert runs(f.read()) == O.parse_fastx(s), s[:200]
+    assert flagged > 0  # the block-walk departures were among the cases
+
+
 # ------------------------------------------------------------------ GPU
 
 def _ctx():
