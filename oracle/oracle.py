@@ -175,6 +175,26 @@ def count_fastx(data, k: int, m: int, n_parts: int = 16, ci: int = 1,
     return _take(p, k, st)
 
 
+def write_kff_stream(seq, k: int, m: int, path: str, n_parts: int = 16, ci: int = 1,
+                     cx: int = (1 << 64) - 1, threads: int = 1) -> int:
+    """Count a sequence stream and write the pairs as a KFF file, as the
+    reference's kff_output.hpp lays it out; returns the number of pairs."""
+    buf = _as_u8(seq)
+    st = _Stats()
+    L = lib()
+    p = L.tor_count_stream(buf.ctypes.data if buf.size else None, buf.size, k, m, n_parts, ci, cx, threads,
+                           ctypes.byref(st))
+    if not p:
+        raise ValueError("oracle rejected the parameters")
+    try:
+        n = int(L.tor_result_size(p))
+        if L.tor_write_kff(p, k, os.fsencode(path)) != 0:
+            raise OSError(f"cannot write {path}")
+    finally:
+        L.tor_result_free(p)
+    return n
+
+
 def partition_stream(seq, k: int, m: int, n_parts: int, threads: int = 1) -> List[bytes]:
     """Phase 1 only: the concatenated records of each partition, in the
     reference's superkmer file layout."""
