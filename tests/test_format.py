@@ -74,4 +74,3 @@ def test_drain_many_batches():
     lines = res.formatted.split(b"\n")[:-1]
     assert len(lines) == len(res)
     assert res.formatted == _tsv(res)
-
