@@ -94,3 +94,10 @@ def test_host_planning_invariants(tmp_path):
     assert r.returncode == 0, r.stdout + r.stderr
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0 and r.stdout.strip().endswith("OK"), r.stdout + r.stderr
+
+
+def test_server_needs_a_worker():
+    import pytest
+    from tuna_gb300 import serve
+    with pytest.raises(ValueError):
+        serve.Server(0, workers=0)

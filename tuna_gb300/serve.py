@@ -67,6 +67,8 @@ def _pinned(n: int, dtype):
 class Server:
     def __init__(self, device: int = 0, workers: int = 2, max_batch_bases: Optional[int] = None,
                  host_threads: int = 0):
+        if workers < 1:
+            raise ValueError("a server needs at least one worker")
         import tuna_gb300 as T
         self._T = T
         self._L = T.library()
