@@ -22,6 +22,8 @@
  *   tg_job_drain                     write_counts / write_counts_kff /
  *                                    write_counts_callback (src/count.hpp:180-298)
  *   tg_job_result_copy               count_to_raw (include/tuna/tuna.hpp:181-195)
+ *   tg_job_result_digest             no counterpart: a checksum of the output lines of
+ *                                    write_counts (src/count.hpp:180-216), any order
  *   tg_job_export_partitions         the hash_<p>.superkmers files of the disk
  *                                    pipeline (src/superkmer_io.hpp:3-19, -tp -kt)
  *   tg_job_stats                     the phase1:/phase2:/superkmers:/unique_kmers:
@@ -190,6 +192,24 @@ int tg_job_key_words(const tg_job* job);
  * same order every call). keys: n * key_words u64; counts: n u32. */
 tg_status tg_job_result_copy(tg_job* job, uint64_t* keys, uint32_t* counts,
                              uint64_t first, uint64_t n);
+/* Order-independent digest of results [first, first + n): the check of an
+ * output against another (the reference's TSV, a CPU count) when the outputs
+ * are too large to sort and compare. The reference's output contract is the
+ * multiset of (canonical k-mer, count) lines in any order (write_counts,
+ * src/count.hpp:180-216); each pair maps to two 64-bit terms and the terms are
+ * summed mod 2^64:
+ *   words w[0..nw), nw = ceil(k/32), in the tuna::Kmer<k> layout
+ *   a = 0x243F6A8885A308D3; b = 0x13198A2E03707344
+ *   for i in 0..nw-1: a = fa(a ^ w[i]); b = fb(b + w[i])
+ *   h1 += fa(a ^ (count | 1 << 40)); h2 += fb(b + (count ^ 0xA4093822299F31D0))
+ * with fa MurmurHash3's 64-bit finaliser and fb SplitMix64's. Computed on the
+ * device (or on host threads for a job whose pairs are in host memory). */
+typedef struct {
+    uint64_t pairs;      /* n */
+    uint64_t count_sum;  /* sum of the counts */
+    uint64_t h1, h2;     /* the two digests */
+} tg_digest;
+tg_status tg_job_result_digest(tg_job* job, uint64_t first, uint64_t n, tg_digest* out);
 /* Format results on the device and hand them to sink in chunks. */
 tg_status tg_job_drain(tg_job* job, tg_format fmt, tg_sink_fn sink, void* user);
 /* Write results to a file: TSV, or a complete KFF file when fmt == TG_FMT_KFF. */

@@ -8,9 +8,14 @@
 # and the KFF stand-in in oracle/ref_stub/ (TSV output only).
 #
 # Usage: oracle/build_ref.sh [REF_ROOT] [k:m ...]
+# REF_ROOT defaults to $TUNA_REFERENCE, else the benchmark's reference_path.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${TUNA_REFERENCE:-}}"
+if [ -z "$REF" ]; then
+  REF="$(python3 -c 'import json,sys; print(json.load(open(sys.argv[1])).get("reference_path", ""))' \
+         "$HERE/../BASELINE.json" 2>/dev/null || true)"
+fi
 shift || true
 PAIRS=("$@")
 if [ ${#PAIRS[@]} -eq 0 ]; then

@@ -18,24 +18,47 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD, "libtuna_oracle.so")
 SRC = os.path.join(HERE, "tuna_oracle.c")
+DIGEST_H = os.path.join(HERE, "tuna_digest.h")
+TSV_DIGEST_SRC = os.path.join(HERE, "tsv_digest.c")
+TSV_DIGEST_BIN = os.path.join(BUILD, "tsv_digest")
 
 _lib = None
 
 
+def _stale(target: str, *srcs: str) -> bool:
+    return not os.path.exists(target) or any(os.path.getmtime(target) < os.path.getmtime(s) for s in srcs)
+
+
 def build(force: bool = False) -> str:
-    """Compile the oracle shared library (portable C11, no ISA flags)."""
+    """Compile the oracle shared library and the TSV digester (portable C11,
+    no ISA flags)."""
     os.makedirs(BUILD, exist_ok=True)
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(SRC):
+    hdr = os.path.join(HERE, "tuna_oracle.h")
+    if force or _stale(LIB_PATH, SRC, hdr, DIGEST_H):
         tmp = LIB_PATH + ".tmp"
         subprocess.check_call(["gcc", "-O3", "-std=c11", "-shared", "-fPIC", "-pthread",
                                SRC, "-o", tmp])
         os.replace(tmp, LIB_PATH)
+    if force or _stale(TSV_DIGEST_BIN, TSV_DIGEST_SRC, DIGEST_H):
+        tmp = TSV_DIGEST_BIN + ".tmp"
+        subprocess.check_call(["gcc", "-O3", "-std=c11", TSV_DIGEST_SRC, "-o", tmp])
+        os.replace(tmp, TSV_DIGEST_BIN)
     return LIB_PATH
 
 
 class _Stats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in
                 ("n_runs", "n_kmers", "n_superkmers", "n_distinct", "n_out", "record_bytes")]
+
+
+class _Digest(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in ("pairs", "count_sum", "h1", "h2")]
+
+
+def digest_dict(d) -> Dict[str, object]:
+    """The digest as stored in the golden fixtures (hashes as 16 hex digits)."""
+    return {"pairs": int(d.pairs), "count_sum": int(d.count_sum),
+            "h1": f"{int(d.h1):016x}", "h2": f"{int(d.h2):016x}"}
 
 
 _RUN_CB = ctypes.CFUNCTYPE(None, ctypes.POINTER(ctypes.c_uint8), ctypes.c_size_t, ctypes.c_void_p)
@@ -63,6 +86,14 @@ def lib():
         L.tor_result_counts.argtypes = [vp]
         L.tor_result_counts.restype = ctypes.POINTER(ctypes.c_uint32)
         L.tor_result_free.argtypes = [vp]
+        for fn in (L.tor_digest_stream, L.tor_digest_fastx):
+            fn.argtypes = [vp, ctypes.c_size_t, i32, i32, u64, u64, u64, i32, ctypes.POINTER(_Stats),
+                           ctypes.POINTER(_Digest)]
+            fn.restype = i32
+        L.tor_result_digest.argtypes = [vp, ctypes.POINTER(_Digest)]
+        L.tor_result_digest.restype = None
+        L.tor_digest_pairs.argtypes = [vp, i32, i32, vp, u64, ctypes.POINTER(_Digest)]
+        L.tor_digest_pairs.restype = None
         L.tor_partition_stream.argtypes = [vp, ctypes.c_size_t, i32, i32, u64, i32]
         L.tor_partition_stream.restype = vp
         L.tor_parts_data.argtypes = [vp]
@@ -173,6 +204,52 @@ def count_fastx(data, k: int, m: int, n_parts: int = 16, ci: int = 1,
     p = lib().tor_count_fastx(buf.ctypes.data, buf.size, k, m, n_parts, ci, cx, threads,
                               ctypes.byref(st))
     return _take(p, k, st)
+
+
+def digest_stream(seq, k: int, m: int, n_parts: int = 16, ci: int = 1,
+                  cx: int = (1 << 64) - 1, threads: int = 1, fastx: bool = False):
+    """Count a sequence stream (or FASTA/FASTQ bytes with fastx=True) and return
+    (digest dict, stats dict) without keeping the pairs: memory for Phase 1's
+    records and one partition table per thread, so it scales to the
+    full-size workloads."""
+    buf = _as_u8(seq)
+    if fastx and buf.size == 0:
+        raise RuntimeError("Empty file")
+    st = _Stats()
+    d = _Digest()
+    fn = lib().tor_digest_fastx if fastx else lib().tor_digest_stream
+    rc = fn(buf.ctypes.data if buf.size else None, buf.size, k, m, n_parts, ci, cx, threads,
+            ctypes.byref(st), ctypes.byref(d))
+    if rc != 0:
+        raise ValueError("oracle rejected the parameters")
+    return digest_dict(d), {f: int(getattr(st, f)) for f, _ in _Stats._fields_}
+
+
+def digest_pairs(keys: np.ndarray, counts: np.ndarray, k: int) -> Dict[str, object]:
+    """Digest of (keys, counts) arrays held in host memory (keys: (n, words)
+    uint64 in the Kmer<k> layout; only the first ceil(k/32) words count)."""
+    keys = np.ascontiguousarray(keys, dtype=np.uint64)
+    counts = np.ascontiguousarray(counts, dtype=np.uint32)
+    n = int(counts.shape[0])
+    stride = int(keys.shape[1]) if keys.ndim == 2 else 1
+    nw = (k + 31) // 32
+    if stride < nw or keys.size < n * stride:
+        raise ValueError("keys have fewer words than k needs")
+    d = _Digest()
+    lib().tor_digest_pairs(keys.ctypes.data if n else None, stride, nw, counts.ctypes.data if n else None, n,
+                           ctypes.byref(d))
+    return digest_dict(d)
+
+
+def tsv_digest_file(path: str) -> Dict[str, object]:
+    """Digest of a TSV file by the C digester (the program the goldens use)."""
+    build()
+    with open(path, "rb") as f:
+        r = subprocess.run([TSV_DIGEST_BIN], stdin=f, capture_output=True, check=True)
+    import json
+    d = json.loads(r.stdout)
+    d.pop("k", None)
+    return d
 
 
 def write_kff_stream(seq, k: int, m: int, path: str, n_parts: int = 16, ci: int = 1,

@@ -9,6 +9,7 @@
  */
 #define _GNU_SOURCE
 #include "tuna_oracle.h"
+#include "tuna_digest.h"
 
 #include <pthread.h>
 #include <stdatomic.h>
@@ -585,6 +586,7 @@ typedef struct {
     uint64_t n_parts;
     uint64_t ci, cx;
     _Atomic uint64_t next;
+    int digest_only;      /* fold the pairs into a digest instead of keeping them */
     /* per thread output */
     bbuf keys, cnts;
     uint64_t n_distinct, n_out;
@@ -594,6 +596,7 @@ typedef struct {
     p2_ctx* c;
     bbuf keys, cnts;
     uint64_t n_distinct, n_out;
+    tor_digest dg;
 } p2_job;
 
 static void* p2_worker(void* arg) {
@@ -625,9 +628,13 @@ static void* p2_worker(void* arg) {
             const uint32_t cnt = tab.cnt[i];
             if (!cnt) continue;
             if ((uint64_t)cnt < c->ci || (uint64_t)cnt > c->cx) continue;
+            pj->n_out++;
+            if (c->digest_only) {
+                tdg_add(&pj->dg, tab.keys + i * g.nw, g.nw, cnt);
+                continue;
+            }
             bb_put(&pj->keys, (const uint8_t*)(tab.keys + i * g.nw), g.nw * 8);
             bb_put(&pj->cnts, (const uint8_t*)&cnt, 4);
-            pj->n_out++;
         }
         kt_free(&tab);
     }
@@ -733,23 +740,25 @@ static void free_phase1(p1_job* jobs, int threads, uint64_t n_parts) {
 
 static tor_result* count_stream_impl(const uint8_t* seq, size_t len, int k, int m,
                                      uint64_t n_parts, uint64_t ci, uint64_t cx,
-                                     int threads, tor_stats* st, int sort_output);
+                                     int threads, tor_stats* st, int sort_output, tor_digest* dg);
 
 tor_result* tor_count_stream(const uint8_t* seq, size_t len, int k, int m,
                              uint64_t n_parts, uint64_t ci, uint64_t cx,
                              int threads, tor_stats* st) {
-    return count_stream_impl(seq, len, k, m, n_parts, ci, cx, threads, st, 1);
+    return count_stream_impl(seq, len, k, m, n_parts, ci, cx, threads, st, 1, NULL);
 }
 
 tor_result* tor_count_stream_unsorted(const uint8_t* seq, size_t len, int k, int m,
                                       uint64_t n_parts, uint64_t ci, uint64_t cx,
                                       int threads, tor_stats* st) {
-    return count_stream_impl(seq, len, k, m, n_parts, ci, cx, threads, st, 0);
+    return count_stream_impl(seq, len, k, m, n_parts, ci, cx, threads, st, 0, NULL);
 }
 
+/* With dg non-null the pairs are folded into *dg as they are found (memory for
+ * one partition's table per thread) and the result holds no pairs. */
 static tor_result* count_stream_impl(const uint8_t* seq, size_t len, int k, int m,
                                      uint64_t n_parts, uint64_t ci, uint64_t cx,
-                                     int threads, tor_stats* st, int sort_output) {
+                                     int threads, tor_stats* st, int sort_output, tor_digest* dg) {
     if (k < 2 || k > 256 || m < 1 || m > 32 || m >= k) return NULL;
     if (n_parts == 0 || (n_parts & (n_parts - 1))) return NULL;
     threads = clamp_threads(threads);
@@ -759,6 +768,7 @@ static tor_result* count_stream_impl(const uint8_t* seq, size_t len, int k, int 
     memset(&c, 0, sizeof c);
     c.jobs = jobs; c.nthreads = threads; c.k = k; c.m = m; c.n_parts = n_parts;
     c.ci = ci; c.cx = cx;
+    c.digest_only = dg != NULL;
     atomic_store(&c.next, 0);
     p2_job* pj = (p2_job*)calloc((size_t)threads, sizeof(p2_job));
     pthread_t* th = (pthread_t*)calloc((size_t)threads, sizeof(pthread_t));
@@ -770,14 +780,20 @@ static tor_result* count_stream_impl(const uint8_t* seq, size_t len, int k, int 
     r->nw = nw;
     uint64_t n_out = 0, n_distinct = 0;
     for (int t = 0; t < threads; ++t) { n_out += pj[t].n_out; n_distinct += pj[t].n_distinct; }
-    r->n = n_out;
-    r->keys = (uint64_t*)malloc((n_out ? n_out : 1) * nw * sizeof(uint64_t));
-    r->counts = (uint32_t*)malloc((n_out ? n_out : 1) * sizeof(uint32_t));
+    if (dg) {
+        memset(dg, 0, sizeof *dg);
+        for (int t = 0; t < threads; ++t) tdg_merge(dg, &pj[t].dg);
+    }
+    r->n = dg ? 0 : n_out;
+    r->keys = (uint64_t*)malloc((r->n ? r->n : 1) * nw * sizeof(uint64_t));
+    r->counts = (uint32_t*)malloc((r->n ? r->n : 1) * sizeof(uint32_t));
     uint64_t o = 0;
     for (int t = 0; t < threads; ++t) {
-        memcpy(r->keys + o * nw, pj[t].keys.p, pj[t].n_out * nw * 8);
-        memcpy(r->counts + o, pj[t].cnts.p, pj[t].n_out * 4);
-        o += pj[t].n_out;
+        if (!dg) {
+            memcpy(r->keys + o * nw, pj[t].keys.p, pj[t].n_out * nw * 8);
+            memcpy(r->counts + o, pj[t].cnts.p, pj[t].n_out * 4);
+            o += pj[t].n_out;
+        }
         bb_free(&pj[t].keys); bb_free(&pj[t].cnts);
     }
     free(pj);
@@ -812,6 +828,35 @@ tor_result* tor_count_fastx(const uint8_t* data, size_t len, int k, int m,
     tor_result* r = tor_count_stream(s.p ? s.p : (const uint8_t*)"", s.n, k, m, n_parts, ci, cx, threads, st);
     bb_free(&s);
     return r;
+}
+
+int tor_digest_stream(const uint8_t* seq, size_t len, int k, int m, uint64_t n_parts,
+                      uint64_t ci, uint64_t cx, int threads, tor_stats* st, tor_digest* dg) {
+    tor_result* r = count_stream_impl(seq, len, k, m, n_parts, ci, cx, threads, st, 0, dg);
+    if (!r) return -1;
+    tor_result_free(r);
+    return 0;
+}
+
+int tor_digest_fastx(const uint8_t* data, size_t len, int k, int m, uint64_t n_parts,
+                     uint64_t ci, uint64_t cx, int threads, tor_stats* st, tor_digest* dg) {
+    bbuf s = {0};
+    if (tor_parse_fastx(data, len, append_run, &s) != 0) return -1;
+    const int rc = tor_digest_stream(s.p ? s.p : (const uint8_t*)"", s.n, k, m, n_parts, ci, cx,
+                                     threads, st, dg);
+    bb_free(&s);
+    return rc;
+}
+
+void tor_digest_pairs(const uint64_t* keys, int stride, int nw, const uint32_t* counts, uint64_t n,
+                      tor_digest* dg) {
+    memset(dg, 0, sizeof *dg);
+    for (uint64_t i = 0; i < n; ++i) tdg_add(dg, keys + i * (uint64_t)stride, nw, counts[i]);
+}
+
+void tor_result_digest(const tor_result* r, tor_digest* dg) {
+    memset(dg, 0, sizeof *dg);
+    for (uint64_t i = 0; i < r->n; ++i) tdg_add(dg, r->keys + i * r->nw, r->nw, r->counts[i]);
 }
 
 tor_parts* tor_partition_stream(const uint8_t* seq, size_t len, int k, int m,

@@ -78,6 +78,21 @@ const uint64_t* tor_result_keys(const tor_result* r);
 const uint32_t* tor_result_counts(const tor_result* r);
 void tor_result_free(tor_result* r);
 
+/* Order-independent digest of the pairs (tuna_digest.h defines it). The
+ * *_digest_* pipelines keep no pairs: memory for Phase 1's records and one
+ * partition table per thread. Return 0, or -1 for rejected parameters / an
+ * empty FASTX buffer. */
+#include "tuna_digest.h"
+int tor_digest_stream(const uint8_t* seq, size_t len, int k, int m, uint64_t n_parts,
+                      uint64_t ci, uint64_t cx, int threads, tor_stats* st, tor_digest* dg);
+int tor_digest_fastx(const uint8_t* data, size_t len, int k, int m, uint64_t n_parts,
+                     uint64_t ci, uint64_t cx, int threads, tor_stats* st, tor_digest* dg);
+void tor_result_digest(const tor_result* r, tor_digest* dg);
+/* Digest of n pairs held in arrays: pair i's words are keys[i * stride ..
+ * i * stride + nw) (nw = ceil(k/32) <= stride). */
+void tor_digest_pairs(const uint64_t* keys, int stride, int nw, const uint32_t* counts, uint64_t n,
+                      tor_digest* dg);
+
 /* Phase 1 only: partition contents in the reference's record layout.
  * Returns a buffer of all records grouped by partition; offsets[n_parts + 1]. */
 typedef struct tor_parts tor_parts;

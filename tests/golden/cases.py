@@ -186,6 +186,29 @@ CASES = [
 ]
 
 
+# Digest fixtures at the benchmarked sizes. The reference's TSV output for these
+# inputs (billions of lines at full size) is recorded as the order-independent
+# digest of oracle/tuna_digest.h (the one tg_job_result_digest computes), with
+# the line count and the superkmers: value. Inputs are regenerated from their
+# seed; their sha256 pins them.
+#   scale_reads_*      the small read set at its full size (138 Mbp of reads)
+#   scale_rep_fasta_*  the repetitive assembly at 1/10 (310 Mbp)
+#   scale_large_k63_*  the k=63 read set at 1/10 (300 Mbp of reads), ci/cx
+#   bench_*            the bench's full-size workloads (3.1 Gbp assembly,
+#                      3 Gbp k=63 read set), checked by bench.py
+SCALE_CASES = [
+    dict(name="scale_reads_k31_m21", k=31, m=21, n=64, source=_synth("synth_reads", scale=1.0, seed=1)),
+    dict(name="scale_rep_fasta_k31_m23", k=31, m=23, n=4096,
+         source=_synth("synth_rep_fasta", scale=0.1, seed=7)),
+    dict(name="scale_large_k63_m21", k=63, m=21, n=64, ci=2, cx=10000,
+         source=_synth("synth_large_k", scale=0.1, seed=11)),
+    dict(name="bench_rep_fasta_k31_m23", k=31, m=23, n=4096,
+         source=_synth("synth_rep_fasta", scale=1.0, seed=7)),
+    dict(name="bench_large_k63_m21", k=63, m=21, n=64, ci=2, cx=10000,
+         source=_synth("synth_large_k", scale=1.0, seed=11)),
+]
+
+
 def input_bytes(case: dict) -> bytes:
     src = case["source"]
     return GENERATORS[src["gen"]](src)

@@ -20,8 +20,14 @@ bytes are non-ACGT and produce nothing) and run with -ram 1 -tp -kt -w <dir>.
 Inputs made by tuna_gb300.synth are regenerated bit-identically from their
 seed on any host, so only their sha256 is stored.
 
-Usage: python tests/golden/make_golden.py   (needs oracle/_ref/, i.e. the
-reference sources, which only this container has)
+Scale cases (cases.SCALE_CASES, --scale): inputs of up to 3.1 Gbp whose TSV
+output is too large to keep. The reference writes its TSV to standard output,
+which oracle/tsv_digest reads: <case>.json then holds the digest (pairs, count
+sum, h1, h2), the line count and the superkmers: value.
+
+Usage: python tests/golden/make_golden.py [--scale [NAME ...]]   (needs
+oracle/_ref/, i.e. the reference sources: TUNA_REFERENCE names their root,
+else the benchmark's reference_path)
 """
 from __future__ import annotations
 
@@ -44,10 +50,20 @@ from tests.golden import cases as C  # noqa: E402
 REF = os.path.join(ROOT, "oracle", "_ref")
 
 
+def reference_root() -> str:
+    """Root of the reference sources: $TUNA_REFERENCE, else the benchmark's
+    reference_path."""
+    env = os.environ.get("TUNA_REFERENCE")
+    if env:
+        return env
+    with open(os.path.join(ROOT, "BASELINE.json")) as f:
+        return json.load(f)["reference_path"]
+
+
 def ref_bin(k: int, m: int) -> str:
     p = os.path.join(REF, f"tuna_k{k}_m{m}")
     if not os.path.exists(p):
-        subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh"), "/root/reference", f"{k}:{m}"])
+        subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh"), reference_root(), f"{k}:{m}"])
     return p
 
 
@@ -106,7 +122,68 @@ def _write_gz(path: str, data: bytes) -> None:
         f.write(data)
 
 
+def run_ref_digest(case: dict, data: bytes, tmp: str) -> dict:
+    """The reference on a large input, its TSV piped through oracle/tsv_digest."""
+    from oracle import oracle as O
+    O.build()
+    suffix = ".fq" if data[:1] == b"@" else ".fa"
+    inp = os.path.join(tmp, case["name"] + suffix)
+    with open(inp, "wb") as f:
+        f.write(data)
+    cmd = [ref_bin(case["k"], case["m"]), "-k", str(case["k"]), "-m", str(case["m"]),
+           "-n", str(case.get("n", 16)), "-t", str(os.cpu_count() or 1), "-hp"]
+    if case.get("ci", 1) != 1:
+        cmd += ["-ci", str(case["ci"])]
+    if case.get("cx") is not None:
+        cmd += ["-cx", str(case["cx"])]
+    cmd += ["-w", os.path.join(tmp, "wd_" + case["name"]), inp, "/dev/stdout"]
+    err_path = os.path.join(tmp, case["name"] + ".err")
+    with open(err_path, "w") as err:
+        ref = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=err)
+        dg = subprocess.run([O.TSV_DIGEST_BIN], stdin=ref.stdout, capture_output=True)
+        ref.stdout.close()
+        rc = ref.wait()
+    os.remove(inp)
+    with open(err_path) as f:
+        stderr = f.read()
+    if rc != 0 or dg.returncode != 0:
+        raise RuntimeError(f"{case['name']}: reference rc {rc}, digest rc {dg.returncode}: {stderr} "
+                           f"{dg.stderr.decode(errors='replace')}")
+    d = json.loads(dg.stdout)
+    d.pop("k", None)
+    stats = {}
+    for ln in stderr.splitlines():
+        if ":" in ln:
+            key, _, val = ln.partition(":")
+            if key in ("superkmers", "unique_kmers", "n_parts"):
+                stats[key] = int(val.strip())
+    return {"digest": d, "reference_stderr": stats}
+
+
+def main_scale(names) -> None:
+    with tempfile.TemporaryDirectory() as tmp:
+        for case in C.SCALE_CASES:
+            if names and case["name"] not in names:
+                continue
+            data = C.input_bytes(case)
+            r = run_ref_digest(case, data, tmp)
+            fx = {
+                "name": case["name"], "k": case["k"], "m": case["m"], "n": case.get("n", 16),
+                "ci": case.get("ci", 1), "cx": case.get("cx"),
+                "source": case["source"], "input_bytes": len(data),
+                "input_sha256": hashlib.sha256(data).hexdigest(),
+                "lines": r["digest"]["pairs"], "digest": r["digest"],
+                "reference_stderr": r["reference_stderr"],
+            }
+            with open(os.path.join(HERE, case["name"] + ".json"), "w") as f:
+                json.dump(fx, f, indent=1, sort_keys=True)
+            print(f"{case['name']}: {fx['lines']} lines {fx['reference_stderr']}", flush=True)
+
+
 def main() -> None:
+    if "--scale" in sys.argv:
+        main_scale([a for a in sys.argv[1:] if a != "--scale"])
+        return
     out_dir = HERE
     with tempfile.TemporaryDirectory() as tmp:
         for case in C.CASES:

@@ -32,7 +32,7 @@ def full_tsv(name: str):
 
 
 def case(name: str) -> dict:
-    for c in C.CASES:
+    for c in C.CASES + C.SCALE_CASES:
         if c["name"] == name:
             return c
     raise KeyError(name)

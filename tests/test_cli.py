@@ -35,6 +35,19 @@ BAD_ARGS = [
     ["-n", "99999999999", "a.fa", "out.tsv"],
     ["only_one_arg"],
     ["@/nonexistent/list.txt", "out.tsv"],
+    ["-k", "31x", "a.fa", "out.tsv"],
+    ["-k", "", "a.fa", "out.tsv"],
+    ["-ci", "99999999999999999999999", "a.fa", "out.tsv"],
+    ["-ci", "4294967296", "a.fa", "out.tsv"],
+    ["-ram", "x", "a.fa", "out.tsv"],
+    ["-ram", "17179869184", "a.fa", "out.tsv"],
+    ["-w"],
+    ["-t", "-1", "a.fa", "out.tsv"],
+    ["-m", "31", "-k", "31", "a.fa", "out.tsv"],
+    ["-k", "40", "-m", "20", "-t", "0", "-h", "a.fa", "out.tsv"],
+    ["-x", "-k", "31"],
+    ["a.fa", "-k"],
+    ["-h"],
 ]
 
 
@@ -56,6 +69,27 @@ def test_argument_errors(cli, args, tmp_path):
         ref = subprocess.run([REF_BIN, *args], capture_output=True, text=True, cwd=tmp_path)
         assert ref.returncode == r.returncode
         assert _err_line(ref.stderr) == _err_line(r.stderr)
+
+
+HEADER_ARGS = [
+    ["-k", " 25", "-m", "+13"],
+    ["-cx", "-1"],
+    ["-ci", "3", "-cx", "100", "-t", "2"],
+    ["-k", "33", "-m", "17", "-n", "0"],
+]
+
+
+@pytest.mark.parametrize("args", HEADER_ARGS, ids=[" ".join(a) for a in HEADER_ARGS])
+def test_accepted_forms_header(cli, tmp_path, args):
+    """Integer forms std::stoull accepts (blanks, signs, wrap-around of "-1")
+    are accepted alike: the header line equals the reference binary's."""
+    (tmp_path / "a.fa").write_bytes(b">s\nACGTACGTTGCAACGTAGCTAGCTAGGATCCATGCATGCA\n")
+    r = subprocess.run([cli, *args, "a.fa", "out.tsv"], capture_output=True, text=True, cwd=tmp_path)
+    head = [ln for ln in r.stderr.splitlines() if ln.startswith("tuna  k=")]
+    assert head, r.stderr
+    if os.path.exists(REF_BIN) and "-k" not in args:
+        ref = subprocess.run([REF_BIN, *args, "a.fa", "ref.tsv"], capture_output=True, text=True, cwd=tmp_path)
+        assert [ln for ln in ref.stderr.splitlines() if ln.startswith("tuna  k=")] == head
 
 
 def _header_n(stderr: str) -> str:

@@ -67,6 +67,16 @@ class _Stats(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class _Digest(ctypes.Structure):
+    _fields_ = [("pairs", ctypes.c_uint64), ("count_sum", ctypes.c_uint64), ("h1", ctypes.c_uint64),
+                ("h2", ctypes.c_uint64)]
+
+    def as_dict(self) -> Dict[str, object]:
+        """As stored in the golden fixtures: hashes as 16 hex digits."""
+        return {"pairs": int(self.pairs), "count_sum": int(self.count_sum), "h1": f"{int(self.h1):016x}",
+                "h2": f"{int(self.h2):016x}"}
+
+
 _PART_SINK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint8), ctypes.c_size_t,
                               ctypes.c_void_p)
 _SINK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint64, ctypes.c_void_p)
@@ -80,7 +90,8 @@ ABI_SYMBOLS = ["tg_ctx_create", "tg_ctx_destroy", "tg_last_error", "tg_ctx_strea
                "tg_job_result_copy", "tg_job_drain", "tg_job_write", "tg_job_export_partitions", "tg_job_end",
                "tg_count_seq", "tg_count_seq_device_noalloc", "tg_job_next_sample", "tg_job_sample_count",
                "tg_job_sample_offsets", "tg_count_batch", "tg_job_feed_fastx_device", "tg_count_fastx",
-               "tg_fastx_to_stream", "tg_read_input", "tg_count_batch_fastx", "tg_job_set_shard"]
+               "tg_fastx_to_stream", "tg_read_input", "tg_count_batch_fastx", "tg_job_set_shard",
+               "tg_job_result_digest"]
 
 
 def library(build_if_missing: bool = True) -> ctypes.CDLL:
@@ -136,6 +147,7 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
     L.tg_job_sample_count.restype = u32
     L.tg_job_sample_offsets.argtypes = [vp, vp]
     L.tg_job_set_shard.argtypes = [vp, u32, u32]
+    L.tg_job_result_digest.argtypes = [vp, u64, u64, ctypes.POINTER(_Digest)]
     L.tg_count_batch.argtypes = [vp, ctypes.POINTER(_JobOpts), u32, ctypes.POINTER(vp), ctypes.POINTER(sz), vp, vp,
                                  vp, u64, ctypes.POINTER(u64), ctypes.POINTER(_Stats)]
     for fn in ("tg_ctx_create", "tg_ctx_destroy", "tg_job_begin", "tg_job_feed_seq", "tg_job_feed_seq_device",
@@ -143,7 +155,7 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
                "tg_job_drain", "tg_job_write", "tg_job_export_partitions", "tg_job_end", "tg_count_seq",
                "tg_job_next_sample", "tg_job_sample_offsets", "tg_count_batch", "tg_job_feed_fastx_device",
                "tg_count_fastx", "tg_fastx_to_stream", "tg_read_input", "tg_count_batch_fastx",
-               "tg_job_set_shard"):
+               "tg_job_set_shard", "tg_job_result_digest"):
         getattr(L, fn).restype = i32
     _lib = L
     return L
@@ -168,6 +180,8 @@ class Result:
     k: int = 0
     samples: Optional[np.ndarray] = None  # (n,) uint32 sample of each pair (jobs of several samples)
     formatted: Optional[bytes] = None     # tg_job_drain output, when asked for
+    digest: Optional[Dict[str, object]] = None  # tg_job_result_digest of all pairs, when asked for
+    sample_digests: Optional[List[Dict[str, object]]] = None  # per sample (jobs of several samples)
 
     def __len__(self) -> int:
         return int(self.counts.shape[0])
@@ -272,7 +286,7 @@ class Context:
     def run(self, k: int, m: int, *, seq=None, dev_seq=None, dev_len: int = 0, fastx=None, files=(),
             dev_fastx=None, samples=None, n_parts: int = 16, ci: int = 1, cx: int = _U64_MAX, gpu_parts: int = 0,
             export: bool = False, want_results: bool = True, drain: Optional[int] = None,
-            shard: Optional[tuple] = None):
+            shard: Optional[tuple] = None, digest: bool = False):
         """Run one job. seq: host stream (bytes / uint8 array); dev_seq: device
         pointer (int) of dev_len bytes; fastx: FASTA/FASTQ bytes; dev_fastx: device
         pointer of dev_len FASTA/FASTQ bytes; files: paths;
@@ -280,8 +294,9 @@ class Context:
         Result then carries the sample of each pair); drain: a tg_format (0 TSV,
         1 KFF entries, 2 RAW) whose bytes tg_job_drain hands back in
         Result.formatted; shard: (s, n) counts only shard s of n of the bins
-        (tg_job_set_shard), whose pairs the n shards' results split between them.
-        Returns (Result, partitions or None)."""
+        (tg_job_set_shard), whose pairs the n shards' results split between them;
+        digest: Result.digest (and per sample, Result.sample_digests) from
+        tg_job_result_digest. Returns (Result, partitions or None)."""
         L = self._L
         o = self._opts(k, m, n_parts, ci, cx, gpu_parts)
         j = ctypes.c_void_p()
@@ -319,10 +334,21 @@ class Context:
             smp = None
             if want_results and n:
                 self.check(L.tg_job_result_copy(j, keys.ctypes.data, counts.ctypes.data, 0, n))
+            dg, sdg = None, None
+            if digest:
+                d = _Digest()
+                self.check(L.tg_job_result_digest(j, 0, n, ctypes.byref(d)))
+                dg = d.as_dict()
             if samples is not None and len(samples) > 1:
                 off = np.zeros(len(samples) + 1, dtype=np.uint64)
                 self.check(L.tg_job_sample_offsets(j, off.ctypes.data))
                 smp = np.repeat(np.arange(len(samples), dtype=np.uint32), np.diff(off).astype(np.int64))
+                if digest:
+                    sdg = []
+                    for i in range(len(samples)):
+                        d = _Digest()
+                        self.check(L.tg_job_result_digest(j, int(off[i]), int(off[i + 1] - off[i]), ctypes.byref(d)))
+                        sdg.append(d.as_dict())
             formatted = None
             if drain is not None:
                 chunks = []
@@ -344,7 +370,7 @@ class Context:
 
                 cb = _PART_SINK(sink)
                 self.check(L.tg_job_export_partitions(j, cb, None))
-            return Result(keys, counts, st.as_dict(), k, smp, formatted), parts
+            return Result(keys, counts, st.as_dict(), k, smp, formatted, dg, sdg), parts
         finally:
             L.tg_job_end(j)
 

@@ -98,6 +98,7 @@ uint32_t next_pow2_u32(uint64_t v) {
 constexpr size_t MISC_CUT_STATS = 0;    // u64[3]: k-mers, records, runs (k_cut)
 constexpr size_t MISC_BASES = 24;       // u64: ACGT bases (k_pack)
 constexpr size_t MISC_OVERFLOW = 32;    // u32: descriptor list overflow (k_cut)
+constexpr size_t MISC_DIGEST = 64;      // u64[4]: result digest (tg_job_result_digest)
 constexpr size_t MISC_NDESC = 256;      // u32[C]: descriptors per Phase-1 CTA
 constexpr size_t MISC_BYTES = MISC_NDESC + 4 * 65536;
 
@@ -1078,6 +1079,70 @@ tg_status tg_job_result_copy(tg_job* j, uint64_t* keys, uint32_t* counts, uint64
     CK(cudaStreamSynchronize(ctx->st), "d2h");
     j->st.d2h_ms += now_ms() - t0;
     return TG_OK;
+}
+
+static tg_status tg_job_result_digest_impl(tg_job* j, uint64_t first, uint64_t n, tg_digest* out) {
+    if (!j || !out) return TG_ERR_ARG;
+    tg_ctx* ctx = j->ctx;
+    if (!j->ran) return ctx->fail(TG_ERR_STATE, "result before run");
+    if (first > j->n_out || n > j->n_out - first) return ctx->fail(TG_ERR_ARG, "result range out of bounds");
+    *out = tg_digest{};
+    const int W = j->W, nw = (j->o.k + 31) / 32;
+    if (j->spilled) {  // the pairs are in host memory: the same terms on host threads
+        const unsigned nt = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(ctx->host_threads, n >> 20));
+        std::vector<tg_digest> part(nt);
+        auto body = [&](unsigned t) {
+            const uint64_t a = first + n * t / nt, b = first + n * (t + 1) / nt;
+            tg_digest d{};
+            for (uint64_t i = a; i < b; ++i) {
+                const uint64_t* w = j->host_keys.data() + i * W;
+                uint64_t ta, tb;
+                digest_terms(w[0], W > 1 ? w[1] : 0, nw, j->host_counts[i], ta, tb);
+                d.h1 += ta;
+                d.h2 += tb;
+                d.count_sum += j->host_counts[i];
+                ++d.pairs;
+            }
+            part[t] = d;
+        };
+        std::vector<std::thread> th;
+        for (unsigned t = 1; t < nt; ++t) {
+            try {
+                th.emplace_back(body, t);
+            } catch (...) {
+                body(t);
+            }
+        }
+        body(0);
+        for (auto& t : th) t.join();
+        for (const tg_digest& d : part) {
+            out->pairs += d.pairs;
+            out->count_sum += d.count_sum;
+            out->h1 += d.h1;
+            out->h2 += d.h2;
+        }
+        return TG_OK;
+    }
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const bool multi = j->sample_start.size() > 1;
+    const uint64_t* kd = (multi ? ctx->okeys2 : ctx->okeys).as<uint64_t>();
+    const uint32_t* cd = (multi ? ctx->ocnt2 : ctx->ocnt).as<uint32_t>();
+    unsigned long long* dd = reinterpret_cast<unsigned long long*>(ctx->misc.as<uint8_t>() + MISC_DIGEST);
+    int launches = 0;
+    CK(launch_digest(j->o.k, n ? kd + first * W : kd, n ? cd + first : cd, n, dd, ctx->n_sm, ctx->st, &launches),
+       "k_digest");
+    unsigned long long h[4];
+    CK(cudaMemcpyAsync(h, dd, sizeof h, cudaMemcpyDeviceToHost, ctx->st), "d2h digest");
+    CK(cudaStreamSynchronize(ctx->st), "digest");
+    out->pairs = h[0];
+    out->count_sum = h[1];
+    out->h1 = h[2];
+    out->h2 = h[3];
+    return TG_OK;
+}
+
+tg_status tg_job_result_digest(tg_job* j, uint64_t first, uint64_t n, tg_digest* out) {
+    return guarded(j ? j->ctx : nullptr, [&] { return tg_job_result_digest_impl(j, first, n, out); });
 }
 
 tg_status tg_job_sample_offsets(tg_job* j, uint64_t* offsets) {

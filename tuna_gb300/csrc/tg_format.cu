@@ -184,7 +184,52 @@ cudaError_t launch_fmt_w(int W, const uint64_t* keys, const uint32_t* counts, ui
     return cudaGetLastError();
 }
 
+// Digest of pairs [0, n): each thread sums the terms of its pairs, a warp
+// reduces them, one atomic per warp and field. out[4] = pairs, count sum, h1,
+// h2 (zeroed by the caller).
+__global__ void __launch_bounds__(256) k_digest(const uint64_t* __restrict__ keys, int W, int nw,
+                                                const uint32_t* __restrict__ counts, uint64_t n,
+                                                unsigned long long* __restrict__ out) {
+    unsigned long long h1 = 0, h2 = 0, cs = 0, np = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t w0 = keys[i * W];
+        const uint64_t w1 = W > 1 ? keys[i * W + 1] : 0;
+        const uint32_t c = counts[i];
+        uint64_t a, b;
+        digest_terms(w0, w1, nw, c, a, b);
+        h1 += a;
+        h2 += b;
+        cs += c;
+        ++np;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        h1 += __shfl_down_sync(0xffffffffu, h1, o);
+        h2 += __shfl_down_sync(0xffffffffu, h2, o);
+        cs += __shfl_down_sync(0xffffffffu, cs, o);
+        np += __shfl_down_sync(0xffffffffu, np, o);
+    }
+    if ((threadIdx.x & 31) == 0 && np) {
+        atomicAdd(&out[0], np);
+        atomicAdd(&out[1], cs);
+        atomicAdd(&out[2], h1);
+        atomicAdd(&out[3], h2);
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_digest(int k, const uint64_t* keys, const uint32_t* counts, uint64_t n, unsigned long long* out,
+                          int n_sm, cudaStream_t st, int* launches) {
+    const int W = k <= 31 ? 1 : 2;
+    const int nw = (k + 31) / 32;
+    cudaError_t e = cudaMemsetAsync(out, 0, 4 * sizeof(unsigned long long), st);
+    if (e != cudaSuccess || n == 0) return e;
+    const uint64_t blocks = std::min<uint64_t>((n + 255) / 256, (uint64_t)std::max(n_sm, 1) * 8);
+    k_digest<<<(unsigned)blocks, 256, 0, st>>>(keys, W, nw, counts, n, out);
+    ++*launches;
+    return cudaGetLastError();
+}
 
 size_t fmt_scratch_bytes(uint64_t n_pairs) {
     const uint64_t n_tiles = (n_pairs + FMT_T - 1) / FMT_T;

@@ -293,4 +293,36 @@ __device__ __forceinline__ uint64_t mix_key2(const K2& k) {
     return mix_key1(k.lo ^ mix_key1(k.hi + 0x632BE59BD9B4E019ull));
 }
 
+// ---------------------------------------------------------------- result digest
+// Order-independent digest of (k-mer, count) pairs (tg_job_result_digest): two
+// 64-bit terms per pair, summed mod 2^64. The words are the first nw =
+// ceil(k/32) words of the key in the tuna::Kmer<k> layout (w1 is ignored when
+// nw == 1); fa is MurmurHash3's 64-bit finaliser, fb SplitMix64's.
+__host__ __device__ __forceinline__ uint64_t digest_fa(uint64_t x) {
+    x ^= x >> 33;
+    x *= 0xff51afd7ed558ccdull;
+    x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ull;
+    x ^= x >> 33;
+    return x;
+}
+__host__ __device__ __forceinline__ uint64_t digest_fb(uint64_t x) {
+    x ^= x >> 30;
+    x *= 0xbf58476d1ce4e5b9ull;
+    x ^= x >> 27;
+    x *= 0x94d049bb133111ebull;
+    x ^= x >> 31;
+    return x;
+}
+__host__ __device__ __forceinline__ void digest_terms(uint64_t w0, uint64_t w1, int nw, uint32_t count,
+                                                      uint64_t& ta, uint64_t& tb) {
+    uint64_t a = digest_fa(0x243F6A8885A308D3ull ^ w0), b = digest_fb(0x13198A2E03707344ull + w0);
+    if (nw > 1) {
+        a = digest_fa(a ^ w1);
+        b = digest_fb(b + w1);
+    }
+    ta = digest_fa(a ^ ((uint64_t)count | (1ull << 40)));
+    tb = digest_fb(b + ((uint64_t)count ^ 0xA4093822299F31D0ull));
+}
+
 }  // namespace tg

@@ -43,6 +43,10 @@ size_t fmt_scratch_bytes(uint64_t n_pairs);
 uint64_t fmt_max_bytes(int fmt, int k, uint64_t n_pairs);
 cudaError_t launch_format(int fmt, int k, const uint64_t* keys, const uint32_t* counts, uint64_t n, uint8_t* out,
                           void* scratch, int n_sm, cudaStream_t st, unsigned long long* d_total, int* launches);
+// Digest of n pairs (tg_job_result_digest) into out[4] (device): pairs, count
+// sum, h1, h2.
+cudaError_t launch_digest(int k, const uint64_t* keys, const uint32_t* counts, uint64_t n, unsigned long long* out,
+                          int n_sm, cudaStream_t st, int* launches);
 size_t key_bytes(int W);
 uint32_t count_slots(int W);
 
