@@ -65,9 +65,43 @@ def parse_args():
                     help="genome sizes of the batched mix: log-uniform 10 kbp - 50 Mbp times this")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="length of the arrival trace")
     ap.add_argument("--serve-scale", type=float, default=0.05, help="request sizes: median 20 Mbp times this")
+    ap.add_argument("--no-parity-cpu", action="store_true",
+                    help="skip the oracle port's digest of the full-size results (about 30 s of host work each)")
     ap.add_argument("--cpu-shard-mbp", type=float, default=80.0,
                     help="CPU sample: one shard of this size per core (about 10 s of work on 16 cores)")
     return ap.parse_args()
+
+
+def golden(name: str):
+    """A digest fixture of tests/golden (the reference binary's output over the
+    same seeded input, recorded by tests/golden/make_golden.py --scale)."""
+    path = os.path.join(ROOT, "tests", "golden", name + ".json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        return json.load(f)
+
+
+def parity_against(device_digest, data, name: str, cpu_digest=None):
+    """Key-level parity of one result: its device digest against the
+    reference's digest for the same input bytes (when the input's sha256 equals
+    the one the reference ran on) and against the oracle port's digest computed
+    here (cpu_digest)."""
+    import hashlib
+    g = golden(name)
+    out = {"device_digest": device_digest, "reference_fixture": name}
+    if g is not None and data is not None:
+        same_input = hashlib.sha256(memoryview(data)).hexdigest() == g["input_sha256"]
+        out["input_matches_reference_run"] = same_input
+        if same_input:
+            out["reference_digest"] = g["digest"]
+            out["device_vs_reference"] = device_digest == g["digest"]
+    if cpu_digest is not None:
+        out["oracle_digest"] = cpu_digest
+        out["device_vs_oracle"] = device_digest == cpu_digest
+    checks = [out[k2] for k2 in ("device_vs_reference", "device_vs_oracle") if k2 in out]
+    out["ok"] = bool(checks) and all(checks)
+    return out
 
 
 def load_peaks():
@@ -299,7 +333,7 @@ def output_drain(ctx, dev, n_stream: int):
     return out
 
 
-def large_k(ctx, scale: float, steps: int):
+def large_k(ctx, scale: float, steps: int, parity_cpu: bool = True):
     """The k=63 read set: a seeded 100 Mbp genome with 20% repeats (1 kbp
     families, 5% divergence), 150 bp reads at 30x (3 Gbp), 0.5% substitutions;
     k=63 m=21, ci=2 cx=10000. End to end from the FASTQ bytes (tg_count_fastx),
@@ -323,7 +357,14 @@ def large_k(ctx, scale: float, steps: int):
     t_dev = (time.perf_counter() - t0) / steps
     st = res.stats
     n_out = int(st["out"])
+    dres, _ = ctx.run(k, m, dev_fastx=dev.data_ptr(), dev_len=int(fq.size), ci=ci, cx=cx, want_results=False,
+                      digest=True)
     del dev
+    cpu_dg = None
+    if parity_cpu:
+        from oracle import oracle as O
+        cpu_dg, _ = O.digest_stream(fq, k, m, 64, ci, cx, threads=os.cpu_count() or 1, fastx=True)
+    parity = parity_against(dres.digest, fq, "bench_large_k63_m21", cpu_dg)
     h_in = torch.from_numpy(fq).pin_memory()
     cap = n_out + 1024
     h_keys = torch.empty(cap * 2, dtype=torch.int64, pin_memory=True)
@@ -341,6 +382,11 @@ def large_k(ctx, scale: float, steps: int):
     for _ in range(steps):
         step()
     t_e2e = (time.perf_counter() - t0) / steps
+    from oracle import oracle as O
+    e2e_dg = O.digest_pairs(h_keys[: int(nout.value) * 2].numpy().view(np.uint64).reshape(-1, 2),
+                            h_cnt[: int(nout.value)].numpy().view(np.uint32), k, threads=os.cpu_count() or 1)
+    parity["e2e_fastx_digest_same"] = e2e_dg == dres.digest
+    parity["ok"] = parity["ok"] and parity["e2e_fastx_digest_same"]
     # the KFF file body of this result
     tot = [0]
 
@@ -369,7 +415,7 @@ def large_k(ctx, scale: float, steps: int):
             "group_load_pct": int(st["group_load_pct"]),
             "parts_ms": {f: float(st[f]) for f in ("lex_ms", "pack_ms", "phase1_ms", "phase2_keys_ms",
                                                      "phase2_count_ms")},
-            "kff_drain_s": t_kff, "kff_bytes": tot[0],
+            "kff_drain_s": t_kff, "kff_bytes": tot[0], "parity": parity,
             "api": "device: tg_job_feed_fastx_device + tg_job_run; e2e: tg_count_fastx from pinned FASTQ bytes, "
                    "pairs to pinned host buffers"}
 
@@ -432,11 +478,14 @@ def small_reads(ctx, steps: int):
     c0 = time.perf_counter()
     ref = O.count_fastx(fq, 31, 21, threads=cores)
     tc = time.perf_counter() - c0
+    got = O.digest_pairs(hk[: int(n.value)].numpy().view(np.uint64).reshape(-1, 1),
+                         hc[: int(n.value)].numpy().view(np.uint32), 31, threads=cores)
+    parity = parity_against(got, fq, "scale_reads_k31_m21", O.digest_pairs(ref.keys, ref.counts, 31))
     return {"workload": "4.6 Mbp genome, 920 k reads of 150 bp (30x, both strands), 0.5 % substitutions, "
                         "0.01 % N, FASTQ; k=31 m=21", "bases": bases, "fastq_bytes": int(fq.size),
             "e2e_gbases_s": bases / t / 1e9, "e2e_ms": t * 1e3, "distinct": int(n.value),
             "cpu_port_gbases_s": bases / tc / 1e9, "cpu_port_s": tc, "cpu_cores": cores,
-            "same_distinct": int(n.value) == len(ref),
+            "same_distinct": int(n.value) == len(ref), "parity": parity,
             "api": "tg_count_fastx from pinned FASTQ bytes; CPU: the oracle port (tor_count_fastx)"}
 
 
@@ -581,7 +630,7 @@ def main():
     def max_over_ranks(x: float) -> float:
         return rank_max(x, world, "cuda")
 
-    stream_h, bases, lens, fasta_h = workload(args.scale, want_fasta=not args.no_e2e)
+    stream_h, bases, lens, fasta_h = workload(args.scale, want_fasta=True)
     dev = torch.from_numpy(stream_h).to(f"cuda:{local}")
     ctx = T.Context(local, autotune=True)  # the first warm-up step times the group sizes
     ext = torch.cuda.ExternalStream(ctx.stream_ptr, device=f"cuda:{local}")
@@ -618,6 +667,26 @@ def main():
     clk = clocks.stop()
     ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
     value = bases * world / (ms / 1e3) / 1e9
+
+    # ---- key-level parity of the full-size result: the device digest of its
+    # pairs against the reference's (same input bytes) and the oracle port's
+    dres, _ = ctx.run(K, M, dev_seq=dev.data_ptr(), dev_len=dev.numel(), n_parts=NPARTS, want_results=False,
+                      digest=True)
+    parity_full = None
+    if rank == 0:
+        cpu_dg, cpu_s = None, None
+        if not args.no_parity_cpu:
+            from oracle import oracle as O
+            c0 = time.perf_counter()
+            cpu_dg, _ = O.digest_stream(stream_h, K, M, NPARTS, threads=os.cpu_count() or 1)
+            cpu_s = time.perf_counter() - c0
+        parity_full = parity_against(dres.digest, fasta_h, "bench_rep_fasta_k31_m23", cpu_dg)
+        parity_full["oracle_seconds"] = cpu_s
+        parity_full["oracle_threads"] = os.cpu_count() or 1
+        kmers_expected = sum(max(0, L - K + 1) for L in lens)
+        parity_full["kmers"] = int(st["kmers"])
+        parity_full["kmers_expected"] = kmers_expected
+        parity_full["ok"] = parity_full["ok"] and dres.digest["count_sum"] == int(st["kmers"]) == kmers_expected
 
     # ---- roofline of the dominant kernel (algorithmic bytes / CUDA-event time)
     peak, peak_kind = load_peaks()
@@ -696,14 +765,14 @@ def main():
                       "h2d_bytes_per_step": int(h_in.numel()), "d2h_bytes_per_step": int(nout.value) * (8 * W + 4),
                       "api": "tg_count_seq (include/tuna_gpu.h), pinned host buffers, input the parsed stream",
                       "parts_ms": parts_str}
-        # parity on the full run, size-independent: every k-mer counted once, and
-        # the instances equal what the contig lengths alone give (the contigs
-        # are ACGT only, one separator between two): sum of (length - k + 1)
-        cnt = h_cnt[: int(nout.value)].numpy().view(np.uint32)
-        sum_counts = int(cnt.astype(np.uint64).sum())
-        kmers_expected = sum(max(0, L - K + 1) for L in lens)
-        parity_full = {"sum_counts": sum_counts, "kmers": int(st["kmers"]), "kmers_expected": kmers_expected,
-                       "ok": sum_counts == int(st["kmers"]) == kmers_expected}
+        from oracle import oracle as O
+
+        def host_digest():
+            nn = int(nout.value)
+            return O.digest_pairs(h_keys[:nn].numpy().view(np.uint64).reshape(-1, 1),
+                                  h_cnt[:nn].numpy().view(np.uint32), K, threads=os.cpu_count() or 1)
+
+        e2e_stream["digest_same_as_device"] = host_digest() == dres.digest
         del h_in
         h_fa = torch.from_numpy(fasta_h).pin_memory()
         t_e2e, parts_fx = timed(L.tg_count_fastx, h_fa)
@@ -712,12 +781,11 @@ def main():
                "api": "tg_count_fastx (include/tuna_gpu.h): 60-column FASTA bytes in pinned host memory, "
                       "lexed on the device; pairs back in pinned host memory",
                "parts_ms": parts_fx, "link_h2d_gbs": link_h2d_gbs, "stream": e2e_stream}
-        cnt = h_cnt[: int(nout.value)].numpy().view(np.uint32)
-        parity_full["fastx_sum_counts"] = int(cnt.astype(np.uint64).sum())
-        parity_full["ok"] = parity_full["ok"] and parity_full["fastx_sum_counts"] == int(st["kmers"])
+        e2e["digest_same_as_device"] = host_digest() == dres.digest
+        if parity_full is not None:
+            parity_full["e2e_digests_same"] = e2e["digest_same_as_device"] and e2e_stream["digest_same_as_device"]
+            parity_full["ok"] = parity_full["ok"] and parity_full["e2e_digests_same"]
         del h_fa, h_keys, h_cnt
-    else:
-        parity_full = None
 
     small = None
     if rank == 0 and not args.no_small:
@@ -734,7 +802,7 @@ def main():
     del dev
     large = None
     if rank == 0 and not args.no_large_k:
-        large = large_k(ctx, args.large_k_scale, max(1, min(args.steps, 3)))
+        large = large_k(ctx, args.large_k_scale, max(1, min(args.steps, 3)), parity_cpu=not args.no_parity_cpu)
 
     batched = None
     if rank == 0 and not args.no_batch:

@@ -31,6 +31,7 @@
 #include <cstdint>
 #include <cstring>
 #include <filesystem>
+#include <ostream>
 #include <limits>
 #include <mutex>
 #include <stdexcept>
@@ -46,18 +47,67 @@
 namespace tuna {
 
 // Packed canonical k-mer: ceil(k/32) words, 2 bits per base (A0 C1 G2 T3),
-// word 0 holds the last 32 bases with the last base in its two low bits.
+// word 0 holds the last 32 bases with the last base in its two low bits (the
+// layout of kache_hash::Kmer<k>, include/kache-hash/Kmer.hpp:38-48 of the
+// reference). The members a counting callback uses are here with the
+// reference's names and meaning: construction from a label, the labels
+// (get_label, string_label, std::string conversion, operator<<), order and
+// equality, base access (base_at, front, back; 2-bit codes where the reference
+// returns DNA::Base, whose values are the same codes), data(), num_words(),
+// as_int(), reverse_complement(), canonical(), write_packed_2bit_msb().
+// Not provided: to_u64(seed) and Kmer_Hasher (they hash with the reference's
+// vendored XXH3), the rolling and (k+1)-mer members (roll_*, from_prefix,
+// from_suffix, from_super_kmer, lmer_at, in_forward), which only the reference's
+// own counting loop uses.
 template <uint16_t k>
 struct Kmer {
     static_assert(k >= 2 && k <= 63, "tuna (GPU): k must be in [2, 63]");
     static constexpr uint16_t NUM_INTS = (k + 31) / 32;
     uint64_t kmer_data[NUM_INTS];
 
+    Kmer() { std::memset(kmer_data, 0, sizeof kmer_data); }
+    // From the k characters of label starting at label[kmer_idx] (ACGT, any case).
+    Kmer(const char* label, std::size_t kmer_idx = 0) {
+        std::memset(kmer_data, 0, sizeof kmer_data);
+        for (uint16_t i = 0; i < k; ++i) {
+            const char c = label[kmer_idx + i];
+            const uint64_t b = (uint64_t)(((c >> 2) ^ (c >> 1)) & 3);  // A0 C1 G2 T3, case-folded
+            const uint16_t from_end = (uint16_t)(k - 1 - i);
+            kmer_data[from_end >> 5] |= b << (2 * (from_end & 31));
+        }
+    }
+    explicit Kmer(const std::string& label, std::size_t kmer_idx = 0) : Kmer(label.c_str(), kmer_idx) {}
+
+    static constexpr uint16_t num_words() { return NUM_INTS; }
+    const uint64_t* data() const { return kmer_data; }
+    uint64_t* data() { return kmer_data; }
+    // The lowest word (the whole k-mer for k <= 32).
+    uint64_t as_int() const { return kmer_data[0]; }
+
     // Base i of the k-mer (0 = first), as a 2-bit code.
     uint8_t base_at(uint16_t i) const {
         const uint16_t from_end = (uint16_t)(k - 1 - i);
         return (uint8_t)((kmer_data[from_end >> 5] >> (2 * (from_end & 31))) & 3u);
     }
+    uint8_t front() const { return base_at(0); }
+    uint8_t back() const { return base_at(k - 1); }
+
+    Kmer reverse_complement() const {
+        Kmer r;
+        for (uint16_t i = 0; i < k; ++i) {
+            const uint64_t b = 3u - base_at((uint16_t)(k - 1 - i));
+            const uint16_t from_end = (uint16_t)(k - 1 - i);
+            r.kmer_data[from_end >> 5] |= b << (2 * (from_end & 31));
+        }
+        return r;
+    }
+    // The smaller of the k-mer and its reverse complement (results of the
+    // counting path are canonical already).
+    Kmer canonical() const {
+        const Kmer r = reverse_complement();
+        return r < *this ? r : *this;
+    }
+
     template <typename T_container_>
     void get_label(T_container_& label) const {
         label.resize(k);
@@ -68,6 +118,14 @@ struct Kmer {
         get_label(s);
         return s;
     }
+    operator std::string() const { return string_label(); }
+    // ceil(k/4) bytes, first base in the two high bits of byte 0 (the KFF
+    // layout of the reference's write_packed_2bit_msb).
+    void write_packed_2bit_msb(uint8_t* dst) const {
+        std::memset(dst, 0, (k + 3) / 4);
+        for (uint16_t i = 0; i < k; ++i) dst[i >> 2] |= (uint8_t)(base_at(i) << (6 - 2 * (i & 3)));
+    }
+
     bool operator==(const Kmer& o) const { return std::memcmp(kmer_data, o.kmer_data, sizeof kmer_data) == 0; }
     bool operator!=(const Kmer& o) const { return !(*this == o); }
     // lexicographic order of the bases (A < C < G < T)
@@ -76,6 +134,8 @@ struct Kmer {
             if (kmer_data[w] != o.kmer_data[w]) return kmer_data[w] < o.kmer_data[w];
         return false;
     }
+    bool operator>(const Kmer& o) const { return o < *this; }
+    friend std::ostream& operator<<(std::ostream& out, const Kmer& km) { return out << km.string_label(); }
 };
 
 struct Options {

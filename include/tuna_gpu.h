@@ -313,9 +313,17 @@ tg_status tg_read_input(const char* path, uint32_t threads, uint8_t* out, size_t
  *   - len above TG_NOALLOC_MAX_LEN, or an input whose intermediate arrays do not
  *     fit in the scratch array, fails with TG_ERR_ARG and a message in errbuf
  *     (errbuf / errlen may be NULL / 0); k must be <= 63.
- *   - The first call on a device looks up the scratch array's device address
- *     (with that device current); make that first call before any stream
- *     capture on the device.
+ *   - The array is reserved on a device by the first call there: the CUDA
+ *     runtime loads the library's module for this entry point, which holds the
+ *     array, when the call first looks up the array's device address (with that
+ *     device current), so that call does allocate device memory. Make a first
+ *     call with len == 0 (it only reserves the array) on each device before the
+ *     caller's own allocator takes the device's memory and before any stream
+ *     capture; or set CUDA_MODULE_LOADING=EAGER to reserve it when the library
+ *     is loaded. Later calls allocate nothing.
+ *   - The call blocks the calling host thread twice while it runs: once after
+ *     Phase 1, to size Phase 2 from the record counts, and at the end.
+ *   - gpu_parts: 0 or a power of two up to 4096, as tg_job_begin.
  *   - All calls share the one scratch array, so calls whose work overlaps on the
  *     GPU (two host threads, or two streams without ordering) race; serialise
  *     them. Each call re-initialises the parts that must start at zero.

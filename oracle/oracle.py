@@ -225,9 +225,10 @@ def digest_stream(seq, k: int, m: int, n_parts: int = 16, ci: int = 1,
     return digest_dict(d), {f: int(getattr(st, f)) for f, _ in _Stats._fields_}
 
 
-def digest_pairs(keys: np.ndarray, counts: np.ndarray, k: int) -> Dict[str, object]:
+def digest_pairs(keys: np.ndarray, counts: np.ndarray, k: int, threads: int = 1) -> Dict[str, object]:
     """Digest of (keys, counts) arrays held in host memory (keys: (n, words)
-    uint64 in the Kmer<k> layout; only the first ceil(k/32) words count)."""
+    uint64 in the Kmer<k> layout; only the first ceil(k/32) words count),
+    computed on `threads` host threads (slices summed mod 2^64)."""
     keys = np.ascontiguousarray(keys, dtype=np.uint64)
     counts = np.ascontiguousarray(counts, dtype=np.uint32)
     n = int(counts.shape[0])
@@ -235,10 +236,27 @@ def digest_pairs(keys: np.ndarray, counts: np.ndarray, k: int) -> Dict[str, obje
     nw = (k + 31) // 32
     if stride < nw or keys.size < n * stride:
         raise ValueError("keys have fewer words than k needs")
-    d = _Digest()
-    lib().tor_digest_pairs(keys.ctypes.data if n else None, stride, nw, counts.ctypes.data if n else None, n,
-                           ctypes.byref(d))
-    return digest_dict(d)
+    L = lib()
+    nt = max(1, min(int(threads), n >> 20)) if n else 1
+    parts = [_Digest() for _ in range(nt)]
+
+    def one(t):
+        a, b = n * t // nt, n * (t + 1) // nt
+        if b > a:
+            L.tor_digest_pairs(keys.ctypes.data + a * stride * 8, stride, nw, counts.ctypes.data + a * 4, b - a,
+                               ctypes.byref(parts[t]))
+
+    if nt == 1:
+        one(0)
+    else:
+        from concurrent.futures import ThreadPoolExecutor
+        with ThreadPoolExecutor(nt) as ex:
+            list(ex.map(one, range(nt)))
+    tot = _Digest()
+    mask = (1 << 64) - 1
+    for f in ("pairs", "count_sum", "h1", "h2"):
+        setattr(tot, f, sum(int(getattr(p, f)) for p in parts) & mask)
+    return digest_dict(tot)
 
 
 def tsv_digest_file(path: str) -> Dict[str, object]:

@@ -82,6 +82,18 @@ int main(int argc, char** argv) {
     jo.k = 31;
     EXPECT(tg_count_seq_device_noalloc(&jo, (const uint8_t*)"x", TG_NOALLOC_MAX_LEN + 1u, NULL, NULL, 0, &n, NULL,
                                        err, sizeof err) == TG_ERR_ARG);
+    /* gpu_parts: 0 or a power of two up to 4096, checked before any device work */
+    {
+        const uint32_t bad_parts[] = {3u, 8192u, 0x80000000u, 0xFFFFFFFFu};
+        for (size_t i = 0; i < sizeof bad_parts / sizeof bad_parts[0]; ++i) {
+            jo.gpu_parts = bad_parts[i];
+            err[0] = 0;
+            EXPECT(tg_count_seq_device_noalloc(&jo, (const uint8_t*)"ACGT", 4, NULL, NULL, 0, &n, NULL, err,
+                                               sizeof err) == TG_ERR_ARG);
+            EXPECT(strstr(err, "gpu_parts") != NULL);
+        }
+        jo.gpu_parts = 0;
+    }
 
     EXPECT(tg_read_input(NULL, 1, NULL, 0, &len, err, sizeof err) == TG_ERR_ARG);
     if (argc > 1) {

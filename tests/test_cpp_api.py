@@ -68,3 +68,34 @@ def test_api_errors(api_bin, tmp_path):
     r = subprocess.run([api_bin, "31", "21", "count_to", "1", "4294967295", str(empty)], capture_output=True,
                        text=True)
     assert r.returncode == 4 and "Empty file" in r.stderr
+
+
+@pytest.mark.parametrize("k", [5, 31, 32, 63])
+def test_kmer_members(tmp_path, k):
+    """tuna::Kmer<k> members (no device): construction from a label (any case),
+    the label, reverse complement, canonical form, KFF bytes, word layout,
+    order and first/last base, against a Python restatement."""
+    import random
+    exe = str(tmp_path / "kmer_check")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "kmer_check.cpp"), "-o", exe], check=True)
+    rng = random.Random(k)
+    labels = ["".join(rng.choice("ACGTacgt") for _ in range(k)) for _ in range(200)] + ["A" * k, "T" * k]
+    r = subprocess.run([exe, str(k)], input="\n".join(labels) + "\n", capture_output=True, text=True, check=True)
+    code = {"A": 0, "C": 1, "G": 2, "T": 3}
+    prev = None
+    for lab, out in zip(labels, r.stdout.splitlines()):
+        up = lab.upper()
+        rc = "".join("TGCA"["ACGT".index(c)] for c in reversed(up))
+        v = 0
+        for c in up:
+            v = (v << 2) | code[c]
+        nw = (k + 31) // 32
+        words = ",".join(f"{(v >> (64 * w)) & ((1 << 64) - 1):016x}" for w in range(nw))
+        packed = bytearray((k + 3) // 4)
+        for i, c in enumerate(up):
+            packed[i >> 2] |= code[c] << (6 - 2 * (i & 3))
+        cmp = 0 if prev is None else (up > prev) - (up < prev)
+        want = f"{up} {rc} {min(up, rc)} {packed.hex()} {words} {cmp} {code[up[0]]}{code[up[-1]]}"
+        assert out == want, (lab, out, want)
+        prev = up

@@ -64,6 +64,44 @@ def test_noalloc_matches_regular_twice(k, m):
         assert np.array_equal(got.counts, want.counts)
 
 
+def test_noalloc_allocates_nothing_after_warmup():
+    """After one warm-up call (len == 0, which reserves the scratch array on the
+    device) a counting call leaves the device's free memory unchanged: it
+    allocates nothing. Counting the same input twice gives the same pairs."""
+    torch = pytest.importorskip("torch")
+    import tuna_gb300 as T
+    from tuna_gb300 import synth
+    L = T.library()
+    o = T._JobOpts(31, 21, 16, 1, (1 << 64) - 1, 0, 0)
+    n_out = ctypes.c_uint64(7)
+    err = ctypes.create_string_buffer(256)
+    stream = synth.fastq_sequence_stream(synth.reads_fastq(synth.genome(100_000, 5, 0.5), 2000, 150, 0.005, 0.0, 6))
+    d_in = torch.from_numpy(stream).to("cuda:0")
+    cap = int(stream.size)
+    d_keys = torch.zeros(cap, dtype=torch.int64, device="cuda:0")
+    d_cnt = torch.zeros(cap, dtype=torch.int32, device="cuda:0")
+    s = torch.cuda.current_stream()
+
+    def call(n):
+        return L.tg_count_seq_device_noalloc(ctypes.byref(o), ctypes.c_void_p(d_in.data_ptr()), n,
+                                             ctypes.c_void_p(d_keys.data_ptr()), ctypes.c_void_p(d_cnt.data_ptr()),
+                                             cap, ctypes.byref(n_out), ctypes.c_void_p(s.cuda_stream), err, 256)
+
+    assert call(0) == 0, err.value.decode()
+    assert n_out.value == 0
+    assert call(d_in.numel()) == 0, err.value.decode()  # loads the kernels this input uses
+    first = (d_keys[: n_out.value].cpu().numpy().copy(), d_cnt[: n_out.value].cpu().numpy().copy())
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    assert call(d_in.numel()) == 0, err.value.decode()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    a = np.sort(first[0])
+    b = np.sort(d_keys[: n_out.value].cpu().numpy())
+    assert np.array_equal(a, b)
+
+
 def test_noalloc_filters_and_limits():
     torch = pytest.importorskip("torch")
     import tuna_gb300 as T

@@ -10,8 +10,12 @@
 // output buffers from the caller and keeps every intermediate array (packed
 // bases, superkmer descriptors, the bin histogram and key offsets,
 // k-mer keys, group lists, fallback table) in one file-scope device array of
-// TG_NOALLOC_SCRATCH_BYTES that the CUDA runtime reserves when the library is
-// loaded on a device and that stays reserved until the process exits.
+// TG_NOALLOC_SCRATCH_BYTES that stays reserved until the process exits. The CUDA
+// runtime loads this file's module, and so reserves the array, on a device the
+// first time the array's address is looked up there, which is the first call on
+// that device (or at library load with CUDA_MODULE_LOADING=EAGER): that first
+// call does allocate. A call with len == 0 does only this, so a caller makes it
+// once per device before its own allocator takes the device's memory.
 //
 // It runs the same kernels as tg_job_run on the same parameters, so its output
 // is the same set of (k-mer, count) pairs: the counting of run_callback<k,m>
@@ -93,6 +97,11 @@ static tg_status count_noalloc(const tg_job_opts* opts, const uint8_t* d_seq, si
         set_err(errbuf, errlen, "k must be in [2, 63] and m in [1, min(k-1, 32)]");
         return o.k > 63 ? TG_ERR_UNSUPPORTED : TG_ERR_ARG;
     }
+    // the same rule as tg_job_begin: 0 (auto) or a power of two up to P1_MAX
+    if (o.gpu_parts && ((o.gpu_parts & (o.gpu_parts - 1)) || o.gpu_parts > (uint32_t)P1_MAX)) {
+        set_err(errbuf, errlen, "gpu_parts must be 0 or a power of two <= " + std::to_string(P1_MAX));
+        return TG_ERR_ARG;
+    }
     if (len > TG_NOALLOC_MAX_LEN) {
         set_err(errbuf, errlen, "input of " + std::to_string(len) + " bytes exceeds the no-allocation limit of " +
                                     std::to_string(TG_NOALLOC_MAX_LEN) + " bytes");
@@ -104,9 +113,20 @@ static tg_status count_noalloc(const tg_job_opts* opts, const uint8_t* d_seq, si
     if (e != cudaSuccess || dev < 0 || dev >= MAX_DEV) { set_err(errbuf, errlen, "no current CUDA device"); return TG_ERR_CUDA; }
     uint8_t* base = nullptr;
     e = scratch_address(dev, &base);
-    if (e != cudaSuccess) { set_err(errbuf, errlen, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e)); return TG_ERR_CUDA; }
+    if (e != cudaSuccess) {
+        set_err(errbuf, errlen, std::string("cudaGetSymbolAddress (reserving the scratch array on this device): ") +
+                                    cudaGetErrorString(e));
+        return TG_ERR_CUDA;
+    }
+    // an empty input: nothing to count. A call with len == 0 is the warm-up that
+    // reserves the scratch array on the current device (see tuna_gpu.h).
+    if (len == 0) return TG_OK;
     int n_sm = 0;
-    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess || n_sm <= 0) {
+        set_err(errbuf, errlen, std::string("multiprocessor count: ") + cudaGetErrorString(e));
+        return TG_ERR_CUDA;
+    }
 #define NA_CK(call, what)                                                                          \
     do {                                                                                           \
         const cudaError_t e_ = (call);                                                             \
