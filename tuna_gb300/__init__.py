@@ -91,7 +91,7 @@ ABI_SYMBOLS = ["tg_ctx_create", "tg_ctx_destroy", "tg_last_error", "tg_ctx_strea
                "tg_count_seq", "tg_count_seq_device_noalloc", "tg_job_next_sample", "tg_job_sample_count",
                "tg_job_sample_offsets", "tg_count_batch", "tg_job_feed_fastx_device", "tg_count_fastx",
                "tg_fastx_to_stream", "tg_read_input", "tg_count_batch_fastx", "tg_job_set_shard",
-               "tg_job_result_digest"]
+               "tg_job_result_digest", "tg_host_alloc", "tg_host_free"]
 
 
 def library(build_if_missing: bool = True) -> ctypes.CDLL:
@@ -148,6 +148,8 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
     L.tg_job_sample_offsets.argtypes = [vp, vp]
     L.tg_job_set_shard.argtypes = [vp, u32, u32]
     L.tg_job_result_digest.argtypes = [vp, u64, u64, ctypes.POINTER(_Digest)]
+    L.tg_host_alloc.argtypes = [sz, ctypes.POINTER(vp)]
+    L.tg_host_free.argtypes = [vp]
     L.tg_count_batch.argtypes = [vp, ctypes.POINTER(_JobOpts), u32, ctypes.POINTER(vp), ctypes.POINTER(sz), vp, vp,
                                  vp, u64, ctypes.POINTER(u64), ctypes.POINTER(_Stats)]
     for fn in ("tg_ctx_create", "tg_ctx_destroy", "tg_job_begin", "tg_job_feed_seq", "tg_job_feed_seq_device",
@@ -155,7 +157,7 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
                "tg_job_drain", "tg_job_write", "tg_job_export_partitions", "tg_job_end", "tg_count_seq",
                "tg_job_next_sample", "tg_job_sample_offsets", "tg_count_batch", "tg_job_feed_fastx_device",
                "tg_count_fastx", "tg_fastx_to_stream", "tg_read_input", "tg_count_batch_fastx",
-               "tg_job_set_shard", "tg_job_result_digest"):
+               "tg_job_set_shard", "tg_job_result_digest", "tg_host_alloc", "tg_host_free"):
         getattr(L, fn).restype = i32
     _lib = L
     return L
@@ -394,6 +396,44 @@ class Context:
             return st.as_dict()
         finally:
             L.tg_job_end(j)
+
+
+class HostBuffer:
+    """Page-locked host memory from tg_host_alloc (huge-page backed where the
+    host offers it): .array(dtype, count) views it as numpy; close() frees it."""
+
+    def __init__(self, nbytes: int):
+        L = library()
+        p = ctypes.c_void_p()
+        rc = L.tg_host_alloc(max(1, int(nbytes)), ctypes.byref(p))
+        if rc != 0:
+            raise GpuError(rc, f"tg_host_alloc({nbytes}) failed")
+        self.ptr, self.nbytes, self._L = int(p.value), int(nbytes), L
+
+    def array(self, dtype=np.uint8, count: Optional[int] = None) -> np.ndarray:
+        dt = np.dtype(dtype)
+        n = self.nbytes // dt.itemsize if count is None else int(count)
+        if n * dt.itemsize > self.nbytes:
+            raise ValueError("view larger than the buffer")
+        buf = (ctypes.c_uint8 * (n * dt.itemsize)).from_address(self.ptr)
+        return np.frombuffer(buf, dtype=dt, count=n)
+
+    def close(self) -> None:
+        if self.ptr:
+            self._L.tg_host_free(ctypes.c_void_p(self.ptr))
+            self.ptr = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def read_input(path: str, threads: int = 0, cap: Optional[int] = None) -> bytes:

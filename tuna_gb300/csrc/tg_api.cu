@@ -328,10 +328,8 @@ tg_status tg_ctx_destroy(tg_ctx* ctx) {
         cudaStreamDestroy(ctx->st_copy);
     }
     if (ctx->wave_out) cudaFreeHost(ctx->wave_out);
-    for (uint8_t* h : ctx->fhost)
-        if (h) cudaFreeHost(h);
-    for (uint8_t* h : ctx->stage)
-        if (h) cudaFreeHost(h);
+    for (uint8_t* h : ctx->fhost) tgh::pinned_free(h);
+    for (uint8_t* h : ctx->stage) tgh::pinned_free(h);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
     return TG_OK;
@@ -727,7 +725,11 @@ static tg_status run_cut(tg_job* j, bool exp, uint32_t p1_bits, int* launches, c
 static tg_status d2h_pageable(tg_ctx* ctx, void* dst, const void* src, size_t bytes) {
     constexpr size_t CH = 64u << 20;
     for (uint8_t*& b : ctx->stage)
-        if (!b) CK(cudaHostAlloc(reinterpret_cast<void**>(&b), CH, cudaHostAllocDefault), "alloc pinned staging");
+        if (!b) {
+            std::string why;
+            b = static_cast<uint8_t*>(tgh::pinned_alloc(CH, &why));
+            if (!b) return ctx->fail(TG_ERR_OOM, "pinned staging: " + why);
+        }
     const size_t n_ch = (bytes + CH - 1) / CH;
     const unsigned nt = std::max(1u, std::min(ctx->host_threads, 16u));
     auto issue = [&](size_t c) -> cudaError_t {
@@ -1185,11 +1187,15 @@ static tg_status tg_job_drain_impl(tg_job* j, tg_format fmt, tg_sink_fn sink, vo
     CK(ctx->ensure(ctx->fscr, fmt_scratch_bytes(B)), "alloc format scratch");
     if (ctx->fhost_cap < cap) {
         for (uint8_t*& h : ctx->fhost) {
-            if (h) cudaFreeHost(h);
+            tgh::pinned_free(h);
             h = nullptr;
         }
         ctx->fhost_cap = 0;
-        for (uint8_t*& h : ctx->fhost) CK(cudaHostAlloc(reinterpret_cast<void**>(&h), cap, cudaHostAllocDefault), "alloc pinned");
+        for (uint8_t*& h : ctx->fhost) {
+            std::string why;
+            h = static_cast<uint8_t*>(tgh::pinned_alloc(cap, &why));
+            if (!h) return ctx->fail(TG_ERR_OOM, "pinned drain buffer: " + why);
+        }
         ctx->fhost_cap = cap;
     }
     const double t0 = now_ms();

@@ -809,6 +809,360 @@ k_cut_seq(CutParams P, const HashTables* __restrict__ gT) {
     }
 }
 
+// ---------------------------------------------------------------- fixed-(k, m) cut
+// The sequential cut compiled for one (k, m) with a window of B = k - m + 1 <= 16
+// m-mers (the reference compiles one binary per (k, m) too, FIXED_K/FIXED_M).
+// Same walk and the same records as k_cut_seq; what the fixed shape buys:
+//  * the window minimum is a van Herk block minimum whose two arrays (the
+//    current block's hashes, the previous block's suffix minima) are register
+//    arrays: the loop is unrolled by whole blocks, so every index is static;
+//  * the per-position work is only the roll, the window minimum and one bit
+//    "minimizer changed" (plus the minimizer's low bits, kept in shared memory
+//    for the chain starts). Validity, chain starts, run ends, forced-split
+//    bookkeeping and record emission are done once per batch of R blocks
+//    (R * B <= 32 k-mers) with bit operations on 32-bit masks: k-mer validity is
+//    a run-AND of k validity bits, a chain starts at a valid k-mer that is the
+//    first of its run or whose minimizer changed, a run ends at the first
+//    invalid k-mer after a valid one;
+//  * records that close inside the batch get their slots from one warp scan and
+//    one shared atomic per warp and batch.
+// The ntHash roll terms CTF/CTR are interleaved (one 16-byte shared load per
+// base). Everything after the walk (the scans across threads, the forced split
+// every L k-mers, the records that cross segments, the tile carries) is the
+// code of k_cut_seq.
+template <int K, int MM>
+struct FixedShape {
+    static constexpr int W = K - MM, B = W + 1;
+    static constexpr int R = 32 / B;            // blocks per batch
+    static constexpr int SB = R * B;            // k-mers per batch (<= 32)
+    static constexpr int NBLK = (SEG + B - 1) / B;
+    static constexpr int NT = 256;
+    static_assert(B >= 2 && B <= 16, "fixed cut: window of 2..16 m-mers");
+};
+
+// Shared-memory layout of k_cut_fixed.
+struct FixedSmem {
+    size_t tables, ct, pk, vb, mlo, sum, total;
+    uint32_t npk, nvb;
+    __host__ __device__ static size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+    __host__ __device__ void layout(int nt, int k) {
+        // bases [t0 - 1, t0 + nt * SEG + 16 + k) from a 32-base boundary, with
+        // room for the validity window of the last batch (128 bits)
+        const uint32_t span = (uint32_t)nt * SEG + (uint32_t)k + 288;
+        npk = span / 16 + 2;
+        nvb = span / 32 + 2;
+        size_t o = 0;
+        tables = o; o = align16(o + sizeof(HashTables));
+        ct = o; o = align16(o + 16 * 16);
+        pk = o; o = align16(o + 4 * (size_t)npk);
+        vb = o; o = align16(o + 4 * (size_t)nvb);
+        mlo = o; o = align16(o + 4 * 32 * (size_t)nt);
+        sum = o; o = align16(o + 20 * (size_t)nt);
+        total = o;
+    }
+};
+
+// 128 bits of b starting at bit index a (bit 0 of the result = bit a).
+__device__ __forceinline__ void bits128(const uint32_t* b, uint32_t a, uint64_t& lo, uint64_t& hi) {
+    const uint32_t w = a >> 5, o = a & 31;
+    const uint32_t x0 = b[w], x1 = b[w + 1], x2 = b[w + 2], x3 = b[w + 3], x4 = b[w + 4];
+    const uint32_t y0 = o ? __funnelshift_r(x0, x1, o) : x0;
+    const uint32_t y1 = o ? __funnelshift_r(x1, x2, o) : x1;
+    const uint32_t y2 = o ? __funnelshift_r(x2, x3, o) : x2;
+    const uint32_t y3 = o ? __funnelshift_r(x3, x4, o) : x3;
+    lo = ((uint64_t)y1 << 32) | y0;
+    hi = ((uint64_t)y3 << 32) | y2;
+}
+
+__device__ __forceinline__ void shr128(uint64_t lo, uint64_t hi, int s, uint64_t& rlo, uint64_t& rhi) {
+    if (s == 0) { rlo = lo; rhi = hi; }
+    else if (s < 64) { rlo = (lo >> s) | (hi << (64 - s)); rhi = hi >> s; }
+    else { rlo = hi >> (s - 64); rhi = 0; }
+}
+
+// Bit j (j < 64) of the result: bits [j, j + K) of v are all set (K <= 64).
+template <int K>
+__device__ __forceinline__ uint64_t run_and(uint64_t lo, uint64_t hi) {
+    uint64_t acc_lo = ~0ull, acc_hi = ~0ull;
+    uint64_t cl = lo, ch = hi;  // runs of `len` set bits starting at each bit
+    int off = 0;
+#pragma unroll
+    for (int b = 0; b < 7; ++b) {
+        const int len = 1 << b;
+        if (K & len) {
+            uint64_t sl, sh;
+            shr128(cl, ch, off, sl, sh);
+            acc_lo &= sl;
+            acc_hi &= sh;
+            off += len;
+        }
+        if ((K >> (b + 1)) == 0) break;
+        uint64_t sl, sh;
+        shr128(cl, ch, len, sl, sh);
+        cl &= sl;
+        ch &= sh;
+    }
+    return acc_lo;
+}
+
+constexpr uint32_t FIXED_CUT_CTAS = 3;  // CTAs of 256 threads per SM
+
+template <int K, int MM>
+__global__ void __launch_bounds__(256, FIXED_CUT_CTAS)
+k_cut_fixed(CutParams P, const HashTables* __restrict__ gT) {
+    using S = FixedShape<K, MM>;
+    constexpr int NT = S::NT, W = S::W, B = S::B, SB = S::SB, R = S::R;
+    extern __shared__ __align__(16) uint8_t smem[];
+    FixedSmem Ly;
+    Ly.layout(NT, K);
+    HashTables& T = *reinterpret_cast<HashTables*>(smem + Ly.tables);
+    ulonglong2* s_ct = reinterpret_cast<ulonglong2*>(smem + Ly.ct);   // {CTF, CTR}[16]
+    uint32_t* s_pk = reinterpret_cast<uint32_t*>(smem + Ly.pk);
+    uint32_t* s_vb = reinterpret_cast<uint32_t*>(smem + Ly.vb);
+    uint32_t* s_mlo = reinterpret_cast<uint32_t*>(smem + Ly.mlo);     // [SB][NT] minimizer low bits
+    int64_t* s_cs = reinterpret_cast<int64_t*>(smem + Ly.sum);
+    int64_t* s_fe = s_cs + NT;
+    uint32_t* s_cm = reinterpret_cast<uint32_t*>(s_fe + NT);
+    __shared__ int s_w[NT / 32];
+    __shared__ int64_t s_carry_cs;
+    __shared__ uint32_t s_carry_m;
+    __shared__ int64_t s_open;
+    __shared__ uint32_t s_open_m;
+    __shared__ int s_open_own;
+    __shared__ uint32_t s_ndesc;
+
+    const int tid = threadIdx.x, lane = tid & 31;
+    const uint32_t c = blockIdx.x;
+    {
+        const uint64_t* src = reinterpret_cast<const uint64_t*>(gT);
+        uint64_t* dst = reinterpret_cast<uint64_t*>(&T);
+        for (int i = tid; i < (int)(sizeof(HashTables) / 8); i += NT) dst[i] = src[i];
+        if (tid < 16) s_ct[tid] = make_ulonglong2(gT->CTF[tid], gT->CTR[tid]);
+        if (tid == 0) { s_carry_cs = -1; s_carry_m = 0; s_open = -1; s_open_m = 0; s_open_own = 0; s_ndesc = 0; }
+    }
+    __syncthreads();
+
+    const int64_t cstart = (int64_t)c * (int64_t)P.chunk;
+    const int64_t cend = min(cstart + (int64_t)P.chunk, (int64_t)P.n);
+    const int64_t Lr = P.L;
+    unsigned long long loc_kmers = 0, loc_recs = 0, loc_runs = 0;
+    bool overflowed = false;
+    uint64_t* dlist = P.desc + (uint64_t)c * P.desc_cap;
+    auto owned = [&](int64_t cs) { return cs >= cstart && cs < cend; };
+    auto sample_of = [&](int64_t pos) -> uint32_t {
+        uint32_t lo = 0, hi = P.n_samples - 1;
+        while (lo < hi) {
+            const uint32_t md = (lo + hi + 1) >> 1;
+            if ((int64_t)P.sample_start[md] <= pos) lo = md; else hi = md - 1;
+        }
+        return lo;
+    };
+    int64_t seg_lo = 0;
+    uint32_t seg_s = 0;
+    auto put = [&](uint32_t idx, int64_t st, uint32_t nk, uint32_t mh) {
+        const uint32_t smp = (seg_s != ~0u && st >= seg_lo && st < seg_lo + SEG) ? seg_s : sample_of(st);
+        const uint32_t bin = P.sample_bin_base[smp] + (mh & ((1u << P.sample_bin_bits[smp]) - 1));
+        if (idx < P.desc_cap) dlist[idx] = desc_pack((uint64_t)st, nk, bin);
+        else overflowed = true;
+        atomicAdd(&P.binhist[bin], nk);
+        loc_kmers += nk;
+        loc_recs += 1;
+    };
+    auto emit_warp = [&](bool e, int64_t st, uint32_t nk, uint32_t mlo) {
+        const unsigned bal = __ballot_sync(0xffffffffu, e);
+        if (!bal) return;
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&s_ndesc, (uint32_t)__popc(bal));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (e) put(base + __popc(bal & ((1u << lane) - 1)), st, nk, mlo);
+    };
+
+    for (int64_t t0 = cstart; t0 < (int64_t)P.n; t0 += (int64_t)NT * SEG) {
+        if (t0 >= cend && !(s_open >= 0 && s_open_own)) break;
+        const uint64_t A0 = (uint64_t)(t0 + TG_PAD - 1) & ~uint64_t(31);
+        for (uint32_t i = tid; i < Ly.npk; i += NT) s_pk[i] = P.packed[(A0 >> 4) + i];
+        for (uint32_t i = tid; i < Ly.nvb; i += NT) s_vb[i] = P.valid[(A0 >> 5) + i];
+        __syncthreads();
+
+        const int64_t ps = t0 + (int64_t)tid * SEG;
+        const int64_t pb = ps - 1;
+        seg_lo = ps;
+        {
+            const uint32_t a = sample_of(ps), b = sample_of(ps + SEG - 1);
+            seg_s = a == b ? a : ~0u;
+        }
+        const uint32_t ra = (uint32_t)((uint64_t)(pb + TG_PAD) - A0);  // staged index of base pb
+        auto rel = [&](int64_t x) {
+            const int64_t d = x - pb;
+            return (int)(d < -1 ? -1 : (d > 0x7FFFFFFF ? 0x7FFFFFFF : d));
+        };
+        const int ownlo = rel(cstart), ownhi = rel(cend);
+        // ---- warm-up: m-mers 0 .. B-1 (block 0); k-mer 0 ends at m-mer W
+        uint64_t f, r;
+        nt_init(T, s_pk, ra, MM, f, r);
+        uint64_t cur[B], sfx[B];
+        uint32_t oi = ra, ii = ra + (uint32_t)MM;  // bases leaving / entering at the next roll
+        uint32_t ow = s_pk[oi >> 4] << (2 * (oi & 15));
+        uint32_t iw = s_pk[ii >> 4] << (2 * (ii & 15));
+        auto roll = [&]() -> uint64_t {
+            const uint32_t bo = ow >> 30, bi = iw >> 30;
+            ow <<= 2;
+            iw <<= 2;
+            ++oi;
+            ++ii;
+            if ((oi & 15) == 0) ow = s_pk[oi >> 4];
+            if ((ii & 15) == 0) iw = s_pk[ii >> 4];
+            const ulonglong2 t = s_ct[(bo << 2) | bi];
+            f = ((f << 1) | (f >> 63)) ^ t.x;
+            r = ((r >> 1) | (r << 63)) ^ t.y;
+            return f ^ r;
+        };
+        cur[0] = f ^ r;
+        uint64_t pmin = cur[0];
+#pragma unroll
+        for (int o = 1; o < B; ++o) {
+            cur[o] = roll();
+            pmin = min(pmin, cur[o]);
+        }
+#pragma unroll
+        for (int q = B - 1; q >= 0; --q) sfx[q] = q == B - 1 ? cur[q] : min(cur[q], sfx[q + 1]);
+        uint64_t mprev = pmin;  // minimizer of k-mer 0
+        // ---- state of the walk
+        bool open = false, last_is_cs = false;
+        int first_ev = -1, last_ev = -1, last_cs = -1, rs = 0;
+        uint32_t rm = 0, last_cs_m = 0;
+        // ---- batches of R blocks (SB k-mers): k-mers kp0 .. kp0 + SB - 1
+        for (int kp0 = 1; kp0 <= SEG; kp0 += SB) {
+            uint32_t chg = 0;
+#pragma unroll
+            for (int rb = 0; rb < R; ++rb) {
+                if (kp0 + rb * B > SEG) break;  // the segment's last blocks (uniform)
+#pragma unroll
+                for (int o = 0; o < B; ++o) {
+                    const uint64_t h = roll();
+                    cur[o] = h;
+                    pmin = o == 0 ? h : min(pmin, h);
+                    const uint64_t M = o == B - 1 ? pmin : min(sfx[o + 1], pmin);
+                    const int j = rb * B + o;
+                    chg |= (M != mprev ? 1u : 0u) << j;
+                    s_mlo[j * NT + tid] = (uint32_t)M;
+                    mprev = M;
+                }
+#pragma unroll
+                for (int q = B - 1; q >= 0; --q) sfx[q] = q == B - 1 ? cur[q] : min(cur[q], sfx[q + 1]);
+            }
+            // k-mers of this batch inside the segment: bits [0, nb)
+            const int nb = min(SB, SEG + 1 - kp0);
+            const uint32_t inseg = nb >= 32 ? ~0u : ((1u << nb) - 1);
+            // validity of k-mers kp0 - 1 .. kp0 + 31: run-AND of K validity bits
+            uint64_t vlo, vhi;
+            bits128(s_vb, ra + (uint32_t)(kp0 - 1), vlo, vhi);
+            const uint64_t vr = run_and<K>(vlo, vhi);
+            const uint32_t vk = (uint32_t)(vr >> 1) & inseg;   // bit j: k-mer kp0 + j valid
+            const uint32_t vpm = (vk << 1) | (uint32_t)(vr & 1u);  // bit j: k-mer kp0 + j - 1 valid
+            const uint32_t first = vk & ~vpm;
+            const uint32_t cs = vk & (first | chg);
+            const uint32_t cut = (cs | (~vk & vpm)) & inseg;
+            // own range of this batch: bits j with ownlo <= kp0 + j < ownhi
+            const int olo = min(max(ownlo - kp0, 0), 32), ohi = min(max(ownhi - kp0, 0), 32);
+            const uint32_t own = (uint32_t)(((olo >= 32 ? 0ull : (~0ull << olo)) & ((1ull << ohi) - 1)));
+            loc_runs += __popc(first & own);
+            // records closed inside the batch: the open record at the first cut,
+            // and every owned chain start followed by another cut
+            uint32_t nrec = 0, top = 0, cl = 0;
+            if (cut) {
+                top = 31 - __clz(cut);
+                cl = cs & own & ~(1u << top);
+                nrec = __popc(cl) + ((open && rs >= ownlo && rs < ownhi) ? 1u : 0u);
+            }
+            uint32_t incl = nrec;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= d) incl += y;
+            }
+            const uint32_t wtot = __shfl_sync(0xffffffffu, incl, 31);
+            if (wtot) {
+                uint32_t base = 0;
+                if (lane == 31) base = atomicAdd(&s_ndesc, wtot);
+                base = __shfl_sync(0xffffffffu, base, 31);
+                uint32_t idx = base + incl - nrec;
+                if (cut) {
+                    const int f0 = __ffs(cut) - 1;
+                    if (open && rs >= ownlo && rs < ownhi) put(idx++, pb + rs, (uint32_t)(kp0 + f0 - rs), rm);
+                    while (cl) {
+                        const int cb = __ffs(cl) - 1;
+                        cl &= cl - 1;
+                        const uint32_t after = cut & (uint32_t)(~0ull << (cb + 1));
+                        const int e = __ffs(after) - 1;
+                        put(idx++, pb + kp0 + cb, (uint32_t)(e - cb), s_mlo[cb * NT + tid] & 0xFFFFFu);
+                    }
+                }
+            }
+            if (cut) {
+                if (first_ev < 0) first_ev = kp0 + __ffs(cut) - 1;
+                last_ev = kp0 + (int)top;
+                last_is_cs = (cs >> top) & 1u;
+                if (cs) {
+                    const int lc = 31 - __clz(cs);
+                    last_cs = kp0 + lc;
+                    last_cs_m = s_mlo[lc * NT + tid] & 0xFFFFFu;
+                }
+                open = last_is_cs;
+                if (open) { rs = last_cs; rm = last_cs_m; }
+            }
+        }
+        // ---- as k_cut_seq: chain in force at the segment start, forced split,
+        // records crossing segments, tile carries
+        s_cs[tid] = last_is_cs ? pb + last_cs : -1;
+        s_cm[tid] = last_cs_m;
+        const int64_t first_abs = first_ev >= 0 ? pb + first_ev : -1;
+        int last_t;
+        const int prev = seq_excl_max<NT>(last_ev >= 0 ? tid : -1, s_w, last_t);
+        int64_t cs_in = s_carry_cs;
+        uint32_t m_in = s_carry_m;
+        if (prev >= 0) { cs_in = s_cs[prev]; m_in = s_cm[prev]; }
+        int64_t fc = -1;
+        if (cs_in >= 0) {
+            const int64_t d = ps - cs_in;
+            const int64_t rem = d % Lr;
+            const int64_t cand = ps + (rem ? Lr - rem : 0);
+            if (cand < ps + SEG && (first_abs < 0 || cand < first_abs)) fc = cand;
+        }
+        emit_warp(fc >= 0 && first_abs >= 0 && owned(cs_in), fc, (uint32_t)(first_abs - fc), m_in);
+        bool oo = false, oown = false;
+        int64_t os = 0;
+        uint32_t om = 0;
+        if (open) { oo = true; os = pb + rs; om = rm; oown = owned(os); }
+        else if (fc >= 0 && first_abs < 0) { oo = true; os = fc; om = m_in; oown = owned(cs_in); }
+        const int64_t fe = fc >= 0 ? fc : first_abs;
+        s_fe[tid] = fe;
+        int first_t;
+        const int nxt = seq_excl_min_rev<NT>(fe >= 0 ? tid : NT, s_w, first_t);
+        emit_warp(oo && nxt < NT && oown, os, nxt < NT ? (uint32_t)(s_fe[nxt] - os) : 0u, om);
+        if (tid == 0 && first_t < NT && s_open >= 0) {
+            if (s_open_own) put(atomicAdd(&s_ndesc, 1u), s_open, (uint32_t)(s_fe[first_t] - s_open), s_open_m);
+            s_open = -1;
+        }
+        __syncthreads();
+        if (oo && nxt == NT) { s_open = os; s_open_m = om; s_open_own = oown ? 1 : 0; }
+        if (tid == 0 && last_t >= 0) { s_carry_cs = s_cs[last_t]; s_carry_m = s_cm[last_t]; }
+        __syncthreads();
+    }
+    if (tid == 0) P.n_desc[c] = s_ndesc;
+    if (overflowed) atomicExch(P.overflow, 1u);
+    for (int o = 16; o > 0; o >>= 1) {
+        loc_kmers += __shfl_down_sync(0xffffffffu, loc_kmers, o);
+        loc_recs += __shfl_down_sync(0xffffffffu, loc_recs, o);
+        loc_runs += __shfl_down_sync(0xffffffffu, loc_runs, o);
+    }
+    if (lane == 0) {
+        if (loc_kmers) atomicAdd(&P.stats[0], loc_kmers);
+        if (loc_recs) atomicAdd(&P.stats[1], loc_recs);
+        if (loc_runs) atomicAdd(&P.stats[2], loc_runs);
+    }
+}
+
 // ---------------------------------------------------------------- offsets
 // Exclusive scan of two u32 arrays of length n into u64 outputs, one CTA per
 // SCAN_ITEMS items, then a fix-up with the scanned block sums.
@@ -862,11 +1216,23 @@ __global__ void k_scan_add(unsigned long long* __restrict__ out, uint64_t n, con
 }
 
 // ---------------------------------------------------------------- launchers
+// (k, m) pairs with a compiled cut (k_cut_fixed): the bench and served
+// workloads' shapes; other pairs take k_cut_seq.
+static bool fixed_cut(int k, int w) {
+    const int m = k - w;
+    return (k == 31 && (m == 21 || m == 23)) || (k == 21 && m == 17) || (k == 25 && m == 21);
+}
+
 size_t cut_smem_bytes(int w, int k, uint32_t p1, bool exp) {
     if (exp) {
         CutSmem L;
         L.layout(w, p1, exp);
         return L.total;
+    }
+    if (fixed_cut(k, w)) {
+        FixedSmem F;
+        F.layout(256, k);
+        return F.total;
     }
     SeqSmem L;
     L.layout(w, seq_threads(w), k);
@@ -878,6 +1244,7 @@ uint64_t cut_tile(int w, bool exp) { return exp ? (uint64_t)CUT_TILE : (uint64_t
 uint32_t cut_ctas_per_sm(int w, int k, uint32_t p1, bool exp) {
     const size_t sm = cut_smem_bytes(w, k, p1, exp) + 1024;
     const uint32_t by_smem = (uint32_t)(228u * 1024u / sm);
+    if (!exp && fixed_cut(k, w)) return std::max<uint32_t>(1, std::min<uint32_t>(FIXED_CUT_CTAS, by_smem));
     // the sequential cut: up to 768 threads per SM (three CTAs of 256; for wide
     // windows, 64-thread CTAs as many as shared memory allows: k=63 m=21 reads,
     // 3 -> 4 CTAs, 11.9 -> 9.0 ms for 0.9 Gbp)
@@ -910,8 +1277,24 @@ static cudaError_t launch_cut_seq(const CutParams& P, const HashTables* gT, size
     return cudaGetLastError();
 }
 
+template <int K, int MM>
+static cudaError_t launch_cut_fixed(const CutParams& P, const HashTables* gT, size_t sm, cudaStream_t st) {
+    const cudaError_t e = set_smem_cap(k_cut_fixed<K, MM>, sm);
+    if (e != cudaSuccess) return e;
+    k_cut_fixed<K, MM><<<P.n_cta, FixedShape<K, MM>::NT, sm, st>>>(P, gT);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_cut(const CutParams& P, const HashTables* gT, bool exp, cudaStream_t st) {
     const size_t sm = cut_smem_bytes(P.w, P.k, 1u << P.p1_bits, exp);
+    if (!exp && fixed_cut(P.k, P.w)) {
+        switch (P.k * 100 + P.m) {
+            case 3121: return launch_cut_fixed<31, 21>(P, gT, sm, st);
+            case 3123: return launch_cut_fixed<31, 23>(P, gT, sm, st);
+            case 2117: return launch_cut_fixed<21, 17>(P, gT, sm, st);
+            default: return launch_cut_fixed<25, 21>(P, gT, sm, st);
+        }
+    }
     if (exp) {
         const cudaError_t e = set_smem_cap(k_cut<true>, sm);
         if (e != cudaSuccess) return e;
