@@ -67,8 +67,10 @@ def parse_args():
     ap.add_argument("--serve-scale", type=float, default=0.05, help="request sizes: median 20 Mbp times this")
     ap.add_argument("--no-parity-cpu", action="store_true",
                     help="skip the oracle port's digest of the full-size results (about 30 s of host work each)")
-    ap.add_argument("--cpu-shard-mbp", type=float, default=80.0,
-                    help="CPU sample: one shard of this size per core (about 10 s of work on 16 cores)")
+    ap.add_argument("--cpu-mbp", type=float, default=1200.0,
+                    help="CPU baseline sample: the first this many Mbp of the assembly (about 10 s on 16 cores)")
+    ap.add_argument("--ref-mbp", type=float, default=400.0,
+                    help="reference arm, per step: the first this many Mbp of the assembly (a few seconds)")
     return ap.parse_args()
 
 
@@ -187,27 +189,31 @@ def workload(scale: float, want_fasta: bool = True):
     return stream, int(g.size), [int(x) for x in lens], fa
 
 
-def cpu_sample(scale_shard_mbp: float, threads: int):
-    """`threads` shards of the workload (first bases of the assembly, cut
-    into shard-sized runs): the reference's best CPU mode for one large file is
-    the same data pre-split into one plain file per core."""
-    import numpy as np
-    from tuna_gb300 import synth
-    shard = int(scale_shard_mbp * 1e6)
-    total = shard * threads
-    g = synth.genome(total, 7, 0.41, fam_a=(200, 300, 0.25), fam_b=(40, 6000, 0.20),
-                     div=(0.10, 0.20), micro=0.03, micro_len=(20, 200))
+def main_config(bases: int, n_stream: int, world: int) -> dict:
+    """The workload as both arms name it (identical in the GB300 and the
+    reference lines; arm-specific details go in their own keys)."""
+    return {"workload": f"{bases / 1e9:.2f} Gbp repetitive assembly, 24 contigs, k=31 m=23 n=4096",
+            "k": K, "m": M, "n_parts": NPARTS, "bases": bases, "stream_bytes": n_stream,
+            "l2": "inputs larger than L2 (3.1 GB), no flush", "parallelism": f"replicas x{world}"}
+
+
+def cpu_sample(stream: np.ndarray, mbp: float, threads: int):
+    """The first `mbp` Mbp of the assembly's sequence stream, cut into `threads`
+    shards (one separator byte between two): the reference's best CPU mode for
+    one large file is the same data pre-split into one plain file per core
+    (phase 1 in parallel over files, src/partition_hash.hpp:271-279)."""
+    seq = stream[stream != 10]
+    total = min(int(mbp * 1e6), int(seq.size))
+    shard = max(1, total // threads)
     cuts = np.arange(shard, total, shard)
-    s = np.insert(g, cuts, np.uint8(10))
+    s = np.insert(seq[:total], cuts, np.uint8(10))
     return np.append(s, np.uint8(10)), total
 
 
-def time_cpu(threads: int, shard_mbp: float, steps: int = 1, warmup: int = 0, sample=None):
+def time_cpu(threads: int, sample, steps: int = 1, warmup: int = 0):
     """Median seconds of `steps` runs of the oracle port over the CPU sample
     (after `warmup` untimed runs; at least a short warm-up of the library)."""
     from oracle import oracle as O
-    if sample is None:
-        sample = cpu_sample(shard_mbp, threads)
     s, bases = sample
     O.count_stream_unsorted(s[: min(s.size, 2_000_000)], K, M, NPARTS, threads=threads)  # load, warm
     for _ in range(warmup):
@@ -219,15 +225,45 @@ def time_cpu(threads: int, shard_mbp: float, steps: int = 1, warmup: int = 0, sa
         ts.append(time.perf_counter() - t0)
     t = statistics.median(ts)
     return {"value": bases / t / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{threads} shards x {shard_mbp:g} Mbp of the workload ({bases / 1e6:.0f} Mbp), "
-                      f"k={K} m={M} n={NPARTS}; phase 1 parallel over shards, phase 2 over partitions",
+            "sample": f"the first {bases / 1e6:.0f} Mbp of the same assembly ({bases / 3.1e9:.3f} of it) cut into "
+                      f"{threads} shards, k={K} m={M} n={NPARTS}; phase 1 parallel over shards, phase 2 over "
+                      f"partitions (the reference's best mode for one large file)",
             "seconds": t, "distinct": len(r)}
 
 
 # ------------------------------------------------------------------ batched and served
+_HOST_BUFS = []
+
+
+def host_array(n: int, dtype=np.uint8, like=None) -> np.ndarray:
+    """n elements of page-locked host memory from the library's allocator
+    (tg_host_alloc); with `like`, a copy of it. The buffer lives until
+    release() or the end of the run."""
+    import tuna_gb300 as T
+    dt = np.dtype(dtype)
+    if like is not None:
+        like = np.ascontiguousarray(like).view(dt).ravel()
+        n = like.size
+    hb = T.HostBuffer(max(1, n) * dt.itemsize)
+    a = hb.array(dt, n)
+    _HOST_BUFS.append((hb, a))
+    if like is not None:
+        a[:] = like
+    return a
+
+
+def release(*arrays) -> None:
+    """Free the host memory of arrays made by host_array (not used afterwards)."""
+    for a in arrays:
+        for i, (hb, b) in enumerate(_HOST_BUFS):
+            if b is a:
+                hb.close()
+                del _HOST_BUFS[i]
+                break
+
+
 def _pinned_copy(a):
-    import torch
-    return torch.from_numpy(np.array(a, dtype=np.uint8)).pin_memory().numpy()
+    return host_array(0, np.uint8, like=np.asarray(a, dtype=np.uint8))
 
 
 def batched_vs_plain(ctx, n_samples: int, scale: float):
@@ -365,16 +401,16 @@ def large_k(ctx, scale: float, steps: int, parity_cpu: bool = True):
         from oracle import oracle as O
         cpu_dg, _ = O.digest_stream(fq, k, m, 64, ci, cx, threads=os.cpu_count() or 1, fastx=True)
     parity = parity_against(dres.digest, fq, "bench_large_k63_m21", cpu_dg)
-    h_in = torch.from_numpy(fq).pin_memory()
+    h_in = host_array(0, np.uint8, like=fq)
     cap = n_out + 1024
-    h_keys = torch.empty(cap * 2, dtype=torch.int64, pin_memory=True)
-    h_cnt = torch.empty(cap, dtype=torch.int32, pin_memory=True)
+    h_keys = host_array(cap * 2, np.uint64)
+    h_cnt = host_array(cap, np.uint32)
     nout = ctypes.c_uint64()
     sts = T._Stats()
 
     def step():
-        ctx.check(L.tg_count_fastx(ctx.h, ctypes.byref(o), ctypes.c_void_p(h_in.data_ptr()), h_in.numel(),
-                                   ctypes.c_void_p(h_keys.data_ptr()), ctypes.c_void_p(h_cnt.data_ptr()), cap,
+        ctx.check(L.tg_count_fastx(ctx.h, ctypes.byref(o), ctypes.c_void_p(h_in.ctypes.data), h_in.size,
+                                   ctypes.c_void_p(h_keys.ctypes.data), ctypes.c_void_p(h_cnt.ctypes.data), cap,
                                    ctypes.byref(nout), ctypes.byref(sts)))
 
     step()
@@ -383,8 +419,8 @@ def large_k(ctx, scale: float, steps: int, parity_cpu: bool = True):
         step()
     t_e2e = (time.perf_counter() - t0) / steps
     from oracle import oracle as O
-    e2e_dg = O.digest_pairs(h_keys[: int(nout.value) * 2].numpy().view(np.uint64).reshape(-1, 2),
-                            h_cnt[: int(nout.value)].numpy().view(np.uint32), k, threads=os.cpu_count() or 1)
+    e2e_dg = O.digest_pairs(h_keys[: int(nout.value) * 2].reshape(-1, 2), h_cnt[: int(nout.value)], k,
+                            threads=os.cpu_count() or 1)
     parity["e2e_fastx_digest_same"] = e2e_dg == dres.digest
     parity["ok"] = parity["ok"] and parity["e2e_fastx_digest_same"]
     # the KFF file body of this result
@@ -398,14 +434,14 @@ def large_k(ctx, scale: float, steps: int, parity_cpu: bool = True):
     j = ctypes.c_void_p()
     ctx.check(L.tg_job_begin(ctx.h, ctypes.byref(o), ctypes.byref(j)))
     try:
-        ctx.check(L.tg_job_feed_fastx(j, ctypes.c_void_p(h_in.data_ptr()), h_in.numel()))
+        ctx.check(L.tg_job_feed_fastx(j, ctypes.c_void_p(h_in.ctypes.data), h_in.size))
         ctx.check(L.tg_job_run(j))
         t0 = time.perf_counter()
         ctx.check(L.tg_job_drain(j, 1, cb, None))
         t_kff = time.perf_counter() - t0
     finally:
         L.tg_job_end(j)
-    del h_in, h_keys, h_cnt
+    release(h_in, h_keys, h_cnt)
     return {"workload": f"{meta['genome'] / 1e6:.0f} Mbp genome, 20% repeats (1 kbp families, 5% divergence), "
                         f"{meta['reads']} reads of 150 bp (30x), 0.5% substitutions; k=63 m=21 ci=2 cx=10000",
             "bases": bases, "fastq_bytes": int(fq.size),
@@ -454,17 +490,17 @@ def small_reads(ctx, steps: int):
     fq, meta = synth.reads_workload(scale=1.0, seed=1)
     bases = int(meta["reads"]) * 150
     L = T.library()
-    h = torch.from_numpy(fq).pin_memory()
+    h = host_array(0, np.uint8, like=fq)
     cap = bases
-    hk = torch.empty(cap, dtype=torch.int64, pin_memory=True)
-    hc = torch.empty(cap, dtype=torch.int32, pin_memory=True)
+    hk = host_array(cap, np.uint64)
+    hc = host_array(cap, np.uint32)
     o = T._JobOpts(31, 21, 16, 1, (1 << 64) - 1, 0, 0)
     n = ctypes.c_uint64()
     st = T._Stats()
 
     def step():
-        ctx.check(L.tg_count_fastx(ctx.h, ctypes.byref(o), ctypes.c_void_p(h.data_ptr()), h.numel(),
-                                   ctypes.c_void_p(hk.data_ptr()), ctypes.c_void_p(hc.data_ptr()), cap,
+        ctx.check(L.tg_count_fastx(ctx.h, ctypes.byref(o), ctypes.c_void_p(h.ctypes.data), h.size,
+                                   ctypes.c_void_p(hk.ctypes.data), ctypes.c_void_p(hc.ctypes.data), cap,
                                    ctypes.byref(n), ctypes.byref(st)))
 
     for _ in range(3):
@@ -478,9 +514,9 @@ def small_reads(ctx, steps: int):
     c0 = time.perf_counter()
     ref = O.count_fastx(fq, 31, 21, threads=cores)
     tc = time.perf_counter() - c0
-    got = O.digest_pairs(hk[: int(n.value)].numpy().view(np.uint64).reshape(-1, 1),
-                         hc[: int(n.value)].numpy().view(np.uint32), 31, threads=cores)
+    got = O.digest_pairs(hk[: int(n.value)].reshape(-1, 1), hc[: int(n.value)], 31, threads=cores)
     parity = parity_against(got, fq, "scale_reads_k31_m21", O.digest_pairs(ref.keys, ref.counts, 31))
+    release(h, hk, hc)
     return {"workload": "4.6 Mbp genome, 920 k reads of 150 bp (30x, both strands), 0.5 % substitutions, "
                         "0.01 % N, FASTQ; k=31 m=21", "bases": bases, "fastq_bytes": int(fq.size),
             "e2e_gbases_s": bases / t / 1e9, "e2e_ms": t * 1e3, "distinct": int(n.value),
@@ -587,23 +623,31 @@ def rank_max(x: float, world: int, device: str) -> float:
 
 
 def run_reference(args, rank: int):
+    """The reference arm: the CPU path (the oracle port of the reference's
+    pipeline; the reference's own sources are not on this host) on all host
+    cores, on the same assembly bytes as the GB300 arm. Each step counts the
+    first --ref-mbp Mbp of it, pre-split into one shard per core, so that the
+    whole --steps/--warmup run stays within a few minutes; value = those bases
+    / the median step time."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    sample = cpu_sample(args.cpu_shard_mbp, threads)
-    base = time_cpu(threads, args.cpu_shard_mbp, steps=args.steps, warmup=args.warmup, sample=sample)
+    stream_h, bases, _, _ = workload(args.scale, want_fasta=False)
+    n_stream = int(stream_h.size)
+    sample = cpu_sample(stream_h, args.ref_mbp, threads)
+    del stream_h
+    base = time_cpu(threads, sample, steps=args.steps, warmup=args.warmup)
     v = base["value"]
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic",
             "ms_per_step": base["seconds"] * 1e3,  # median over the timed steps
-            "config": {"workload": "3.1 Gbp repetitive assembly (24 contigs), k=31 m=23 n=4096",
-                       "k": K, "m": M, "n_parts": NPARTS, "sample": base["sample"]},
+            "config": main_config(bases, n_stream, args.gpus),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": base["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "the reference CPU path, restated in C (oracle/tuna_oracle.c, pinned to the reference's "
-                    "outputs); the reference sources are not on the GPU host"}
+                    "outputs by digest at the full 3.1 Gbp size); the reference sources are not on the GPU host"}
     print(json.dumps(line), flush=True)
 
 
@@ -720,9 +764,10 @@ def main():
     if not args.no_e2e:
         n_out_cap = int(st["out"]) + 1024
         W = 1
-        h_in = torch.from_numpy(stream_h).pin_memory()
-        h_keys = torch.empty(n_out_cap * W, dtype=torch.int64, pin_memory=True)
-        h_cnt = torch.empty(n_out_cap, dtype=torch.int32, pin_memory=True)
+        # inputs and outputs in the library's page-locked host memory (tg_host_alloc)
+        h_in = host_array(0, np.uint8, like=stream_h)
+        h_keys = host_array(n_out_cap * W, np.uint64)
+        h_cnt = host_array(n_out_cap, np.uint32)
         L = T.library()
         import ctypes
         o = T._JobOpts(K, M, NPARTS, 1, (1 << 64) - 1, 0, 0)
@@ -730,8 +775,8 @@ def main():
         sts = T._Stats()
 
         def e2e_step(fn, h):
-            rc = fn(ctx.h, ctypes.byref(o), ctypes.c_void_p(h.data_ptr()), h.numel(),
-                    ctypes.c_void_p(h_keys.data_ptr()), ctypes.c_void_p(h_cnt.data_ptr()),
+            rc = fn(ctx.h, ctypes.byref(o), ctypes.c_void_p(h.ctypes.data), h.size,
+                    ctypes.c_void_p(h_keys.ctypes.data), ctypes.c_void_p(h_cnt.ctypes.data),
                     n_out_cap, ctypes.byref(nout), ctypes.byref(sts))
             ctx.check(rc)
 
@@ -750,42 +795,45 @@ def main():
             torch.cuda.synchronize()
             return max_over_ranks((time.perf_counter() - t0) / args.steps), parts
 
-        # the host link alone: one event-timed H2D of the same pinned buffer
-        d_tmp = torch.empty(h_in.numel(), dtype=torch.uint8, device=f"cuda:{local}")
-        c0 = torch.cuda.Event(enable_timing=True)
-        c1 = torch.cuda.Event(enable_timing=True)
-        c0.record()
-        d_tmp.copy_(h_in, non_blocking=True)
-        c1.record()
-        c1.synchronize()
-        link_h2d_gbs = h_in.numel() / (c0.elapsed_time(c1) / 1e3) / 1e9
+        # the host link alone: event-timed H2D of the same buffer (first and third copy)
+        d_tmp = torch.empty(h_in.size, dtype=torch.uint8, device=f"cuda:{local}")
+        link = []
+        for _ in range(3):
+            c0 = torch.cuda.Event(enable_timing=True)
+            c1 = torch.cuda.Event(enable_timing=True)
+            c0.record()
+            d_tmp.copy_(torch.from_numpy(h_in), non_blocking=True)
+            c1.record()
+            c1.synchronize()
+            link.append(h_in.size / (c0.elapsed_time(c1) / 1e3) / 1e9)
+        link_h2d_gbs = link[-1]
         del d_tmp
         t_str, parts_str = timed(L.tg_count_seq, h_in)
         e2e_stream = {"value": bases * world / t_str / 1e9, "unit": UNIT, "ms_per_step": t_str * 1e3,
-                      "h2d_bytes_per_step": int(h_in.numel()), "d2h_bytes_per_step": int(nout.value) * (8 * W + 4),
+                      "h2d_bytes_per_step": int(h_in.size), "d2h_bytes_per_step": int(nout.value) * (8 * W + 4),
                       "api": "tg_count_seq (include/tuna_gpu.h), pinned host buffers, input the parsed stream",
                       "parts_ms": parts_str}
         from oracle import oracle as O
 
         def host_digest():
             nn = int(nout.value)
-            return O.digest_pairs(h_keys[:nn].numpy().view(np.uint64).reshape(-1, 1),
-                                  h_cnt[:nn].numpy().view(np.uint32), K, threads=os.cpu_count() or 1)
+            return O.digest_pairs(h_keys[:nn].reshape(-1, 1), h_cnt[:nn], K, threads=os.cpu_count() or 1)
 
         e2e_stream["digest_same_as_device"] = host_digest() == dres.digest
-        del h_in
-        h_fa = torch.from_numpy(fasta_h).pin_memory()
+        release(h_in)
+        h_fa = host_array(0, np.uint8, like=fasta_h)
         t_e2e, parts_fx = timed(L.tg_count_fastx, h_fa)
         e2e = {"value": bases * world / t_e2e / 1e9, "unit": UNIT, "ms_per_step": t_e2e * 1e3,
-               "h2d_bytes_per_step": int(h_fa.numel()), "d2h_bytes_per_step": int(nout.value) * (8 * W + 4),
-               "api": "tg_count_fastx (include/tuna_gpu.h): 60-column FASTA bytes in pinned host memory, "
-                      "lexed on the device; pairs back in pinned host memory",
-               "parts_ms": parts_fx, "link_h2d_gbs": link_h2d_gbs, "stream": e2e_stream}
+               "h2d_bytes_per_step": int(h_fa.size), "d2h_bytes_per_step": int(nout.value) * (8 * W + 4),
+               "api": "tg_count_fastx (include/tuna_gpu.h): 60-column FASTA bytes in page-locked host memory "
+                      "(tg_host_alloc), lexed on the device; pairs back in page-locked host memory",
+               "parts_ms": parts_fx, "link_h2d_gbs": link_h2d_gbs, "link_h2d_gbs_first_copy": link[0],
+               "stream": e2e_stream}
         e2e["digest_same_as_device"] = host_digest() == dres.digest
         if parity_full is not None:
             parity_full["e2e_digests_same"] = e2e["digest_same_as_device"] and e2e_stream["digest_same_as_device"]
             parity_full["ok"] = parity_full["ok"] and parity_full["e2e_digests_same"]
-        del h_fa, h_keys, h_cnt
+        release(h_fa, h_keys, h_cnt)
 
     small = None
     if rank == 0 and not args.no_small:
@@ -813,7 +861,7 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        cpu = time_cpu(os.cpu_count() or 1, args.cpu_shard_mbp)
+        cpu = time_cpu(os.cpu_count() or 1, cpu_sample(stream_h, args.cpu_mbp, os.cpu_count() or 1))
 
     if rank == 0:
         line = {
@@ -822,12 +870,10 @@ def main():
             "vs_baseline": None, "dtype": "u64",
             "data": "synthetic: seeded 3.1 Gbp repetitive assembly (tuna_gb300/synth.py), "
                     "stands in for the reference's genome assemblies",
-            "config": {"workload": f"{bases / 1e9:.2f} Gbp repetitive assembly, 24 contigs, k=31 m=23 n=4096",
-                       "k": K, "m": M, "n_parts": NPARTS, "bases": bases, "stream_bytes": n_stream,
-                       "gpu_parts": int(st["gpu_parts"]), "l2": "inputs larger than L2 (3.1 GB), no flush",
-                       "group_load_pct": int(st["group_load_pct"]),
-                       "autotune": "TG_CTX_AUTOTUNE: group size timed on the first warm-up step (35/50/65 % of the table)",
-                       "parallelism": f"replicas x{world}"},
+            "config": main_config(bases, n_stream, world),
+            "gpu_config": {"gpu_parts": int(st["gpu_parts"]), "group_load_pct": int(st["group_load_pct"]),
+                           "autotune": "TG_CTX_AUTOTUNE: group size timed on the first warm-up step "
+                                       "(35/50/65 % of the table)"},
             "stats": {"kmers": int(st["kmers"]), "superkmers": int(st["superkmers"]),
                       "distinct": int(st["distinct"]), "fallback_groups": int(st["fallback_groups"]),
                       "distinct_kmers_per_s": int(st["distinct"]) / (ms / 1e3),

@@ -297,13 +297,12 @@ tg_status tg_read_input(const char* path, uint32_t threads, uint8_t* out, size_t
 /* ---- host memory for the host link --------------------------------------
  * No counterpart in the reference (its input never leaves host memory).
  * Page-locked host memory for the inputs and outputs of the one-call entry
- * points (tg_count_seq, tg_count_fastx, tg_count_batch*): mapped with 2 MiB
- * transparent huge pages where the host kernel offers them, faulted in on
- * several threads and registered with the CUDA runtime for every device. On
- * the GB300's Grace host, copies from such buffers ran at the link's rate
- * (~200 GB/s) where 4 KiB-page pinned buffers were measured as low as 9-25
- * GB/s. The size is rounded up to 2 MiB. tg_host_free takes only pointers from
- * tg_host_alloc (TG_ERR_ARG otherwise). */
+ * points (tg_count_seq, tg_count_fastx, tg_count_batch*), from the CUDA
+ * driver (portable to every device), so that a caller of this C ABI needs no
+ * CUDA runtime of its own. Copies from and to it run at the host link's rate
+ * (on a GB300: ~211 GB/s H2D, ~193 GB/s D2H); pageable memory goes through
+ * staging copies. tg_host_free takes only pointers from tg_host_alloc
+ * (TG_ERR_ARG otherwise). */
 tg_status tg_host_alloc(size_t bytes, void** out);
 tg_status tg_host_free(void* p);
 

@@ -14,7 +14,7 @@ def _run(extra_env=None):
     env = dict(os.environ)
     env.update(extra_env or {})
     return subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
-                           "--steps", "2", "--warmup", "3", "--cpu-shard-mbp", "1"],
+                           "--steps", "2", "--warmup", "3", "--scale", "0.01", "--ref-mbp", "4"],
                           capture_output=True, text=True, env=env, cwd=ROOT, timeout=600)
 
 
@@ -32,6 +32,12 @@ def test_reference_arm_line():
     assert d["steps"] == 2 and d["warmup"] == 3 and d["value"] > 0 and d["vs_baseline"] is None
     assert d["unit"] == "Gbases/s" and d["higher_is_better"] is True
     assert "workload" in d["config"]
+    # the same config object as the GB300 arm's line (bench.main_config), so the
+    # two arms are on one workload
+    sys.path.insert(0, ROOT)
+    import bench
+    assert d["config"] == bench.main_config(d["config"]["bases"], d["config"]["stream_bytes"], 1)
+    assert d["config"]["bases"] == 31_000_000 and "same assembly" in d["cpu_baseline"]["sample"]
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"] and cb["value"] == d["value"]
     e = d["e2e"]

@@ -399,8 +399,8 @@ class Context:
 
 
 class HostBuffer:
-    """Page-locked host memory from tg_host_alloc (huge-page backed where the
-    host offers it): .array(dtype, count) views it as numpy; close() frees it."""
+    """Page-locked host memory from tg_host_alloc: .array(dtype, count) views it
+    as numpy; close() frees it."""
 
     def __init__(self, nbytes: int):
         L = library()

@@ -46,9 +46,8 @@ bool fastx_to_stream(const uint8_t* data, size_t len, std::vector<uint8_t>& out)
 // error message, or "" on success.
 std::string read_input_file(const std::string& path, Bytes& out, unsigned threads = 1);
 
-// Page-locked host memory backed by huge pages where the host offers them,
-// registered with the CUDA runtime (tg_host_alloc); null with a message in
-// *err on failure. pinned_free takes only pointers from pinned_alloc (false
+// Page-locked host memory from the CUDA driver (tg_host_alloc); null with a
+// message in *err on failure. pinned_free takes only pointers from pinned_alloc (false
 // otherwise).
 void* pinned_alloc(size_t bytes, std::string* err);
 bool pinned_free(void* p);

@@ -826,10 +826,15 @@ k_cut_seq(CutParams P, const HashTables* __restrict__ gT) {
 //    invalid k-mer after a valid one;
 //  * records that close inside the batch get their slots from one warp scan and
 //    one shared atomic per warp and batch.
-// The ntHash roll terms CTF/CTR are interleaved (one 16-byte shared load per
-// base). Everything after the walk (the scans across threads, the forced split
-// every L k-mers, the records that cross segments, the tile carries) is the
-// code of k_cut_seq.
+// The bases that leave and enter the m-mer during a batch come from two 64-bit
+// windows of the staged packed words, read once per batch and shifted by one
+// base per roll. The ntHash roll terms CTF/CTR are interleaved (one 16-byte
+// shared load per base). Measured on 0.93 Gbp of the assembly (k=31 m=23, one
+// GB300): 5.51 ms with per-roll base words, 5.18 with the per-batch windows,
+// 5.11 with the segment's first bin cached as well (k_cut_seq: 7.1);
+// 128-thread CTAs gave 5.59, 192 positions per thread 6.13. Everything after
+// the walk (the scans across threads, the forced split every L k-mers, the
+// records that cross segments, the tile carries) is the code of k_cut_seq.
 template <int K, int MM>
 struct FixedShape {
     static constexpr int W = K - MM, B = W + 1;
@@ -957,11 +962,18 @@ k_cut_fixed(CutParams P, const HashTables* __restrict__ gT) {
         }
         return lo;
     };
+    // the segment's sample when the segment lies in one (its first bin and bin
+    // mask cached), else a lookup per record
     int64_t seg_lo = 0;
-    uint32_t seg_s = 0;
+    uint32_t seg_s = 0, seg_base = 0, seg_mask = 0;
     auto put = [&](uint32_t idx, int64_t st, uint32_t nk, uint32_t mh) {
-        const uint32_t smp = (seg_s != ~0u && st >= seg_lo && st < seg_lo + SEG) ? seg_s : sample_of(st);
-        const uint32_t bin = P.sample_bin_base[smp] + (mh & ((1u << P.sample_bin_bits[smp]) - 1));
+        uint32_t bin;
+        if (seg_s != ~0u && st >= seg_lo && st < seg_lo + SEG) {
+            bin = seg_base + (mh & seg_mask);
+        } else {
+            const uint32_t smp = sample_of(st);
+            bin = P.sample_bin_base[smp] + (mh & ((1u << P.sample_bin_bits[smp]) - 1));
+        }
         if (idx < P.desc_cap) dlist[idx] = desc_pack((uint64_t)st, nk, bin);
         else overflowed = true;
         atomicAdd(&P.binhist[bin], nk);
@@ -990,6 +1002,8 @@ k_cut_fixed(CutParams P, const HashTables* __restrict__ gT) {
         {
             const uint32_t a = sample_of(ps), b = sample_of(ps + SEG - 1);
             seg_s = a == b ? a : ~0u;
+            seg_base = P.sample_bin_base[a];
+            seg_mask = (1u << P.sample_bin_bits[a]) - 1;
         }
         const uint32_t ra = (uint32_t)((uint64_t)(pb + TG_PAD) - A0);  // staged index of base pb
         auto rel = [&](int64_t x) {
@@ -1001,17 +1015,14 @@ k_cut_fixed(CutParams P, const HashTables* __restrict__ gT) {
         uint64_t f, r;
         nt_init(T, s_pk, ra, MM, f, r);
         uint64_t cur[B], sfx[B];
-        uint32_t oi = ra, ii = ra + (uint32_t)MM;  // bases leaving / entering at the next roll
-        uint32_t ow = s_pk[oi >> 4] << (2 * (oi & 15));
-        uint32_t iw = s_pk[ii >> 4] << (2 * (ii & 15));
+        // the bases leaving and entering the m-mer, 32 at a time: 64-bit windows
+        // of the staged packed words (the roll into m-mer i takes out base
+        // pb + i - 1 and in base pb + i - 1 + MM), shifted by one base per roll
+        uint64_t wob = window64(s_pk, ra), wib = window64(s_pk, ra + MM);
         auto roll = [&]() -> uint64_t {
-            const uint32_t bo = ow >> 30, bi = iw >> 30;
-            ow <<= 2;
-            iw <<= 2;
-            ++oi;
-            ++ii;
-            if ((oi & 15) == 0) ow = s_pk[oi >> 4];
-            if ((ii & 15) == 0) iw = s_pk[ii >> 4];
+            const uint32_t bo = (uint32_t)(wob >> 62), bi = (uint32_t)(wib >> 62);
+            wob <<= 2;
+            wib <<= 2;
             const ulonglong2 t = s_ct[(bo << 2) | bi];
             f = ((f << 1) | (f >> 63)) ^ t.x;
             r = ((r >> 1) | (r << 63)) ^ t.y;
@@ -1034,6 +1045,11 @@ k_cut_fixed(CutParams P, const HashTables* __restrict__ gT) {
         // ---- batches of R blocks (SB k-mers): k-mers kp0 .. kp0 + SB - 1
         for (int kp0 = 1; kp0 <= SEG; kp0 += SB) {
             uint32_t chg = 0;
+            {  // the batch's m-mers kp0 + W + j roll out base pb + kp0 + W - 1 + j
+                const uint32_t a0 = ra + (uint32_t)(kp0 + W - 1);
+                wob = window64(s_pk, a0);
+                wib = window64(s_pk, a0 + MM);
+            }
 #pragma unroll
             for (int rb = 0; rb < R; ++rb) {
                 if (kp0 + rb * B > SEG) break;  // the segment's last blocks (uniform)
