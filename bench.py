@@ -61,10 +61,10 @@ def parse_args():
     ap.add_argument("--no-small", action="store_true", help="skip the small read-set section")
     ap.add_argument("--no-passes", action="store_true", help="skip the memory-budget (passes) section")
     ap.add_argument("--batch-samples", type=int, default=2000)
-    ap.add_argument("--batch-scale", type=float, default=0.004,
-                    help="genome sizes of the batched mix: log-uniform 10 kbp - 50 Mbp times this")
-    ap.add_argument("--serve-seconds", type=float, default=10.0, help="length of the arrival trace")
-    ap.add_argument("--serve-scale", type=float, default=0.05, help="request sizes: median 20 Mbp times this")
+    ap.add_argument("--batch-scales", default="0.004,0.02",
+                    help="genome sizes of the batched mix: log-uniform 10 kbp - 50 Mbp times each of these")
+    ap.add_argument("--serve-seconds", type=float, default=60.0, help="length of the arrival trace")
+    ap.add_argument("--serve-scale", type=float, default=1.0, help="request sizes: median 20 Mbp times this")
     ap.add_argument("--no-parity-cpu", action="store_true",
                     help="skip the oracle port's digest of the full-size results (about 30 s of host work each)")
     ap.add_argument("--cpu-mbp", type=float, default=1200.0,
@@ -272,14 +272,13 @@ def batched_vs_plain(ctx, n_samples: int, scale: float):
     import ctypes
     import tuna_gb300 as T
     from tuna_gb300 import synth
-    from tuna_gb300.serve import _pinned
     plan = synth.batch_plan(n_samples, scale=scale)
     seqs = [_pinned_copy(synth.fastq_sequence_stream(synth.batch_sample_fastq(s, i))) for i, s in enumerate(plan)]
     bases = int(sum(s.size for s in seqs))
     L = T.library()
     o = T._JobOpts(31, 21, 16, 1, (1 << 64) - 1, 0, 0)
     cap_one = max(s.size for s in seqs)
-    k1, c1 = _pinned(cap_one, np.uint64), _pinned(cap_one, np.uint32)
+    k1, c1 = host_array(cap_one, np.uint64), host_array(cap_one, np.uint32)
     n_out = ctypes.c_uint64()
     st = T._Stats()
 
@@ -294,11 +293,14 @@ def batched_vs_plain(ctx, n_samples: int, scale: float):
     t0 = time.perf_counter()
     per_plain = [plain(i) for i in range(len(seqs))]
     t_plain = time.perf_counter() - t0
-    cap = bases
-    kb, cb = _pinned(cap, np.uint64), _pinned(cap, np.uint32)
     off = np.zeros(len(seqs) + 1, dtype=np.uint64)
     ptrs = (ctypes.c_void_p * len(seqs))(*[s.ctypes.data for s in seqs])
     lens = (ctypes.c_size_t * len(seqs))(*[int(s.size) for s in seqs])
+    # the pairs' count, from a call with no room (TG_ERR_ARG with n_out set)
+    rc = L.tg_count_batch(ctx.h, ctypes.byref(o), len(seqs), ptrs, lens, None, None, None, 0,
+                          ctypes.byref(n_out), ctypes.byref(st))
+    cap = int(n_out.value) + 1024 if rc == 1 else bases
+    kb, cb = host_array(cap, np.uint64), host_array(cap, np.uint32)
 
     def batch():
         rc = L.tg_count_batch(ctx.h, ctypes.byref(o), len(seqs), ptrs, lens, ctypes.c_void_p(kb.ctypes.data),
@@ -315,14 +317,22 @@ def batched_vs_plain(ctx, n_samples: int, scale: float):
     t_batch = statistics.median(ts)
     per_batch = np.diff(off.astype(np.int64)).tolist()
     same_sizes = per_batch == per_plain
-    # bit-exact on a few samples: the plain result against the sample's range of the batch
-    exact = True
-    for i in (0, 1, len(seqs) // 2, len(seqs) - 1):
-        n = plain(i)
-        a = T.Result(k1[:n].reshape(n, 1).copy(), c1[:n].copy(), {}, 31).sorted()
+    # bit-exact against the oracle on 12 samples across the size range: the
+    # digest of the sample's range of the batch equals the oracle's digest of
+    # that sample counted alone (and the plain path's, on the same samples)
+    from oracle import oracle as O
+    order = np.argsort([s.size for s in seqs])
+    picks = sorted(set(int(order[int(q * (len(seqs) - 1))]) for q in np.linspace(0, 1, 12)))
+    exact, checked = True, 0
+    for i in picks:
         lo, hi = int(off[i]), int(off[i + 1])
-        b = T.Result(kb[lo:hi].reshape(-1, 1).copy(), cb[lo:hi].copy(), {}, 31).sorted()
-        exact &= np.array_equal(a.keys, b.keys) and np.array_equal(a.counts, b.counts)
+        got = O.digest_pairs(kb[lo:hi].reshape(-1, 1), cb[lo:hi], 31, threads=os.cpu_count() or 1)
+        want, _ = O.digest_stream(seqs[i], 31, 21, 16, threads=os.cpu_count() or 1)
+        n = plain(i)
+        alone = O.digest_pairs(k1[:n].reshape(-1, 1), c1[:n], 31)
+        exact &= got == want == alone
+        checked += 1
+    release(k1, c1, kb, cb, *seqs)
     return {"workload": f"{len(seqs)} samples, genome sizes log-uniform 10 kbp - 50 Mbp scaled by {scale:g} "
                         f"(so {max(1000, 10_000 * scale) / 1e3:g} kbp floor - {50e6 * scale / 1e3:g} kbp), "
                         f"150 bp reads at 5-50x, 0.3-1% errors, k=31 m=21",
@@ -330,7 +340,8 @@ def batched_vs_plain(ctx, n_samples: int, scale: float):
             "plain_gbases_s": bases / t_plain / 1e9, "batched_gbases_s": bases / t_batch / 1e9,
             "speedup": t_plain / t_batch, "plain_s": t_plain, "batched_s": t_batch,
             "api": "tg_count_seq per sample vs tg_count_batch, pinned host buffers, results in host memory",
-            "same_pairs_per_sample": bool(same_sizes), "bit_exact_checked_samples": bool(exact)}
+            "same_pairs_per_sample": bool(same_sizes), "oracle_checked_samples": checked,
+            "bit_exact_checked_samples": bool(exact)}
 
 
 def output_drain(ctx, dev, n_stream: int):
@@ -569,38 +580,73 @@ def gz_input(fasta: np.ndarray, mbytes: float = 300.0):
     return res
 
 
-def served(seconds: float, scale: float):
+def served(seconds: float, scale: float, pool_size: int = 48):
     """Poisson arrivals at 50 requests/s replayed in real time against the
-    continuous-batching server; latency from arrival to result in host memory."""
-    import tuna_gb300 as T
+    continuous-batching server; latency from arrival to result in host memory.
+    Request sizes follow the configured distribution (log-normal, median 20 Mbp
+    x scale, sigma 1.5, cap 2 Gbp x scale); the replay reuses a pool of
+    `pool_size` generated requests (one third per k), the i-th arrival taking
+    the next pooled request of its k. Answers are dropped as they arrive, so the
+    server's result slabs are recycled."""
+    import threading
     from tuna_gb300 import synth
     from tuna_gb300.serve import Server
     plan = synth.served_plan(50.0, seconds, scale=scale)
-    seqs = [_pinned_copy(synth.fastq_sequence_stream(synth.request_fastq(r, i))) for i, r in enumerate(plan)]
-    bases = int(sum(s.size for s in seqs))
+    by_k = {}
+    for i, r in enumerate(plan[: max(pool_size, 1) * 4]):
+        lst = by_k.setdefault(r.k, [])
+        if len(lst) < max(1, pool_size // 3):
+            lst.append((r, _pinned_copy(synth.fastq_sequence_stream(synth.request_fastq(r, i)))))
+    nxt = {k: 0 for k in by_k}
+    replay = []
+    for r in plan:
+        lst = by_k.get(r.k) or next(iter(by_k.values()))
+        pr, seq = lst[nxt.get(r.k, 0) % len(lst)]
+        nxt[r.k] = nxt.get(r.k, 0) + 1
+        replay.append((r.arrival_s, pr.k, pr.m, seq))
+    lat, batch_of, done_t = [], [], []
+    mu = threading.Lock()
+    left = threading.Semaphore(0)
+
+    def record(f):
+        a = f.result()
+        with mu:
+            lat.append(a.latency_s * 1e3)
+            batch_of.append(a.batch)
+            done_t.append(a.done)
+        left.release()
+
     with Server(0, workers=2) as srv:
-        # warm both workers' contexts
-        for f in [srv.submit(seqs[0], plan[0].k, plan[0].m) for _ in range(2)]:
+        for f in [srv.submit(replay[0][3], replay[0][1], replay[0][2]) for _ in range(2)]:  # warm both workers
             f.result()
         srv.batches = 0
+        srv.batch_sizes.clear()
+        bases = 0
         t0 = time.perf_counter()
-        futs = []
-        for r, s in zip(plan, seqs):
-            dt = t0 + r.arrival_s - time.perf_counter()
+        for arr, k, m, seq in replay:
+            dt = t0 + arr - time.perf_counter()
             if dt > 0:
                 time.sleep(dt)
-            futs.append(srv.submit(s, r.k, r.m))
-        ans = [f.result() for f in futs]
-        t_end = max(a.done for a in ans)
-        n_batches = srv.batches
-    lat = np.array([a.latency_s for a in ans]) * 1e3
+            srv.submit(seq, k, m).add_done_callback(record)
+            bases += int(seq.size)
+        for _ in replay:
+            left.acquire()
+        t_end = max(done_t)
+        sizes = list(srv.batch_sizes)
+    lat_a = np.array(lat)
+    hist = {}
+    for n in sizes:
+        hist[str(n)] = hist.get(str(n), 0) + 1
     return {"workload": f"Poisson 50 req/s for {seconds:g} s, sizes log-normal median {20 * scale:g} Mbp "
                         f"(sigma 1.5, cap {2000 * scale:g} Mbp), reads 100-250 bp at 0.5% error, "
-                        f"k in {{21, 25, 31}}",
-            "requests": len(ans), "bases": bases, "p50_ms": float(np.percentile(lat, 50)),
-            "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max()),
-            "gbases_s": bases / (t_end - t0) / 1e9, "batches": n_batches, "workers": 2,
-            "api": "tuna_gb300.serve.Server over tg_count_batch, results in host memory"}
+                        f"k in {{21, 25, 31}}; {sum(len(v) for v in by_k.values())} generated requests replayed",
+            "requests": len(replay), "bases": bases, "p50_ms": float(np.percentile(lat_a, 50)),
+            "p99_ms": float(np.percentile(lat_a, 99)), "max_ms": float(lat_a.max()),
+            "offered_gbases_s": bases / max(seconds, 1e-9) / 1e9,
+            "gbases_s": bases / (t_end - t0) / 1e9, "batches": len(sizes),
+            "requests_per_batch_mean": float(np.mean(sizes)) if sizes else 0.0,
+            "requests_per_batch_hist": hist, "workers": 2,
+            "api": "tuna_gb300.serve.Server over tg_count_batch, results in page-locked host memory"}
 
 
 # ------------------------------------------------------------------ reference arm
@@ -854,7 +900,8 @@ def main():
 
     batched = None
     if rank == 0 and not args.no_batch:
-        batched = batched_vs_plain(ctx, args.batch_samples, args.batch_scale)
+        batched = {f"scale_{sc}": batched_vs_plain(ctx, args.batch_samples, float(sc))
+                   for sc in args.batch_scales.split(",") if sc}
     serve = None
     if rank == 0 and not args.no_serve:
         serve = served(args.serve_seconds, args.serve_scale)

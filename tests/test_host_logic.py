@@ -101,3 +101,44 @@ def test_server_needs_a_worker():
     from tuna_gb300 import serve
     with pytest.raises(ValueError):
         serve.Server(0, workers=0)
+
+
+def test_server_result_slabs_recycle_after_last_view():
+    """The server's result slabs (tuna_gb300.serve._Pool) go back to the pool
+    only when every array viewing them is gone, and are reused by later
+    batches that fit (a fake allocator stands in for tg_host_alloc)."""
+    import ctypes
+    import gc
+    import numpy as np
+    from tuna_gb300 import serve as S
+
+    class FakeBuffer:
+        def __init__(self, n):
+            self.buf = (ctypes.c_uint8 * n)()
+            self.ptr = ctypes.addressof(self.buf)
+
+        def close(self):
+            pass
+
+    class FakeT:
+        HostBuffer = FakeBuffer
+
+    pool = S._Pool(FakeT)
+    lease = pool.get(1000)
+    keys = lease.view(0, 10, np.uint64)
+    counts = lease.view(80, 5, np.uint32)
+    keys[:] = 3
+    del lease
+    gc.collect()
+    assert not pool._free and int(keys.sum()) == 30
+    del keys
+    gc.collect()
+    assert not pool._free
+    del counts
+    gc.collect()
+    assert len(pool._free) == 1 and pool.allocated == 1
+    again = pool.get(600)
+    assert not pool._free and pool.allocated == 1
+    bigger = pool.get(1 << 21)
+    assert pool.allocated == 2
+    del again, bigger

@@ -72,3 +72,43 @@ def test_served_fastq_requests_match_alone():
             want = ctx.run(31, 21, fastx=fq)[0].sorted()
             got = T.Result(a.keys.copy(), a.counts.copy(), {}, 31).sorted()
             assert np.array_equal(got.keys, want.keys) and np.array_equal(got.counts, want.counts)
+
+
+def test_served_batches_merge_and_match_the_oracle():
+    """Requests queued while the workers are held (paused) are merged: a batch
+    takes every waiting request of the oldest one's kind, so at least one batch
+    holds several requests; every answer equals the oracle's count of that
+    request alone (sorted pairs), for k = 21, 25, 31 interleaved."""
+    import tuna_gb300 as T
+    from oracle import oracle as O
+    from tuna_gb300.serve import Server
+    reqs = _requests()[:12]
+    with Server(0, workers=2, paused=True) as srv:
+        futs = [srv.submit(seq, k, m) for seq, k, m in reqs]
+        srv.resume()
+        answers = [f.result(timeout=300) for f in futs]
+        sizes = list(srv.batch_sizes)
+    assert max(sizes) >= 2 and sum(sizes) == len(reqs), sizes
+    assert max(a.batch for a in answers) >= 2
+    for (seq, k, m), a in zip(reqs, answers):
+        want = O.count_stream(seq, k, m, threads=4)
+        got = T.Result(np.asarray(a.keys).copy(), np.asarray(a.counts).copy(), {}, k).sorted()
+        kw = (k + 31) // 32
+        assert len(got) == len(want)
+        assert np.array_equal(got.keys[:, :kw], want.keys) and np.array_equal(got.counts, want.counts)
+
+
+def test_served_result_slabs_are_reused():
+    """A worker's result memory is reused once the answers that view it are
+    gone: many sequential requests allocate only a few slabs."""
+    import gc
+    from tuna_gb300.serve import Server
+    reqs = _requests()[:3]
+    with Server(0, workers=1) as srv:
+        for _ in range(4):
+            for seq, k, m in reqs:
+                a = srv.submit(seq, k, m).result(timeout=300)
+                assert len(a.keys) == len(a.counts)
+                del a
+                gc.collect()
+        assert srv.batches == 12

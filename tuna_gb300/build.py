@@ -23,7 +23,8 @@ SYNTH_LIB = os.path.join(BUILD, "libtuna_synth.so")
 CLI_BIN = os.path.join(BUILD, "tuna")
 
 # translation units of libtuna_gpu.so
-CU_SOURCES = ["tg_api.cu", "tg_phase1.cu", "tg_phase2.cu", "tg_noalloc.cu", "tg_lex.cu", "tg_format.cu"]
+CU_SOURCES = ["tg_api.cu", "tg_phase1.cu", "tg_phase2.cu", "tg_noalloc.cu", "tg_lex.cu", "tg_format.cu",
+              "tg_link.cu"]
 CPP_SOURCES = ["host/fastx.cpp", "host/output.cpp", "host/hostmem.cpp"]
 
 

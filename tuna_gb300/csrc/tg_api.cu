@@ -400,7 +400,7 @@ static tg_status append_stream(tg_job* j, const uint8_t* src, size_t len, cudaMe
     const tg_status s = stream_reserve(j, len + 1, &d);
     if (s != TG_OK) return s;
     const double t0 = now_ms();
-    if (len) CK(cudaMemcpyAsync(d, src, len, kind, ctx->st), "copy input");
+    if (len) CK(link_copy(d, src, len, kind, ctx->st, ctx->n_sm), "copy input");
     CK(cudaMemsetAsync(d + len, '\n', 1, ctx->st), "separator");
     CK(cudaStreamSynchronize(ctx->st), "copy input");
     if (kind == cudaMemcpyHostToDevice) j->st.h2d_ms += now_ms() - t0;
@@ -473,7 +473,7 @@ static tg_status lex_append_host(tg_job* j, const uint8_t* data, size_t len) {
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
     CK(ctx->ensure(ctx->raw, len + 16), "alloc raw input");
     const double t0 = now_ms();
-    CK(cudaMemcpyAsync(ctx->raw.p, data, len, cudaMemcpyHostToDevice, ctx->st), "copy input");
+    CK(link_copy(ctx->raw.p, data, len, cudaMemcpyHostToDevice, ctx->st, ctx->n_sm), "copy input");
     CK(cudaStreamSynchronize(ctx->st), "copy input");
     j->st.h2d_ms += now_ms() - t0;
     return lex_append(j, ctx->raw.as<uint8_t>(), len, data);
@@ -734,8 +734,8 @@ static tg_status d2h_pageable(tg_ctx* ctx, void* dst, const void* src, size_t by
     const unsigned nt = std::max(1u, std::min(ctx->host_threads, 16u));
     auto issue = [&](size_t c) -> cudaError_t {
         const size_t off = c * CH, len = std::min(CH, bytes - off);
-        cudaError_t e = cudaMemcpyAsync(ctx->stage[c & 1], static_cast<const uint8_t*>(src) + off, len,
-                                        cudaMemcpyDeviceToHost, ctx->st);
+        cudaError_t e = link_copy(ctx->stage[c & 1], static_cast<const uint8_t*>(src) + off, len,
+                                  cudaMemcpyDeviceToHost, ctx->st, ctx->n_sm);
         if (e == cudaSuccess) e = cudaEventRecord(ctx->ev[4 + (c & 1)], ctx->st);
         return e;
     };
@@ -1007,9 +1007,12 @@ static tg_status tg_job_run_impl(tg_job* j) {
             if (j->sink_keys || j->sink_counts) {  // straight into the caller's buffers, as far as they reach
                 const uint64_t m = acc < j->sink_cap ? std::min(n_p, j->sink_cap - acc) : 0;
                 if (m && j->sink_keys)
-                    CK(cudaMemcpy(j->sink_keys + acc * W, po.keys, m * key_bytes(W), cudaMemcpyDeviceToHost), "d2h");
+                    CK(link_copy(j->sink_keys + acc * W, po.keys, m * key_bytes(W), cudaMemcpyDeviceToHost, ctx->st,
+                                 ctx->n_sm), "d2h");
                 if (m && j->sink_counts)
-                    CK(cudaMemcpy(j->sink_counts + acc, po.counts, m * 4, cudaMemcpyDeviceToHost), "d2h");
+                    CK(link_copy(j->sink_counts + acc, po.counts, m * 4, cudaMemcpyDeviceToHost, ctx->st, ctx->n_sm),
+                       "d2h");
+                CK(cudaStreamSynchronize(ctx->st), "d2h");
             } else if (n_p) {
                 j->host_keys.resize((acc + n_p) * W);
                 j->host_counts.resize(acc + n_p);
@@ -1075,9 +1078,10 @@ tg_status tg_job_result_copy(tg_job* j, uint64_t* keys, uint32_t* counts, uint64
     const uint8_t* kd = (multi ? ctx->okeys2 : ctx->okeys).as<uint8_t>();
     const uint32_t* cd = (multi ? ctx->ocnt2 : ctx->ocnt).as<uint32_t>();
     if (keys)
-        CK(cudaMemcpyAsync(keys, kd + first * key_bytes(j->W), n * key_bytes(j->W), cudaMemcpyDeviceToHost, ctx->st),
-           "d2h keys");
-    if (counts) CK(cudaMemcpyAsync(counts, cd + first, n * 4, cudaMemcpyDeviceToHost, ctx->st), "d2h counts");
+        CK(link_copy(keys, kd + first * key_bytes(j->W), n * key_bytes(j->W), cudaMemcpyDeviceToHost, ctx->st,
+                     ctx->n_sm), "d2h keys");
+    if (counts)
+        CK(link_copy(counts, cd + first, n * 4, cudaMemcpyDeviceToHost, ctx->st, ctx->n_sm), "d2h counts");
     CK(cudaStreamSynchronize(ctx->st), "d2h");
     j->st.d2h_ms += now_ms() - t0;
     return TG_OK;
@@ -1228,7 +1232,7 @@ static tg_status tg_job_drain_impl(tg_job* j, tg_format fmt, tg_sink_fn sink, vo
         CK(cudaStreamSynchronize(ctx->st), "format");
         const uint64_t bytes = fmt == TG_FMT_TSV ? (uint64_t)*h_total : fmt_max_bytes((int)fmt, k, m);
         const int cur = (int)(b & 1);
-        CK(cudaMemcpyAsync(ctx->fhost[cur], ctx->fbuf.p, bytes, cudaMemcpyDeviceToHost, ctx->st), "d2h");
+        CK(link_copy(ctx->fhost[cur], ctx->fbuf.p, bytes, cudaMemcpyDeviceToHost, ctx->st, ctx->n_sm), "d2h");
         if (prev >= 0 && sink(ctx->fhost[prev], prev_bytes, prev_pairs, user) != 0)
             s = ctx->fail(TG_ERR_IO, "output sink stopped");
         prev = cur;
@@ -1377,7 +1381,8 @@ static tg_status count_host(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_sam
         uint64_t off = 0;
         for (uint32_t i = 0; i < n_samples && e == cudaSuccess; ++i) {
             if (i > 0) j->sample_start.push_back(off);
-            if (lens[i]) e = cudaMemcpyAsync(ctx->seq.as<uint8_t>() + off, seqs[i], lens[i], cudaMemcpyHostToDevice, ctx->st);
+            if (lens[i])
+                e = link_copy(ctx->seq.as<uint8_t>() + off, seqs[i], lens[i], cudaMemcpyHostToDevice, ctx->st, ctx->n_sm);
             off += lens[i] + 1;
             j->st.input_bytes += lens[i];
         }
@@ -1400,11 +1405,11 @@ static tg_status count_host(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_sam
         if (h <= lo) return TG_OK;
         const double t0 = now_ms();
         if (keys)
-            CK(cudaMemcpyAsync(keys + lo * W, ctx->okeys.as<uint8_t>() + lo * key_bytes(W), (h - lo) * key_bytes(W),
-                               cudaMemcpyDeviceToHost, ctx->st_copy), "d2h keys");
+            CK(link_copy(keys + lo * W, ctx->okeys.as<uint8_t>() + lo * key_bytes(W), (h - lo) * key_bytes(W),
+                         cudaMemcpyDeviceToHost, ctx->st_copy, ctx->n_sm), "d2h keys");
         if (counts)
-            CK(cudaMemcpyAsync(counts + lo, ctx->ocnt.as<uint32_t>() + lo, (h - lo) * 4, cudaMemcpyDeviceToHost,
-                               ctx->st_copy), "d2h counts");
+            CK(link_copy(counts + lo, ctx->ocnt.as<uint32_t>() + lo, (h - lo) * 4, cudaMemcpyDeviceToHost,
+                         ctx->st_copy, ctx->n_sm), "d2h counts");
         d2h_issue_ms += now_ms() - t0;
         return TG_OK;
     };

@@ -47,6 +47,12 @@ cudaError_t launch_format(int fmt, int k, const uint64_t* keys, const uint32_t* 
 // sum, h1, h2.
 cudaError_t launch_digest(int k, const uint64_t* keys, const uint32_t* counts, uint64_t n, unsigned long long* out,
                           int n_sm, cudaStream_t st, int* launches);
+// A copy between device memory and host memory (tg_link.cu): done by a kernel
+// through the mapped address when the host side is page-locked memory mapped
+// for the current device (and both sides are equally aligned mod 16), else by
+// cudaMemcpyAsync; ordered on st like cudaMemcpyAsync.
+cudaError_t link_copy(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaStream_t st, int n_sm,
+                      int* launches = nullptr);
 size_t key_bytes(int W);
 uint32_t count_slots(int W);
 

@@ -7,12 +7,20 @@ device, tg_count_batch_fastx), and its k, m, ci, cx. Requests are queued as
 they arrive. Each of `workers` worker threads owns a device context (its own
 CUDA stream and device buffers); whenever a worker is free it takes every
 waiting request of the same kind with the same (k, m, ci, cx) as the oldest
-one, up to a budget of
-bases sized from the free device memory, and counts them as the samples of one
-job. Requests that arrive while a batch is on the device join a later batch
-as soon as a worker frees up; with two workers two batches are in flight, so
-one batch's host copies and host work overlap the other's kernels. A job keeps
-its samples apart, so every request's result is its result alone.
+one, up to a budget of bases, and counts them as the samples of one job.
+Admission is by free device memory at the moment a batch is taken: the
+budget is the device's free memory now, plus what this worker's context
+already holds, shared among the workers (DEVICE_BYTES_PER_BASE per base).
+Requests that arrive while a batch is on the device join a later batch as soon
+as a worker frees up; with two workers two batches are in flight, so one
+batch's host copies and host work overlap the other's kernels. A job keeps its
+samples apart, so every request's result is its result alone.
+
+Results land in page-locked host memory (tg_host_alloc) that each worker keeps
+and reuses: a slab holds one batch's pairs, the answers of the batch are
+numpy views of it, and the slab returns to its worker when the last array
+viewing it is gone (pinning fresh memory per batch cost tens of milliseconds
+for large batches).
 
 The reference has no serving mode (it counts one input set per process run);
 this is the request loop around the same counting path.
@@ -20,6 +28,7 @@ this is the request loop around the same counting path.
 import ctypes
 import threading
 import time
+import weakref
 from collections import deque
 from concurrent.futures import Future
 from dataclasses import dataclass, field
@@ -53,35 +62,97 @@ class _Req:
     future: Future = field(default_factory=Future)
 
 
-def _pinned(n: int, dtype):
-    """Page-locked host array of n items (torch's pinned allocator when present),
-    else an ordinary numpy array."""
-    try:
-        import torch
-        tdt = {np.uint64: torch.int64, np.uint32: torch.int32, np.uint8: torch.uint8}[dtype]
-        return torch.empty(max(n, 1), dtype=tdt, pin_memory=True).numpy().view(dtype)[:n]
-    except Exception:
-        return np.empty(max(n, 1), dtype=dtype)[:n]
+class _Slab:
+    """Page-locked host memory of one worker (tg_host_alloc)."""
+
+    def __init__(self, T, nbytes: int):
+        self.hb = T.HostBuffer(nbytes)
+        self.nbytes = nbytes
+
+
+class _Pool:
+    """A worker's slabs: grow-only, each reused once every view of it is gone."""
+
+    def __init__(self, T):
+        self._T = T
+        self._free: List[_Slab] = []
+        self._mu = threading.Lock()
+        self.allocated = 0
+
+    def get(self, nbytes: int) -> "_Lease":
+        with self._mu:
+            fit = [s for s in self._free if s.nbytes >= nbytes]
+            if fit:
+                slab = min(fit, key=lambda s: s.nbytes)
+                self._free.remove(slab)
+            else:
+                slab = None
+        if slab is None:
+            # grow-only: round up so that similar batches reuse the slab
+            size = 1 << max(20, (max(1, nbytes) - 1).bit_length())
+            slab = _Slab(self._T, size)
+            self.allocated += 1
+        return _Lease(self, slab)
+
+    def give_back(self, slab: _Slab) -> None:
+        with self._mu:
+            self._free.append(slab)
+
+    def close(self) -> None:
+        with self._mu:
+            for s in self._free:
+                s.hb.close()
+            self._free.clear()
+
+
+class _Lease:
+    """One batch's use of a slab; the slab goes back to the pool when the lease
+    (held by every array viewing it) is collected."""
+
+    def __init__(self, pool: _Pool, slab: _Slab):
+        self.slab = slab
+        weakref.finalize(self, pool.give_back, slab)
+
+    def view(self, offset: int, n: int, dtype) -> np.ndarray:
+        dt = np.dtype(dtype)
+        if offset + n * dt.itemsize > self.slab.nbytes:
+            raise ValueError("view past the slab")
+        return np.asarray(_View(self, self.slab.hb.ptr + offset, n, dt))
+
+
+class _View:
+    """numpy array interface over slab memory; keeps the lease alive."""
+
+    def __init__(self, lease: _Lease, ptr: int, n: int, dt: np.dtype):
+        self._lease = lease
+        self.__array_interface__ = {"data": (ptr, False), "shape": (n,), "typestr": dt.str,
+                                    "version": 3}
 
 
 class Server:
+    """max_batch_bases: a fixed budget of bases per batch instead of admission
+    by free device memory. paused: workers take nothing until resume() (a
+    caller can queue requests first, e.g. to measure merging)."""
+
     def __init__(self, device: int = 0, workers: int = 2, max_batch_bases: Optional[int] = None,
-                 host_threads: int = 0):
+                 host_threads: int = 0, paused: bool = False):
         if workers < 1:
             raise ValueError("a server needs at least one worker")
         import tuna_gb300 as T
         self._T = T
         self._L = T.library()
-        if max_batch_bases is None:
-            free = _free_device_bytes(device)
-            max_batch_bases = max(1 << 20, int(free * 0.8 / max(1, workers) / DEVICE_BYTES_PER_BASE))
-        self.max_batch_bases = int(max_batch_bases)
+        self.device = device
+        self.workers = workers
+        self.max_batch_bases = None if max_batch_bases is None else int(max_batch_bases)
         self._q: Deque[_Req] = deque()
         self._cv = threading.Condition()
         self._stop = False
+        self._paused = bool(paused)
         self._alive = workers       # workers that hold a device context
         self._error: Optional[BaseException] = None  # why no worker is left
         self.batches = 0
+        self.batch_sizes: List[int] = []   # requests per batch, in the order batches were taken
+        self.budgets: List[int] = []       # admission budget (bases) when each batch was taken
         self._threads = [threading.Thread(target=self._work, args=(device, host_threads), daemon=True)
                          for _ in range(workers)]
         for t in self._threads:
@@ -104,9 +175,16 @@ class Server:
             self._cv.notify()
         return r.future
 
+    def resume(self) -> None:
+        """Let the workers take requests (a server made with paused=True)."""
+        with self._cv:
+            self._paused = False
+            self._cv.notify_all()
+
     def close(self) -> None:
         with self._cv:
             self._stop = True
+            self._paused = False
             self._cv.notify_all()
         for t in self._threads:
             t.join()
@@ -118,9 +196,14 @@ class Server:
         self.close()
 
     # ------------------------------------------------------------------ worker
-    def _take(self) -> List[_Req]:
-        batch, self._q = take_batch(self._q, self.max_batch_bases)
-        return batch
+    def _budget(self, held: int) -> int:
+        """Bases one batch may take now: free device memory plus what this
+        worker's context already holds (its grow-only buffers are reused),
+        shared among the workers."""
+        if self.max_batch_bases is not None:
+            return self.max_batch_bases
+        free = _free_device_bytes(self.device) + held
+        return max(1 << 20, int(free * 0.8 / self.workers / DEVICE_BYTES_PER_BASE))
 
     def _work(self, device: int, host_threads: int) -> None:
         T, L = self._T, self._L
@@ -129,22 +212,29 @@ class Server:
         except Exception as e:  # noqa: BLE001 - the last worker lost fails every waiting request
             self._worker_lost(e)
             return
+        pool = _Pool(T)
+        held = 0  # device bytes this worker's context holds (its largest batch so far)
         try:
             while True:
                 with self._cv:
-                    while not self._q and not self._stop:
+                    while (not self._q or self._paused) and not self._stop:
                         self._cv.wait()
                     if not self._q:
                         return
-                    batch = self._take()
+                    budget = self._budget(held)
+                    batch, self._q = take_batch(self._q, budget)
                     self.batches += 1
+                    self.batch_sizes.append(len(batch))
+                    self.budgets.append(budget)
+                held = max(held, DEVICE_BYTES_PER_BASE * sum(int(r.seq.size) for r in batch))
                 try:
-                    self._run(ctx, batch)
+                    self._run(ctx, pool, batch)
                 except Exception as e:  # noqa: BLE001 - every waiting future learns of it
                     for r in batch:
                         if not r.future.done():
                             r.future.set_exception(e)
         finally:
+            pool.close()
             ctx.close()
 
     def _worker_lost(self, e: BaseException) -> None:
@@ -159,7 +249,7 @@ class Server:
                     r.future.set_exception(e)
             self._cv.notify_all()
 
-    def _run(self, ctx, batch: List[_Req]) -> None:
+    def _run(self, ctx, pool: "_Pool", batch: List[_Req]) -> None:
         T, L = self._T, self._L
         k, m, ci, cx, fastx = batch[0].key
         W = 1 if k <= 31 else 2
@@ -167,8 +257,9 @@ class Server:
         ptrs = (ctypes.c_void_p * n)(*[r.seq.ctypes.data if r.seq.size else None for r in batch])
         lens = (ctypes.c_size_t * n)(*[int(r.seq.size) for r in batch])
         cap = max(1, sum(int(r.seq.size) for r in batch))  # pairs <= k-mer instances < bases
-        keys = _pinned(cap * W, np.uint64)
-        cnt = _pinned(cap, np.uint32)
+        lease = pool.get(cap * (8 * W + 4))
+        keys = lease.view(0, cap * W, np.uint64)
+        cnt = lease.view(cap * W * 8, cap, np.uint32)
         off = np.zeros(n + 1, dtype=np.uint64)
         o = T._JobOpts(k, m, 16, ci, cx, 0, 0)
         n_out = ctypes.c_uint64()
