@@ -33,6 +33,8 @@
  *     tg_job_next_sample             set per run): several samples in one pass
  *   hbm_budget_bytes (phase 2 in     the disk mode of src/pipeline.hpp:186-263
  *     passes)
+ *   tg_job_set_spill                 the disk pipeline: per-partition superkmer files
+ *                                    (src/pipeline.hpp:186-263, src/superkmer_io.hpp:154-266)
  *   tg_job_set_shard                 the partitions one worker takes in phase 2
  *                                    (src/count.hpp:322-336), as a static share per
  *                                    device: the partition -> device map
@@ -234,6 +236,26 @@ tg_status tg_job_end(tg_job* job);
 tg_status tg_job_next_sample(tg_job* job);
 uint32_t tg_job_sample_count(const tg_job* job);
 tg_status tg_job_sample_offsets(tg_job* job, uint64_t* offsets);
+
+/* ---- spill: jobs larger than device memory --------------------------------
+ * The disk pipeline of the reference (src/pipeline.hpp:186-263: phase 1 appends
+ * every superkmer to its partition's file, SuperkmerWriter::append_kache,
+ * src/superkmer_io.hpp:154-172; phase 2 replays one partition file at a time,
+ * SuperkmerReader, :196-266). After tg_job_set_spill, the job's input is
+ * handled in chunks of at most chunk_bytes stream bytes (0 = a sixteenth of the
+ * phase-2 memory budget): when a feed would pass that size, Phase 1 runs on
+ * the chunk fed so far and its superkmer records go, by bucket (a run of
+ * consecutive minimizer bins, tg_job_opts.gpu_parts of them, 64 by default),
+ * to host memory (dir == NULL) or to two files per bucket under dir. A
+ * sequence-stream feed longer than a chunk is cut at a byte that separates
+ * runs, a FASTA file before a record's '>'; a FASTQ file, or a single run or
+ * record longer than a chunk, goes whole. tg_job_run then counts in passes over
+ * consecutive buckets that fit the memory budget, uploading each pass's records
+ * and keeping the pairs in host memory (results then stay on the host). The
+ * pairs are the same as without spill. Call before the first feed; a job in
+ * spill mode counts one sample, unsharded, and exports no partitions.
+ * tg_stats.record_bytes receives the bytes spilled. */
+tg_status tg_job_set_spill(tg_job* job, uint64_t chunk_bytes, const char* dir);
 
 /* ---- shards: one job's partitions spread over devices ---------------------
  * Every instance of a canonical k-mer has the same minimizer, so the same bin

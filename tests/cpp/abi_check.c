@@ -95,6 +95,7 @@ int main(int argc, char** argv) {
         jo.gpu_parts = 0;
     }
 
+    EXPECT(tg_job_set_spill(NULL, 0, NULL) == TG_ERR_ARG);
     EXPECT(tg_read_input(NULL, 1, NULL, 0, &len, err, sizeof err) == TG_ERR_ARG);
     if (argc > 1) {
         uint8_t buf[256];

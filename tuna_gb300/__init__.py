@@ -91,7 +91,7 @@ ABI_SYMBOLS = ["tg_ctx_create", "tg_ctx_destroy", "tg_last_error", "tg_ctx_strea
                "tg_count_seq", "tg_count_seq_device_noalloc", "tg_job_next_sample", "tg_job_sample_count",
                "tg_job_sample_offsets", "tg_count_batch", "tg_job_feed_fastx_device", "tg_count_fastx",
                "tg_fastx_to_stream", "tg_read_input", "tg_count_batch_fastx", "tg_job_set_shard",
-               "tg_job_result_digest", "tg_host_alloc", "tg_host_free"]
+               "tg_job_result_digest", "tg_host_alloc", "tg_host_free", "tg_job_set_spill"]
 
 
 def library(build_if_missing: bool = True) -> ctypes.CDLL:
@@ -149,6 +149,7 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
     L.tg_job_set_shard.argtypes = [vp, u32, u32]
     L.tg_job_result_digest.argtypes = [vp, u64, u64, ctypes.POINTER(_Digest)]
     L.tg_host_alloc.argtypes = [sz, ctypes.POINTER(vp)]
+    L.tg_job_set_spill.argtypes = [vp, u64, ctypes.c_char_p]
     L.tg_host_free.argtypes = [vp]
     L.tg_count_batch.argtypes = [vp, ctypes.POINTER(_JobOpts), u32, ctypes.POINTER(vp), ctypes.POINTER(sz), vp, vp,
                                  vp, u64, ctypes.POINTER(u64), ctypes.POINTER(_Stats)]
@@ -157,7 +158,7 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
                "tg_job_drain", "tg_job_write", "tg_job_export_partitions", "tg_job_end", "tg_count_seq",
                "tg_job_next_sample", "tg_job_sample_offsets", "tg_count_batch", "tg_job_feed_fastx_device",
                "tg_count_fastx", "tg_fastx_to_stream", "tg_read_input", "tg_count_batch_fastx",
-               "tg_job_set_shard", "tg_job_result_digest", "tg_host_alloc", "tg_host_free"):
+               "tg_job_set_shard", "tg_job_result_digest", "tg_host_alloc", "tg_host_free", "tg_job_set_spill"):
         getattr(L, fn).restype = i32
     _lib = L
     return L
@@ -288,7 +289,7 @@ class Context:
     def run(self, k: int, m: int, *, seq=None, dev_seq=None, dev_len: int = 0, fastx=None, files=(),
             dev_fastx=None, samples=None, n_parts: int = 16, ci: int = 1, cx: int = _U64_MAX, gpu_parts: int = 0,
             export: bool = False, want_results: bool = True, drain: Optional[int] = None,
-            shard: Optional[tuple] = None, digest: bool = False):
+            shard: Optional[tuple] = None, digest: bool = False, spill: Optional[tuple] = None):
         """Run one job. seq: host stream (bytes / uint8 array); dev_seq: device
         pointer (int) of dev_len bytes; fastx: FASTA/FASTQ bytes; dev_fastx: device
         pointer of dev_len FASTA/FASTQ bytes; files: paths;
@@ -298,7 +299,10 @@ class Context:
         Result.formatted; shard: (s, n) counts only shard s of n of the bins
         (tg_job_set_shard), whose pairs the n shards' results split between them;
         digest: Result.digest (and per sample, Result.sample_digests) from
-        tg_job_result_digest. Returns (Result, partitions or None)."""
+        tg_job_result_digest; spill: (chunk_bytes, dir or None) runs the job in
+        spill mode (tg_job_set_spill: phase 1 per chunk, records to host memory
+        or files under dir, phase 2 in passes). Returns (Result, partitions or
+        None)."""
         L = self._L
         o = self._opts(k, m, n_parts, ci, cx, gpu_parts)
         j = ctypes.c_void_p()
@@ -306,6 +310,9 @@ class Context:
         try:
             if shard is not None:
                 self.check(L.tg_job_set_shard(j, int(shard[0]), int(shard[1])))
+            if spill is not None:
+                d = spill[1] if len(spill) > 1 else None
+                self.check(L.tg_job_set_spill(j, int(spill[0]), os.fsencode(d) if d else None))
             for i, smp in enumerate(samples or ()):
                 if i:
                     self.check(L.tg_job_next_sample(j))

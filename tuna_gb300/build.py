@@ -24,7 +24,7 @@ CLI_BIN = os.path.join(BUILD, "tuna")
 
 # translation units of libtuna_gpu.so
 CU_SOURCES = ["tg_api.cu", "tg_phase1.cu", "tg_phase2.cu", "tg_noalloc.cu", "tg_lex.cu", "tg_format.cu",
-              "tg_link.cu"]
+              "tg_link.cu", "tg_spill.cu"]
 CPP_SOURCES = ["host/fastx.cpp", "host/output.cpp", "host/hostmem.cpp"]
 
 

@@ -33,6 +33,7 @@
 #include <chrono>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <numeric>
 #include <string>
 #include <thread>
@@ -144,7 +145,7 @@ struct tg_ctx {
     unsigned host_threads = 1;
     std::string err;
     DevBuf seq, packed, valid, desc, xdesc, hist, scratch, okeys, ocnt, osamp, samp, okeys2, ocnt2, osoff,
-        misc, fbtab, tables, raw, lexs, fbuf, fscr;
+        misc, fbtab, tables, raw, lexs, fbuf, fscr, sp_desc, sp_bytes, sp_aux;
     uint8_t* fhost[2] = {nullptr, nullptr};  // pinned host buffers of the output drain
     size_t fhost_cap = 0;
     uint8_t* stage[2] = {nullptr, nullptr};  // pinned staging of copies to pageable host memory
@@ -181,6 +182,33 @@ struct tg_ctx {
     }
 };
 
+// Host store of spill mode (tg_job_set_spill): per bucket (a run of
+// 2^20 / nb consecutive bins), its record stream (2-bit bases, four per byte,
+// in the byte order of the packed u32 words; every chunk's part a multiple of
+// 4 bytes) and its descriptors (start = 4 x byte position in the stream), in
+// host memory or in two files per bucket under `dir`; the k-mers per bin of
+// all chunks; the chunks' phase-1 totals.
+struct SpillStore {
+    uint32_t nb = 64;
+    int shift = 14;  // bucket = bin >> shift
+    std::string dir;
+    std::vector<tgh::Bytes> bytes;
+    std::vector<std::vector<uint64_t>> desc;
+    std::vector<uint64_t> n_bytes, n_desc;
+    std::vector<uint64_t> hist;
+    uint64_t kmers = 0, records = 0, runs = 0, bases = 0, chunks = 0, spilled_bytes = 0;
+    std::string path(uint32_t b, const char* what) const {
+        return dir + "/tuna_spill_" + std::to_string(b) + "." + what;
+    }
+    ~SpillStore() {
+        if (dir.empty()) return;
+        for (uint32_t b = 0; b < nb; ++b) {
+            std::remove(path(b, "bytes").c_str());
+            std::remove(path(b, "desc").c_str());
+        }
+    }
+};
+
 struct tg_job {
     tg_ctx* ctx = nullptr;
     tg_job_opts o{};
@@ -213,6 +241,11 @@ struct tg_job {
     uint64_t sink_cap = 0;
     // phase 2 over shard `shard` of `n_shards` runs of consecutive segments only
     uint32_t shard = 0, n_shards = 1;
+    // spill mode: phase 1 per chunk of at most spill_chunk stream bytes, records
+    // to the host store, phase 2 in passes over buckets read back from it
+    bool spill = false;
+    uint64_t spill_chunk = 0;
+    std::unique_ptr<SpillStore> store;
     const uint8_t* seq_ptr() const { return ext ? ext : ctx->seq.as<uint8_t>(); }
 };
 
@@ -370,9 +403,15 @@ tg_status tg_job_begin(tg_ctx* ctx, const tg_job_opts* opts, tg_job** out) {
 
 // Room for `extra` more stream bytes in ctx->seq (a device feed used in place
 // is moved into it first); *at receives the device address of position j->n.
+static tg_status spill_flush(tg_job* j);
+
 static tg_status stream_reserve(tg_job* j, size_t extra, uint8_t** at) {
     tg_ctx* ctx = j->ctx;
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if (j->spill && j->n && j->n + extra > j->spill_chunk) {  // spill mode: this chunk is full
+        const tg_status s = spill_flush(j);
+        if (s != TG_OK) return s;
+    }
     if (j->ext) {
         CK(ctx->ensure(ctx->seq, j->n + extra + 2), "alloc seq");
         CK(cudaMemcpyAsync(ctx->seq.p, j->ext, j->n, cudaMemcpyDeviceToDevice, ctx->st), "copy seq");
@@ -479,8 +518,24 @@ static tg_status lex_append_host(tg_job* j, const uint8_t* data, size_t len) {
     return lex_append(j, ctx->raw.as<uint8_t>(), len, data);
 }
 
+static inline bool is_acgt_byte(uint8_t c) {
+    const uint8_t u = c & 0xDF;
+    return u == 'A' || u == 'C' || u == 'G' || u == 'T';
+}
+
 static tg_status tg_job_feed_seq_impl(tg_job* j, const uint8_t* seq, size_t len) {
     if (!j || (!seq && len)) return TG_ERR_ARG;
+    // spill mode: a feed longer than a chunk goes in pieces cut at a byte that
+    // separates runs (nothing changes: every feed ends with a separator)
+    while (j->spill && len > j->spill_chunk) {
+        size_t cut = (size_t)j->spill_chunk;
+        while (cut > 0 && is_acgt_byte(seq[cut])) --cut;
+        if (cut == 0) break;  // one run longer than a chunk: fed whole
+        const tg_status s = append_stream(j, seq, cut, cudaMemcpyHostToDevice);
+        if (s != TG_OK) return s;
+        seq += cut + 1;
+        len -= cut + 1;
+    }
     return append_stream(j, seq, len, cudaMemcpyHostToDevice);
 }
 
@@ -535,9 +590,25 @@ tg_status tg_job_set_shard(tg_job* j, uint32_t shard, uint32_t n_shards) {
     return TG_OK;
 }
 
+// Spill mode: a FASTA file longer than a chunk goes in pieces cut before a
+// record's '>' (the parser restarts at every '>', so the runs are the same);
+// FASTQ files go whole.
+static tg_status feed_fastx_pieces(tg_job* j, const uint8_t* data, size_t len) {
+    while (j->spill && len > j->spill_chunk && data[0] == '>') {
+        size_t cut = (size_t)j->spill_chunk;
+        while (cut > 1 && !(data[cut] == '>' && data[cut - 1] == '\n')) --cut;
+        if (cut <= 1) break;  // one record longer than a chunk: fed whole
+        const tg_status s = lex_append_host(j, data, cut);
+        if (s != TG_OK) return s;
+        data += cut;
+        len -= cut;
+    }
+    return lex_append_host(j, data, len);
+}
+
 static tg_status tg_job_feed_fastx_impl(tg_job* j, const uint8_t* data, size_t len) {
     if (!j || (!data && len)) return TG_ERR_ARG;
-    return lex_append_host(j, data, len);
+    return feed_fastx_pieces(j, data, len);
 }
 
 tg_status tg_job_feed_fastx(tg_job* j, const uint8_t* data, size_t len) {
@@ -570,7 +641,7 @@ static tg_status tg_job_feed_file_impl(tg_job* j, const char* path) {
         const bool empty = err.rfind("Empty file", 0) == 0;
         return j->ctx->fail(empty ? TG_ERR_PARSE : TG_ERR_IO, err);
     }
-    return lex_append_host(j, raw.data(), raw.size());
+    return feed_fastx_pieces(j, raw.data(), raw.size());
 }
 
 tg_status tg_job_feed_file(tg_job* j, const char* path) {
@@ -749,17 +820,20 @@ static tg_status d2h_pageable(tg_ctx* ctx, void* dst, const void* src, size_t by
     return TG_OK;
 }
 
-static tg_status tg_job_run_impl(tg_job* j) {
-    if (!j) return TG_ERR_ARG;
-    const TraceRange tr("tuna.job_run");
+// Phase 1 over the job's current stream: pack, then the cut into record
+// descriptors (per-CTA lists) and the k-mers per bin. p1: segments of bins
+// (0: chosen from the input size).
+struct P1Out {
+    SampleBins B;
+    unsigned long long cstats[3] = {0, 0, 0};  // k-mers, records, runs
+    unsigned long long n_bases = 0;
+    std::vector<uint32_t> nd;                   // descriptors per list
+};
+
+static tg_status run_phase1(tg_job* j, int* launches_out, P1Out& r, uint32_t p1_force = 0) {
     tg_ctx* ctx = j->ctx;
-    if (j->ran) return ctx->fail(TG_ERR_STATE, "job already ran");
-    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
     int launches = 0;
     const uint64_t n = j->n;
-    const int k = j->o.k;
-    const int W = j->W;
-    j->ran = true;
     if (n >= (1ull << DESC_START_BITS)) return ctx->fail(TG_ERR_ARG, "input stream longer than 2^36 bytes");
     // hash tables for m
     CK(ctx->ensure(ctx->tables, sizeof(HashTables)), "alloc tables");
@@ -780,18 +854,18 @@ static tg_status tg_job_run_impl(tg_job* j) {
                    reinterpret_cast<unsigned long long*>(ctx->misc.as<uint8_t>() + MISC_BASES), ctx->st), "k_pack");
     ++launches;
     CK(cudaEventRecord(ctx->ev[1], ctx->st), "event");
-    unsigned long long n_bases = 0;
-    CK(cudaMemcpyAsync(&n_bases, ctx->misc.as<uint8_t>() + MISC_BASES, 8, cudaMemcpyDeviceToHost, ctx->st), "d2h");
+    CK(cudaMemcpyAsync(&r.n_bases, ctx->misc.as<uint8_t>() + MISC_BASES, 8, cudaMemcpyDeviceToHost, ctx->st), "d2h");
     // ---- phase 1: cut
     nvtxMarkA("tuna.phase1");
-    uint32_t p1 = j->o.gpu_parts;
+    uint32_t p1 = p1_force ? p1_force : j->o.gpu_parts;
     if (!p1) p1 = std::max(j->n_shards, std::min<uint32_t>(1024, std::max<uint32_t>(16, next_pow2_u32(n / 32768))));
     uint32_t p1_bits = 0;
     while ((1u << p1_bits) < p1) ++p1_bits;
     // the bins of the samples (2^20 in all, cut into p1 segments for one sample)
     std::vector<unsigned long long> starts = j->sample_start;
     starts.push_back(n);
-    const SampleBins B = layout_bins(starts, (1u << BIN_BITS) >> p1_bits);
+    r.B = layout_bins(starts, (1u << BIN_BITS) >> p1_bits);
+    const SampleBins& B = r.B;
     const uint32_t ns = (uint32_t)B.base.size();
     if (j->n_shards > 1 && ns > 1) return ctx->fail(TG_ERR_UNSUPPORTED, "a job of several samples cannot be sharded");
     {
@@ -809,14 +883,40 @@ static tg_status tg_job_run_impl(tg_job* j) {
     cs.bits = ctx->samp.as<uint8_t>() + 12 * (size_t)ns + 8;
     cs.n = ns;
     tg_status s = run_cut(j, false, p1_bits, &launches, cs);
+    *launches_out += launches;
     if (s != TG_OK) return s;
-    unsigned long long cstats[3] = {0, 0, 0};
     const uint32_t C = j->n_cta;
-    std::vector<uint32_t> nd(C);
-    CK(cudaMemcpyAsync(cstats, ctx->misc.as<uint8_t>() + MISC_CUT_STATS, 24, cudaMemcpyDeviceToHost, ctx->st), "d2h");
-    CK(cudaMemcpyAsync(nd.data(), ctx->misc.as<uint8_t>() + MISC_NDESC, (size_t)C * 4, cudaMemcpyDeviceToHost,
+    r.nd.assign(C, 0);
+    CK(cudaMemcpyAsync(r.cstats, ctx->misc.as<uint8_t>() + MISC_CUT_STATS, 24, cudaMemcpyDeviceToHost, ctx->st),
+       "d2h");
+    CK(cudaMemcpyAsync(r.nd.data(), ctx->misc.as<uint8_t>() + MISC_NDESC, (size_t)C * 4, cudaMemcpyDeviceToHost,
                        ctx->st), "d2h");
     CK(cudaStreamSynchronize(ctx->st), "phase 1");
+    return TG_OK;
+}
+
+static tg_status run_spill(tg_job* j);
+
+static tg_status tg_job_run_impl(tg_job* j) {
+    if (!j) return TG_ERR_ARG;
+    const TraceRange tr("tuna.job_run");
+    tg_ctx* ctx = j->ctx;
+    if (j->ran) return ctx->fail(TG_ERR_STATE, "job already ran");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if (j->spill) return run_spill(j);
+    int launches = 0;
+    const int k = j->o.k;
+    const int W = j->W;
+    j->ran = true;
+    P1Out r1;
+    const tg_status s1 = run_phase1(j, &launches, r1);
+    if (s1 != TG_OK) return s1;
+    const SampleBins& B = r1.B;
+    const uint32_t ns = (uint32_t)B.base.size();
+    const unsigned long long* cstats = r1.cstats;
+    const unsigned long long n_bases = r1.n_bases;
+    const uint32_t C = j->n_cta;
+    std::vector<uint32_t>& nd = r1.nd;
     nvtxMarkA("tuna.phase2");
     // ---- phase 2: one run over all bins or, when their keys and pairs do not
     // fit in the memory budget, passes over ranges of consecutive segments
@@ -1049,6 +1149,317 @@ static tg_status tg_job_run_impl(tg_job* j) {
 
 tg_status tg_job_run(tg_job* j) {
     return guarded(j ? j->ctx : nullptr, [&] { return tg_job_run_impl(j); });
+}
+
+// ---------------------------------------------------------------- spill mode
+// The device budget phase 2 may use (tg_ctx_opts.hbm_budget_bytes, else free
+// memory plus the context's reusable buffers minus a reserve).
+static tg_status phase2_budget(tg_ctx* ctx, uint64_t* budget) {
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+    const uint64_t have = free_b + ctx->scratch.cap + ctx->okeys.cap + ctx->ocnt.cap;
+    const uint64_t reserve = (2ull << 30) + total_b / 50;
+    *budget = ctx->hbm_budget ? ctx->hbm_budget : (have > reserve ? have - reserve : 0);
+    return TG_OK;
+}
+
+tg_status tg_job_set_spill(tg_job* j, uint64_t chunk_bytes, const char* dir) {
+    if (!j) return TG_ERR_ARG;
+    tg_ctx* ctx = j->ctx;
+    return guarded(ctx, [&]() -> tg_status {
+        if (j->ran || j->n || j->ext) return ctx->fail(TG_ERR_STATE, "spill mode is set before the first feed");
+        if (j->sample_start.size() > 1 || j->n_shards > 1)
+            return ctx->fail(TG_ERR_UNSUPPORTED, "spill mode counts one sample, unsharded");
+        if (!chunk_bytes) {
+            uint64_t budget = 0;
+            const tg_status s = phase2_budget(ctx, &budget);
+            if (s != TG_OK) return s;
+            chunk_bytes = std::max<uint64_t>(1ull << 24, budget / 16);
+        }
+        auto st = std::make_unique<SpillStore>();
+        st->nb = j->o.gpu_parts ? std::max<uint32_t>(16, std::min<uint32_t>(j->o.gpu_parts, SPILL_MAX_BUCKETS)) : 64;
+        st->shift = BIN_BITS;
+        for (uint32_t v = st->nb; v > 1; v >>= 1) --st->shift;
+        st->dir = dir ? dir : "";
+        st->bytes.resize(dir ? 0 : st->nb);
+        st->desc.resize(dir ? 0 : st->nb);
+        st->n_bytes.assign(st->nb, 0);
+        st->n_desc.assign(st->nb, 0);
+        st->hist.assign((size_t)1 << BIN_BITS, 0);
+        if (dir) {  // fresh, empty bucket files
+            for (uint32_t b = 0; b < st->nb; ++b)
+                for (const char* what : {"bytes", "desc"}) {
+                    FILE* f = std::fopen(st->path(b, what).c_str(), "wb");
+                    if (!f) return ctx->fail(TG_ERR_IO, "cannot create spill file " + st->path(b, what));
+                    std::fclose(f);
+                }
+        }
+        j->store = std::move(st);
+        j->spill = true;
+        j->spill_chunk = chunk_bytes;
+        return TG_OK;
+    });
+}
+
+static tg_status append_file(tg_ctx* ctx, const std::string& path, const void* data, size_t bytes) {
+    if (!bytes) return TG_OK;
+    FILE* f = std::fopen(path.c_str(), "ab");
+    if (!f) return ctx->fail(TG_ERR_IO, "cannot open spill file " + path);
+    const size_t w = std::fwrite(data, 1, bytes, f);
+    const bool ok = std::fclose(f) == 0 && w == bytes;
+    return ok ? TG_OK : ctx->fail(TG_ERR_IO, "cannot write spill file " + path);
+}
+
+static tg_status read_file(tg_ctx* ctx, const std::string& path, void* out, size_t bytes) {
+    if (!bytes) return TG_OK;
+    FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) return ctx->fail(TG_ERR_IO, "cannot open spill file " + path);
+    const size_t r = std::fread(out, 1, bytes, f);
+    std::fclose(f);
+    return r == bytes ? TG_OK : ctx->fail(TG_ERR_IO, "short spill file " + path);
+}
+
+// Phase 1 of the chunk fed so far; its records to the store, by bucket.
+static tg_status spill_flush(tg_job* j) {
+    tg_ctx* ctx = j->ctx;
+    SpillStore& S = *j->store;
+    if (!j->n) return TG_OK;
+    int launches = 0;
+    P1Out r;
+    tg_status s = run_phase1(j, &launches, r, S.nb);
+    if (s != TG_OK) return s;
+    const uint32_t nb = S.nb, C = j->n_cta;
+    const uint32_t* d_nd = reinterpret_cast<const uint32_t*>(ctx->misc.as<uint8_t>() + MISC_NDESC);
+    {  // k-mers per bin
+        std::vector<uint32_t> h((size_t)1 << BIN_BITS);
+        CK(cudaMemcpy(h.data(), ctx->hist.p, h.size() * 4, cudaMemcpyDeviceToHost), "d2h");
+        for (size_t b = 0; b < h.size(); ++b) S.hist[b] += h[b];
+    }
+    // per-bucket records and bytes, then the staging layout
+    // sp_aux: totals [2 nb], cursors [2 nb], host shifts [nb] (u64 / i64 each)
+    CK(ctx->ensure(ctx->sp_aux, 8 * 5 * (size_t)nb), "alloc spill counters");
+    unsigned long long* d_tot = ctx->sp_aux.as<unsigned long long>();
+    CK(launch_spill_size(ctx->desc.as<uint64_t>(), j->desc_cap, d_nd, C, j->o.k, S.shift, nb, d_tot, ctx->st),
+       "k_spill_size");
+    std::vector<unsigned long long> tot(2 * (size_t)nb);
+    CK(cudaMemcpyAsync(tot.data(), d_tot, 16 * (size_t)nb, cudaMemcpyDeviceToHost, ctx->st), "d2h");
+    CK(cudaStreamSynchronize(ctx->st), "k_spill_size");
+    std::vector<unsigned long long> cur(2 * (size_t)nb);
+    std::vector<long long> shift(nb);
+    uint64_t recs = 0, bytes = 0;
+    for (uint32_t b = 0; b < nb; ++b) {
+        // a descriptor's start is 4 x the record's byte position in its bucket
+        if (4 * (S.n_bytes[b] + tot[nb + b] + 4) >= (1ull << DESC_START_BITS))
+            return ctx->fail(TG_ERR_UNSUPPORTED, "a spill bucket passes 2^34 bytes; use more buckets (gpu_parts)");
+        cur[b] = recs;
+        cur[nb + b] = bytes;
+        shift[b] = (long long)S.n_bytes[b] - (long long)bytes;
+        recs += tot[b];
+        bytes += (tot[nb + b] + 3) & ~3ull;  // every bucket's part a multiple of 4 bytes
+    }
+    CK(ctx->ensure(ctx->sp_desc, recs * 8 + 8), "alloc spill descriptors");
+    CK(ctx->ensure(ctx->sp_bytes, bytes + 16), "alloc spill bytes");
+    CK(cudaMemsetAsync(ctx->sp_bytes.p, 0, bytes + 16, ctx->st), "memset");
+    unsigned long long* d_cur = d_tot + 2 * (size_t)nb;
+    long long* d_shift = reinterpret_cast<long long*>(d_tot + 4 * (size_t)nb);
+    CK(cudaMemcpyAsync(d_cur, cur.data(), 16 * (size_t)nb, cudaMemcpyHostToDevice, ctx->st), "h2d");
+    CK(cudaMemcpyAsync(d_shift, shift.data(), 8 * (size_t)nb, cudaMemcpyHostToDevice, ctx->st), "h2d");
+    CK(launch_spill_write(ctx->packed.as<uint32_t>(), ctx->desc.as<uint64_t>(), j->desc_cap, d_nd, C, j->o.k,
+                          S.shift, nb, d_cur, d_shift, ctx->sp_desc.as<uint64_t>(), ctx->sp_bytes.as<uint8_t>(),
+                          ctx->st), "k_spill_write");
+    launches += 2;
+    j->lex_launches += launches;  // counted with the job's other launches
+    // to the store
+    std::vector<uint64_t> hd(recs);
+    tgh::Bytes hb(bytes);
+    s = d2h_pageable(ctx, hd.data(), ctx->sp_desc.p, recs * 8);
+    if (s == TG_OK) s = d2h_pageable(ctx, hb.data(), ctx->sp_bytes.p, bytes);
+    if (s != TG_OK) return s;
+    for (uint32_t b = 0; b < nb; ++b) {
+        const uint64_t r0 = cur[b], rn = tot[b];
+        const uint64_t b0 = cur[nb + b], bn = (tot[nb + b] + 3) & ~3ull;
+        if (S.dir.empty()) {
+            S.desc[b].insert(S.desc[b].end(), hd.begin() + r0, hd.begin() + r0 + rn);
+            S.bytes[b].insert(S.bytes[b].end(), hb.begin() + b0, hb.begin() + b0 + bn);
+        } else {
+            s = append_file(ctx, S.path(b, "desc"), hd.data() + r0, rn * 8);
+            if (s == TG_OK) s = append_file(ctx, S.path(b, "bytes"), hb.data() + b0, bn);
+            if (s != TG_OK) return s;
+        }
+        S.n_desc[b] += rn;
+        S.n_bytes[b] += bn;
+    }
+    S.kmers += r.cstats[0];
+    S.records += r.cstats[1];
+    S.runs += r.cstats[2];
+    S.bases += r.n_bases;
+    S.spilled_bytes += recs * 8 + bytes;
+    ++S.chunks;
+    j->n = 0;
+    j->ext = nullptr;
+    return TG_OK;
+}
+
+// Phase 2 of a spill-mode job: passes over consecutive buckets whose keys and
+// pairs fit the budget; each pass uploads its buckets' record streams (one
+// after the other, each at a 16-base boundary after the leading pad) and
+// descriptors (rebased to the pass stream) and counts them.
+static tg_status run_spill(tg_job* j) {
+    tg_ctx* ctx = j->ctx;
+    SpillStore& S = *j->store;
+    tg_status s = spill_flush(j);
+    if (s != TG_OK) return s;
+    j->ran = true;
+    const int W = j->W, k = j->o.k;
+    const uint32_t nb = S.nb;
+    const uint32_t seg_bins = (1u << BIN_BITS) / nb;
+    int launches = 0;
+    // k-mers per bin of all chunks, for the scan of each pass
+    std::vector<uint32_t> h32(S.hist.size());
+    std::vector<uint64_t> bk(nb, 0);
+    for (size_t b = 0; b < S.hist.size(); ++b) {
+        if (S.hist[b] > 0xFFFFFFFFull) return ctx->fail(TG_ERR_UNSUPPORTED, "a bin holds more than 2^32 k-mers");
+        h32[b] = (uint32_t)S.hist[b];
+        bk[b / seg_bins] += S.hist[b];
+    }
+    CK(ctx->ensure(ctx->hist, (size_t)4 << BIN_BITS), "alloc bin histogram");
+    CK(cudaMemcpy(ctx->hist.p, h32.data(), h32.size() * 4, cudaMemcpyHostToDevice), "h2d");
+    const SampleBins B = layout_bins({0ull, 1ull}, seg_bins);
+    uint64_t budget = 0;
+    s = phase2_budget(ctx, &budget);
+    if (s != TG_OK) return s;
+    const uint64_t per_key = 2 * key_bytes(W) + 4 + 24;
+    const uint64_t max_keys = std::max<uint64_t>(1, budget / per_key);
+    std::vector<std::pair<uint32_t, uint32_t>> passes;
+    for (uint32_t b0 = 0, b = 0; b <= nb; ++b) {
+        uint64_t acc = 0, bytes = 0;
+        for (uint32_t x = b0; x < b; ++x) { acc += bk[x]; bytes += S.n_bytes[x]; }
+        const bool full = b < nb && b > b0 && (acc + bk[b] > max_keys || 4 * (bytes + S.n_bytes[b]) >= (1ull << 35));
+        if (b == nb || full) {
+            if (b > b0) passes.emplace_back(b0, b);
+            b0 = b;
+        }
+    }
+    tg_stats& T = j->st;
+    T.group_load_pct = ctx->tuned_pct[W - 1] ? ctx->tuned_pct[W - 1] : 50;
+    auto fallback_table = [&](size_t bytes) -> void* {
+        return ctx->ensure(ctx->fbtab, bytes) == cudaSuccess ? ctx->fbtab.p : nullptr;
+    };
+    j->spilled = true;
+    j->host_keys.clear();
+    j->host_counts.clear();
+    if (!(j->sink_keys || j->sink_counts)) {
+        j->host_keys.reserve(S.kmers * W);
+        j->host_counts.reserve(S.kmers);
+    }
+    std::string msg;
+    uint64_t acc = 0;
+    float ms = 0;
+    const double t0 = now_ms();
+    for (const auto& pr : passes) {
+        uint64_t nbytes = 0, ndesc = 0, nk = 0;
+        for (uint32_t b = pr.first; b < pr.second; ++b) { nbytes += S.n_bytes[b]; ndesc += S.n_desc[b]; nk += bk[b]; }
+        if (ndesc > 0xFFFFFFFFull) return ctx->fail(TG_ERR_UNSUPPORTED, "a spill pass holds more than 2^32 records");
+        // the pass stream: 8 bytes (TG_PAD bases) of padding, the buckets, slack
+        const uint64_t words = packed_words_for(4 * nbytes);
+        CK(ctx->ensure(ctx->packed, words * 4), "alloc packed");
+        CK(cudaMemsetAsync(ctx->packed.p, 0, words * 4, ctx->st), "memset");
+        CK(ctx->ensure(ctx->desc, ndesc * 8 + 8), "alloc descriptors");
+        uint64_t bo = 0, dof = 0;
+        for (uint32_t b = pr.first; b < pr.second; ++b) {
+            uint8_t* dst_bytes = ctx->packed.as<uint8_t>() + 8 + bo;
+            uint64_t* dst_desc = ctx->desc.as<uint64_t>() + dof;
+            if (S.dir.empty()) {
+                CK(cudaMemcpyAsync(dst_bytes, S.bytes[b].data(), S.n_bytes[b], cudaMemcpyHostToDevice, ctx->st), "h2d");
+                CK(cudaMemcpyAsync(dst_desc, S.desc[b].data(), S.n_desc[b] * 8, cudaMemcpyHostToDevice, ctx->st),
+                   "h2d");
+            } else {
+                tgh::Bytes tmp(S.n_bytes[b] + S.n_desc[b] * 8);
+                s = read_file(ctx, S.path(b, "bytes"), tmp.data(), S.n_bytes[b]);
+                if (s == TG_OK) s = read_file(ctx, S.path(b, "desc"), tmp.data() + S.n_bytes[b], S.n_desc[b] * 8);
+                if (s != TG_OK) return s;
+                CK(cudaMemcpyAsync(dst_bytes, tmp.data(), S.n_bytes[b], cudaMemcpyHostToDevice, ctx->st), "h2d");
+                CK(cudaMemcpyAsync(dst_desc, tmp.data() + S.n_bytes[b], S.n_desc[b] * 8, cudaMemcpyHostToDevice,
+                                   ctx->st), "h2d");
+                CK(cudaStreamSynchronize(ctx->st), "h2d");
+            }
+            CK(launch_rebase(dst_desc, S.n_desc[b], 4 * bo, ctx->n_sm, ctx->st), "k_rebase");
+            bo += S.n_bytes[b];
+            dof += S.n_desc[b];
+        }
+        const uint32_t nlist = (uint32_t)ndesc;
+        P2Input in{};
+        in.W = W;
+        in.k = k;
+        in.segs = B.segs.data() + pr.first;
+        in.n_segs = pr.second - pr.first;
+        in.bin_lo = B.segs[pr.first].bin_lo;
+        in.bin_hi = B.segs[pr.second - 1].bin_hi;
+        in.n_sm = (uint32_t)ctx->n_sm;
+        in.packed = ctx->packed.as<uint32_t>();
+        in.desc = ctx->desc.as<uint64_t>();
+        in.desc_cap = std::max<uint64_t>(ndesc, 1);
+        in.n_lists = 1;
+        in.n_desc = &nlist;
+        in.binhist = ctx->hist.as<uint32_t>();
+        in.n_kmers = nk;
+        in.ci = j->o.ci;
+        in.cx = j->o.cx;
+        in.n_samples = 1;
+        in.group_pct = T.group_load_pct;
+        const uint64_t out_cap = std::max<uint64_t>(nk, 1);
+        CK(ctx->ensure(ctx->okeys, out_cap * key_bytes(W)), "alloc output keys");
+        CK(ctx->ensure(ctx->ocnt, out_cap * 4), "alloc output counts");
+        const size_t p2_bytes = phase2_scratch_bytes(in);
+        CK(ctx->ensure(ctx->scratch, p2_bytes), "alloc phase-2 scratch");
+        P2Output po{};
+        po.keys = ctx->okeys.p;
+        po.counts = ctx->ocnt.as<uint32_t>();
+        po.cap = out_cap;
+        CK(cudaEventRecord(ctx->ev[6], ctx->st), "event");
+        const tg_status ps = phase2_run(in, ctx->scratch.p, p2_bytes, po, fallback_table, ctx->st, ctx->ev[7],
+                                        &launches, msg, P2Overlap());
+        if (ps != TG_OK) return ctx->fail(ps, msg);
+        CK(cudaEventRecord(ctx->ev[8], ctx->st), "event");
+        CK(cudaEventSynchronize(ctx->ev[8]), "sync");
+        cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]); T.phase2_keys_ms += ms;
+        cudaEventElapsedTime(&ms, ctx->ev[7], ctx->ev[8]); T.phase2_count_ms += ms;
+        const uint64_t n_p = po.n_out;
+        const double c0 = now_ms();
+        if (j->sink_keys || j->sink_counts) {
+            const uint64_t m = acc < j->sink_cap ? std::min(n_p, j->sink_cap - acc) : 0;
+            if (m && j->sink_keys)
+                CK(link_copy(j->sink_keys + acc * W, po.keys, m * key_bytes(W), cudaMemcpyDeviceToHost, ctx->st,
+                             ctx->n_sm), "d2h");
+            if (m && j->sink_counts)
+                CK(link_copy(j->sink_counts + acc, po.counts, m * 4, cudaMemcpyDeviceToHost, ctx->st, ctx->n_sm), "d2h");
+            CK(cudaStreamSynchronize(ctx->st), "d2h");
+        } else if (n_p) {
+            j->host_keys.resize((acc + n_p) * W);
+            j->host_counts.resize(acc + n_p);
+            s = d2h_pageable(ctx, j->host_keys.data() + acc * W, po.keys, n_p * key_bytes(W));
+            if (s == TG_OK) s = d2h_pageable(ctx, j->host_counts.data() + acc, po.counts, n_p * 4);
+            if (s != TG_OK) return s;
+        }
+        T.d2h_ms += now_ms() - c0;
+        acc += n_p;
+        T.distinct += po.distinct;
+        T.fallback_groups += po.fallback_groups;
+        T.groups += po.groups;
+        T.heavy_groups += (uint32_t)po.heavy_groups;
+    }
+    T.phase2_ms = now_ms() - t0;
+    T.phase2_passes = passes.size();
+    j->n_out = acc;
+    T.bases = S.bases;
+    T.runs = S.runs;
+    T.kmers = S.kmers;
+    T.superkmers = S.records;
+    T.out = acc;
+    T.gpu_parts = nb;
+    T.record_bytes = S.spilled_bytes;
+    T.gpu_launches = (uint64_t)(launches + j->lex_launches);
+    return TG_OK;
 }
 
 tg_status tg_job_stats(const tg_job* j, tg_stats* out) {

@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <functional>
 #include <string>
 #include <vector>
@@ -53,6 +54,23 @@ cudaError_t launch_digest(int k, const uint64_t* keys, const uint32_t* counts, u
 // cudaMemcpyAsync; ordered on st like cudaMemcpyAsync.
 cudaError_t link_copy(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaStream_t st, int n_sm,
                       int* launches = nullptr);
+// The device address of host memory that is page-locked and mapped for the
+// current device, else null (pageable memory, device memory, bad pointers).
+const void* mapped_address(const void* host);
+// Spill mode (tg_spill.cu): records of the phase-1 descriptor lists to
+// per-bucket staging areas (bucket = bin >> shift, at most SPILL_MAX_BUCKETS).
+// launch_spill_size: totals[b] records and totals[nb + b] bytes of bucket b.
+// launch_spill_write: cursors[b] / cursors[nb + b] start at bucket b's staging
+// base (records / bytes); host_shift[b] = the bucket stream's length before
+// this chunk minus its staging byte base; staging byte bases and stream lengths
+// are multiples of 4. launch_rebase: add `add` to the start of n descriptors.
+constexpr uint32_t SPILL_MAX_BUCKETS = 1024;
+cudaError_t launch_spill_size(const uint64_t* desc, uint64_t desc_cap, const uint32_t* n_desc, uint32_t n_lists,
+                              int k, int shift, uint32_t nb, unsigned long long* totals, cudaStream_t st);
+cudaError_t launch_spill_write(const uint32_t* packed, const uint64_t* desc, uint64_t desc_cap, const uint32_t* n_desc,
+                               uint32_t n_lists, int k, int shift, uint32_t nb, unsigned long long* cursors,
+                               const long long* host_shift, uint64_t* out_desc, uint8_t* out_bytes, cudaStream_t st);
+cudaError_t launch_rebase(uint64_t* desc, uint64_t n, uint64_t add, int n_sm, cudaStream_t st);
 size_t key_bytes(int W);
 uint32_t count_slots(int W);
 

@@ -20,21 +20,34 @@ constexpr size_t LINK_MIN_BYTES = 1u << 20;
 
 // n bytes from src to dst (either may be mapped host memory); src and dst have
 // the same alignment mod 16: bytes up to dst's first 16-byte boundary and after
-// its last one are copied by the first warp, the rest as 16-byte words.
-__global__ void __launch_bounds__(512) k_link_copy(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst,
-                                                   size_t n) {
+// its last one are copied by the first warp, the rest as 16-byte words, two
+// in flight per thread. Narrow CTAs (128 threads, few registers) so that one
+// fits on an SM beside a resident counting CTA: the copy of a counting wave's
+// pairs runs while the next wave counts.
+constexpr int LINK_THREADS = 128;
+
+__global__ void __launch_bounds__(LINK_THREADS, 8) k_link_copy(const uint8_t* __restrict__ src,
+                                                            uint8_t* __restrict__ dst, size_t n) {
     const size_t mis = (16 - (reinterpret_cast<uintptr_t>(dst) & 15)) & 15;
     const size_t head = mis < n ? mis : n;
     const size_t nv = (n - head) / 16;
     const uint4* s = reinterpret_cast<const uint4*>(src + head);
     uint4* d = reinterpret_cast<uint4*>(dst + head);
     const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += stride) d[i] = s[i];
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + stride < nv; i += 2 * stride) {
+        const uint4 a = s[i], b = s[i + stride];
+        d[i] = a;
+        d[i + stride] = b;
+    }
+    for (; i < nv; i += stride) d[i] = s[i];
     if (blockIdx.x == 0 && threadIdx.x < 32) {
         for (size_t b = threadIdx.x; b < head; b += 32) dst[b] = src[b];
         for (size_t b = head + nv * 16 + threadIdx.x; b < n; b += 32) dst[b] = src[b];
     }
 }
+
+}  // namespace
 
 // The device address of a host pointer when it lies in page-locked memory
 // mapped for the current device, else null.
@@ -47,8 +60,6 @@ const void* mapped_address(const void* host) {
     return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
-}  // namespace
-
 cudaError_t link_copy(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaStream_t st, int n_sm,
                       int* launches) {
     if (bytes >= LINK_MIN_BYTES && (kind == cudaMemcpyHostToDevice || kind == cudaMemcpyDeviceToHost)) {
@@ -57,8 +68,9 @@ cudaError_t link_copy(void* dst, const void* src, size_t bytes, cudaMemcpyKind k
         if (kind == cudaMemcpyHostToDevice) s = mapped_address(src);
         else d = const_cast<void*>(mapped_address(dst));
         if (s && d && ((reinterpret_cast<uintptr_t>(s) ^ reinterpret_cast<uintptr_t>(d)) & 15) == 0) {
-            const unsigned grid = (unsigned)(n_sm > 0 ? n_sm : 1) * 8;
-            k_link_copy<<<grid, 512, 0, st>>>(static_cast<const uint8_t*>(s), static_cast<uint8_t*>(d), bytes);
+            const unsigned grid = (unsigned)(n_sm > 0 ? n_sm : 1) * 2;
+            k_link_copy<<<grid, LINK_THREADS, 0, st>>>(static_cast<const uint8_t*>(s), static_cast<uint8_t*>(d),
+                                                       bytes);
             if (launches) ++*launches;
             return cudaGetLastError();
         }

@@ -409,7 +409,12 @@ struct CountSmem {
 // and a half-full table has fewer collisions (measured: 0.7 -> 0.5 of the
 // table, 16.1 -> 14.0 ms for 0.93 G keys).
 template <int W>
-__global__ void __launch_bounds__(COUNT_THREADS, COUNT_PER_SM) k_count(CountParams P) {
+//
+// At most 56 registers per thread (no spills; 64 without the cap): 1,024 x 56
+// leaves 8,192 of the SM's registers, room for one 128-thread CTA of the
+// host-link copy (tg_link.cu) beside each counting CTA, so the copy of a wave's
+// pairs to host memory runs while the next wave counts.
+__global__ void __maxnreg__(56) k_count(CountParams P) {
     using O = KeyOps<W>;
     using Key = typename O::Key;
     constexpr int U = W == 1 ? 4 : 2;                 // keys per thread per round

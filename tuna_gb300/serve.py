@@ -1,9 +1,9 @@
-"""Serving: a continuous-batching request loop over the batched entry point
-(tg_count_batch, include/tuna_gpu.h).
+"""Serving: a continuous-batching request loop over jobs of several samples
+(tg_job_next_sample and the job API of include/tuna_gpu.h).
 
 A request is one count job: a sequence stream (non-ACGT bytes separate runs,
 as tg_job_feed_seq takes it) or the bytes of a FASTA/FASTQ file (lexed on the
-device, tg_count_batch_fastx), and its k, m, ci, cx. Requests are queued as
+device, tg_job_feed_fastx), and its k, m, ci, cx. Requests are queued as
 they arrive. Each of `workers` worker threads owns a device context (its own
 CUDA stream and device buffers); whenever a worker is free it takes every
 waiting request of the same kind with the same (k, m, ci, cx) as the oldest
@@ -17,10 +17,10 @@ batch's host copies and host work overlap the other's kernels. A job keeps its
 samples apart, so every request's result is its result alone.
 
 Results land in page-locked host memory (tg_host_alloc) that each worker keeps
-and reuses: a slab holds one batch's pairs, the answers of the batch are
-numpy views of it, and the slab returns to its worker when the last array
-viewing it is gone (pinning fresh memory per batch cost tens of milliseconds
-for large batches).
+and reuses: a slab holds one batch's pairs (sized by their number, known once
+the job has run), the answers of the batch are numpy views of it, and the slab
+returns to its worker when the last array viewing it is gone (pinning fresh
+memory per batch cost tens of milliseconds to a second for large batches).
 
 The reference has no serving mode (it counts one input set per process run);
 this is the request loop around the same counting path.
@@ -132,10 +132,12 @@ class _View:
 class Server:
     """max_batch_bases: a fixed budget of bases per batch instead of admission
     by free device memory. paused: workers take nothing until resume() (a
-    caller can queue requests first, e.g. to measure merging)."""
+    caller can queue requests first, e.g. to measure merging). slab_bytes:
+    page-locked result memory each worker pins when it starts (more is pinned,
+    and kept, when a batch needs it)."""
 
     def __init__(self, device: int = 0, workers: int = 2, max_batch_bases: Optional[int] = None,
-                 host_threads: int = 0, paused: bool = False):
+                 host_threads: int = 0, paused: bool = False, slab_bytes: int = 1 << 30):
         if workers < 1:
             raise ValueError("a server needs at least one worker")
         import tuna_gb300 as T
@@ -143,6 +145,7 @@ class Server:
         self._L = T.library()
         self.device = device
         self.workers = workers
+        self.slab_bytes = int(slab_bytes)  # page-locked result memory each worker pins at start
         self.max_batch_bases = None if max_batch_bases is None else int(max_batch_bases)
         self._q: Deque[_Req] = deque()
         self._cv = threading.Condition()
@@ -213,6 +216,8 @@ class Server:
             self._worker_lost(e)
             return
         pool = _Pool(T)
+        if self.slab_bytes:
+            pool.give_back(_Slab(T, self.slab_bytes))  # pinned once, at start
         held = 0  # device bytes this worker's context holds (its largest batch so far)
         try:
             while True:
@@ -250,27 +255,39 @@ class Server:
             self._cv.notify_all()
 
     def _run(self, ctx, pool: "_Pool", batch: List[_Req]) -> None:
+        """One batch as one job of several samples (the job API): the pairs stay
+        on the device until the job has run, then go to a slab sized by their
+        number (at most the pairs bound of tg_count_batch's cap, bases, is
+        usually several times too large), copied by the library's host-link
+        copy into the page-locked slab."""
         T, L = self._T, self._L
         k, m, ci, cx, fastx = batch[0].key
         W = 1 if k <= 31 else 2
         n = len(batch)
-        ptrs = (ctypes.c_void_p * n)(*[r.seq.ctypes.data if r.seq.size else None for r in batch])
-        lens = (ctypes.c_size_t * n)(*[int(r.seq.size) for r in batch])
-        cap = max(1, sum(int(r.seq.size) for r in batch))  # pairs <= k-mer instances < bases
-        lease = pool.get(cap * (8 * W + 4))
-        keys = lease.view(0, cap * W, np.uint64)
-        cnt = lease.view(cap * W * 8, cap, np.uint32)
-        off = np.zeros(n + 1, dtype=np.uint64)
         o = T._JobOpts(k, m, 16, ci, cx, 0, 0)
-        n_out = ctypes.c_uint64()
-        st = T._Stats()
-        fn = L.tg_count_batch_fastx if fastx else L.tg_count_batch
-        rc = fn(ctx.h, ctypes.byref(o), n, ptrs, lens, ctypes.c_void_p(keys.ctypes.data),
-                ctypes.c_void_p(cnt.ctypes.data), ctypes.c_void_p(off.ctypes.data), cap,
-                ctypes.byref(n_out), ctypes.byref(st))
-        ctx.check(rc)
+        j = ctypes.c_void_p()
+        ctx.check(L.tg_job_begin(ctx.h, ctypes.byref(o), ctypes.byref(j)))
+        try:
+            feed = L.tg_job_feed_fastx if fastx else L.tg_job_feed_seq
+            for i, r in enumerate(batch):
+                if i:
+                    ctx.check(L.tg_job_next_sample(j))
+                if r.seq.size:
+                    ctx.check(feed(j, ctypes.c_void_p(r.seq.ctypes.data), int(r.seq.size)))
+            ctx.check(L.tg_job_run(j))
+            n_out = int(L.tg_job_result_size(j))
+            lease = pool.get(max(1, n_out) * (8 * W + 4))
+            keys = lease.view(0, n_out * W, np.uint64)
+            cnt = lease.view(n_out * W * 8, n_out, np.uint32)
+            if n_out:
+                ctx.check(L.tg_job_result_copy(j, ctypes.c_void_p(keys.ctypes.data), ctypes.c_void_p(cnt.ctypes.data),
+                                               0, n_out))
+            off = np.zeros(n + 1, dtype=np.uint64)
+            ctx.check(L.tg_job_sample_offsets(j, ctypes.c_void_p(off.ctypes.data)))
+        finally:
+            L.tg_job_end(j)
         done = time.perf_counter()
-        kk = keys[: int(n_out.value) * W].reshape(-1, W)
+        kk = keys.reshape(-1, W)
         for i, r in enumerate(batch):
             a, b = int(off[i]), int(off[i + 1])
             r.future.set_result(Answer(kk[a:b], cnt[a:b], r.arrival, done, n))
