@@ -130,7 +130,9 @@ struct KeysParams {
     const uint32_t* packed;
     const uint64_t* desc;              // phase-1 descriptor lists
     const Slice* slices;
-    unsigned long long* kofs;          // [2^20 + 1] first key of each bin; advanced by k_keys
+    unsigned long long* kofs;          // [2^20 + 1] first key of each bin; a group's first bin's entry
+                                       // is the group's cursor, advanced by k_keys
+    uint32_t* gfirst;                  // [2^20] first bin of each bin's group (written by k_plan)
     const Segment* segs;               // k_plan: one warp per segment
     uint32_t n_segs;
     uint32_t target;                   // k-mer instances per group

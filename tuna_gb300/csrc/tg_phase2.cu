@@ -16,7 +16,7 @@
 //   k_scan_*    bin counts -> key offsets
 //   k_plan      per segment (a run of bins of one sample): groups of whole bins
 //               of at most `target` k-mers
-//   k_keys      every k-mer's canonical key, written at its bin's cursor, so
+//   k_keys      every k-mer's canonical key, written at its group's cursor, so
 //               the keys of a group are one contiguous range of the key array
 //   k_count     persistent, one CTA per SM: each group's keys are read with
 //               coalesced loads (the next round's already in flight while one
@@ -161,7 +161,9 @@ __device__ __forceinline__ U128 kmer_key<2>(const uint32_t* __restrict__ pk, uin
 // from the scanned key offsets ko[bin]. Greedy, in bin order: a group starting
 // at bin s takes the most bins e - s with at most `target` keys (one bin if that
 // bin alone is larger; such a group is listed as heavy). Each step is one
-// upper-bound search over ko, done by the warp as a 32-way search.
+// upper-bound search over ko, done by the warp as a 32-way search. Every bin of
+// the group gets the group's first bin in gfirst: k_keys appends all of the
+// group's keys at that bin's cursor.
 constexpr int PLAN_THREADS = 256;
 
 __global__ void __launch_bounds__(PLAN_THREADS) k_plan(KeysParams P) {
@@ -192,6 +194,7 @@ __global__ void __launch_bounds__(PLAN_THREADS) k_plan(KeysParams P) {
         }
         const uint32_t e = lo;
         const unsigned long long ke = ko[e];
+        for (uint32_t b = s + (uint32_t)lane; b < e; b += 32) P.gfirst[seg.bin_lo + b] = seg.bin_lo + s;
         if (lane == 0) {
             const int heavy = ke - ks > T ? 1 : 0;
             const unsigned long long q = atomicAdd(&P.ctr[heavy ? P2C_HEAVY : P2C_NORMAL], 1ull);
@@ -214,10 +217,15 @@ __global__ void __launch_bounds__(PLAN_THREADS) k_plan(KeysParams P) {
 // ---------------------------------------------------------------- k_keys
 // Every k-mer of a slice of the phase-1 descriptor lists (in stream order, so
 // the packed bases are read front to back): canonical key written at its
-// bin's cursor. A warp takes 32 descriptors at a time; each reserves
-// its k-mers' places with one global atomic on its bin cursor, then the
-// warp's lanes take the batch's k-mers in order (consecutive lanes,
-// consecutive keys).
+// group's cursor (the cursor of the group's first bin, gfirst). A warp takes 32
+// descriptors at a time; each reserves its k-mers' places with one global
+// atomic on that cursor, then the warp's lanes take the batch's k-mers in order
+// (consecutive lanes, consecutive keys). Keys appended per group rather than
+// per bin: a group's keys are the same contiguous range, in another order
+// inside it, with about a third as many places being written at once (groups
+// of ~3 bins), so more of the partly written sectors are completed in L2.
+// The descriptors are loaded two batches ahead and the next batch's gfirst
+// entries one batch ahead, so neither load delays the atomic.
 //
 // A run restricted to a range of bins (the passes of a job larger than the
 // memory budget) keeps only the records of those bins, moved to the front of
@@ -226,32 +234,45 @@ template <int W>
 __global__ void __launch_bounds__(P2_THREADS) k_keys(KeysParams P) {
     using O = KeyOps<W>;
     __shared__ uint64_t s_keep[P2_THREADS];
+    __shared__ uint32_t s_keepg[P2_THREADS];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const Slice sl = P.slices[blockIdx.x];
     const uint64_t* d = P.desc + sl.r_lo;
     const uint32_t n = (uint32_t)(sl.r_hi - sl.r_lo);
     const int k = P.k;
     const bool filt = P.bin_lo != 0 || P.bin_hi != (1u << BIN_BITS);
-    uint64_t dnext = (uint32_t)wid * 32 + lane < n ? d[(uint32_t)wid * 32 + lane] : 0;
+    auto load_desc = [&](uint32_t i) -> uint64_t { return i < n ? d[i] : 0; };
+    // gfirst of a descriptor's bin (any bin of a descriptor is below 2^20;
+    // bins outside this run's range are read but not used)
+    auto group_of = [&](uint64_t dv) -> uint32_t { return desc_nk(dv) ? P.gfirst[desc_bin(dv)] : 0u; };
+    const uint32_t b0 = (uint32_t)wid * 32 + lane;
+    uint64_t dnext = load_desc(b0);                 // batch i + 1 (loaded)
+    uint32_t gnext = group_of(dnext);
+    uint64_t dnext2 = load_desc(b0 + P2_THREADS);   // batch i + 2 (in flight)
     for (uint32_t base = (uint32_t)wid * 32; base < n; base += P2_THREADS) {
-        uint64_t dv = dnext;  // this batch; the next one is loaded while it is processed
-        {
-            const uint32_t i = base + P2_THREADS + lane;
-            dnext = i < n ? d[i] : 0;
-        }
+        uint64_t dv = dnext;
+        uint32_t gv = gnext;
+        dnext = dnext2;
+        gnext = group_of(dnext);
+        dnext2 = load_desc(base + 2 * P2_THREADS + lane);
         if (filt) {
             const uint32_t b = desc_bin(dv);
             const bool keep = desc_nk(dv) && b >= P.bin_lo && b < P.bin_hi;
             const unsigned m = __ballot_sync(0xffffffffu, keep);
-            if (keep) s_keep[wid * 32 + __popc(m & ((1u << lane) - 1u))] = dv;
+            if (keep) {
+                const uint32_t j = wid * 32 + __popc(m & ((1u << lane) - 1u));
+                s_keep[j] = dv;
+                s_keepg[j] = gv;
+            }
             __syncwarp();
             dv = lane < __popc(m) ? s_keep[wid * 32 + lane] : 0;
+            gv = lane < __popc(m) ? s_keepg[wid * 32 + lane] : 0;
             __syncwarp();
             if (m == 0) continue;
         }
         const uint32_t nk = desc_nk(dv);  // 0 past the slice; at least 1 otherwise
         unsigned long long koff = 0;
-        if (nk) koff = atomicAdd(&P.kofs[desc_bin(dv)], (unsigned long long)nk);
+        if (nk) koff = atomicAdd(&P.kofs[gv], (unsigned long long)nk);
         uint32_t incl = nk;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -300,6 +321,12 @@ __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }
 
+// A slot's count in shared memory is its key's occurrences after the first:
+// the thread that claims a slot adds nothing (its key counts through the claim),
+// later occurrences add 1, and the output count is the stored value + 1. Most
+// keys of a group occur once, so most keys take one shared atomic (the CAS),
+// not two.
+//
 // 128-bit keys: slots probed in order from the home slot h with the CAS itself
 // (a 128-bit key cannot be read in one single-copy-atomic load, and a torn
 // read could skip the slot that holds the same k-mer). Returns 1 for a new key,
@@ -309,7 +336,7 @@ __device__ __forceinline__ int claim_cas(U128* keys, uint32_t* cnt, uint32_t mas
     using O = KeyOps<2>;
     for (uint32_t p = 0; p < PROBE_LIMIT; ++p) {
         const U128 prev = O::cas(&keys[h], O::empty(), key);
-        if (O::is_empty(prev)) { atomicAdd(&cnt[h], 1u); slot = h; return 1; }
+        if (O::is_empty(prev)) { slot = h; return 1; }
         if (O::eq(prev, key)) { atomicAdd(&cnt[h], 1u); return 0; }
         h = (h + 1) & mask;
     }
@@ -317,9 +344,12 @@ __device__ __forceinline__ int claim_cas(U128* keys, uint32_t* cnt, uint32_t mas
 }
 
 // The 64-bit table as buckets of 4 slots (32 bytes). A key's probe order is
-// fixed: the slots of its home bucket in order, then the next bucket's, and so
-// on, so two inserts of one key meet in the same slot. One probe reads a whole
-// bucket (two 16-byte loads; each 8-byte slot is read atomically). If the key
+// fixed: its home slot, then the slots of its home bucket (which holds the home
+// slot) in order, then the next bucket's, and so on; a key takes the first slot
+// of that order that is empty when it comes, and slots are never emptied during
+// a group, so two inserts of one key meet in the same slot. After the home slot
+// one probe reads a whole bucket (two 16-byte loads; each 8-byte slot is read
+// atomically). If the key
 // is in the bucket, it is counted there (a slot once taken keeps its key);
 // otherwise the first empty slot is claimed by CAS, and a CAS lost to another
 // key re-reads the bucket. Returns 1 for a new key, 0 for a known one, -1 after
@@ -334,7 +364,21 @@ __device__ __forceinline__ void lds_bucket(const unsigned long long* p, unsigned
 }
 
 __device__ __forceinline__ int claim_bucket(unsigned long long* keys, uint32_t* cnt, uint32_t bmask,
-                                            unsigned long long key, uint32_t b, uint32_t& slot) {
+                                            unsigned long long key, uint32_t hs, uint32_t& slot) {
+    // the home slot first (one 8-byte load): in a table at most half full it is
+    // usually empty or holds the key (20 % less k_count time than reading the
+    // whole bucket first); the probe order goes on with the home bucket's slots
+    {
+        unsigned long long v0;
+        asm volatile("ld.volatile.shared.u64 %0, [%1];" : "=l"(v0) : "r"(smem_addr(keys + hs)));
+        if (v0 == key) { atomicAdd(&cnt[hs], 1u); return 0; }
+        if (v0 == ~0ull) {
+            const unsigned long long prev = atomicCAS(&keys[hs], ~0ull, key);
+            if (prev == ~0ull) { slot = hs; return 1; }
+            if (prev == key) { atomicAdd(&cnt[hs], 1u); return 0; }
+        }
+    }
+    uint32_t b = hs / BUCKET;
     for (uint32_t p = 0; p < PROBE_BUCKETS;) {
         unsigned long long v[BUCKET];
         lds_bucket(keys + b * BUCKET, v);
@@ -347,11 +391,8 @@ __device__ __forceinline__ int claim_bucket(unsigned long long* keys, uint32_t* 
         if (hit >= 0) { atomicAdd(&cnt[b * BUCKET + hit], 1u); return 0; }
         if (emp < 0) { b = (b + 1) & bmask; ++p; continue; }
         const unsigned long long prev = atomicCAS(&keys[b * BUCKET + emp], ~0ull, key);
-        if (prev == ~0ull || prev == key) {
-            atomicAdd(&cnt[b * BUCKET + emp], 1u);
-            slot = b * BUCKET + emp;
-            return prev == key ? 0 : 1;
-        }
+        if (prev == ~0ull) { slot = b * BUCKET + emp; return 1; }
+        if (prev == key) { atomicAdd(&cnt[b * BUCKET + emp], 1u); return 0; }
         // the slot went to another key: read the bucket again
     }
     return -1;
@@ -411,9 +452,9 @@ struct CountSmem {
 template <int W>
 //
 // At most 56 registers per thread (no spills; 64 without the cap): 1,024 x 56
-// leaves 8,192 of the SM's registers, room for one 128-thread CTA of the
-// host-link copy (tg_link.cu) beside each counting CTA, so the copy of a wave's
-// pairs to host memory runs while the next wave counts.
+// leaves 8,192 of the SM's registers, room for one CTA of the host-link copy
+// (tg_link.cu: 256 threads x 32 registers) beside each counting CTA, so the
+// copy of a wave's pairs to host memory runs while the next wave counts.
 __global__ void __maxnreg__(56) k_count(CountParams P) {
     using O = KeyOps<W>;
     using Key = typename O::Key;
@@ -492,7 +533,7 @@ __global__ void __maxnreg__(56) k_count(CountParams P) {
                     int res;
                     if constexpr (W == 1)
                         res = claim_bucket(reinterpret_cast<unsigned long long*>(keys), cnt, mask / BUCKET, K[u],
-                                           (uint32_t)(h >> 32) & (mask / BUCKET), nsl[u]);
+                                           (uint32_t)(h >> 32) & mask, nsl[u]);
                     else
                         res = claim_cas(reinterpret_cast<U128*>(keys), cnt, mask, K[u], (uint32_t)(h >> 32) & mask,
                                         nsl[u]);
@@ -574,13 +615,14 @@ __global__ void __maxnreg__(56) k_count(CountParams P) {
             for (uint32_t i = tid; i < nl; i += COUNT_THREADS) {
                 const uint32_t sl = list[i];
                 const unsigned long long oi = ob + i;
+                const uint32_t c = cnt[sl];
                 if (oi < P.out_cap) {
                     O::store(P.out_keys, oi, keys[sl]);
-                    P.out_counts[oi] = cnt[sl];
+                    P.out_counts[oi] = c + 1;
                     if (P.out_sample) P.out_sample[oi] = g.sample;
                 }
                 keys[sl] = O::empty();
-                cnt[sl] = 0;
+                if (c) cnt[sl] = 0;
             }
             if (tid == 0) distinct += nl;
         } else {
@@ -595,7 +637,7 @@ __global__ void __maxnreg__(56) k_count(CountParams P) {
                 nocc += occ ? 1u : 0u;
                 bool keep = occ;
                 if (filtered && occ) {
-                    const uint32_t c = cnt[sl];
+                    const uint32_t c = cnt[sl] + 1;
                     keep = (uint64_t)c >= P.ci && (uint64_t)c <= P.cx;
                 }
                 keepm |= (keep ? 1u : 0u) << j;
@@ -628,7 +670,7 @@ __global__ void __maxnreg__(56) k_count(CountParams P) {
                     const unsigned long long i = o + __popc(bal & ((1u << lane) - 1));
                     if (i < P.out_cap) {
                         O::store(P.out_keys, i, keys[sl]);
-                        P.out_counts[i] = cnt[sl];
+                        P.out_counts[i] = cnt[sl] + 1;
                         if (P.out_sample) P.out_sample[i] = g.sample;
                     }
                 }
@@ -817,6 +859,7 @@ struct P2Regions {
     unsigned long long* aux;  // [0..1] retry counters, [2..3] list sizes of a retry pass
     unsigned long long* work; // [0..15] group counters of the first pass's launches, [16] of a retry pass
     unsigned long long* kofs;
+    uint32_t* gfirst;
     unsigned long long* sums;
     Segment* segs;
     Slice* slices;
@@ -834,6 +877,7 @@ P2Regions carve(Carve& c, const P2Input& in, const P2Plan& L) {
     R.aux = c.take<unsigned long long>(4);
     R.work = c.take<unsigned long long>(17);
     R.kofs = c.take<unsigned long long>(NBIN_ALL + 1);
+    R.gfirst = c.take<uint32_t>(NBIN_ALL);
     R.sums = c.take<unsigned long long>(L.nsum);
     R.segs = c.take<Segment>(in.n_segs + 1);
     R.slices = c.take<Slice>(L.n_slices + 1);
@@ -955,6 +999,7 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
     K.desc = in.desc;
     K.slices = R.slices;
     K.kofs = R.kofs;
+    K.gfirst = R.gfirst;
     K.segs = R.segs;
     K.n_segs = in.n_segs;
     K.target = std::max<uint32_t>(1, slots * in.group_pct / 100);  // as in make_plan
