@@ -7,7 +7,7 @@ GC 41%, 45% of the sequence from 300 bp / 6 kbp repeat families at 10-20%
 divergence, 3% microsatellites — the largest single-GPU workload of the
 benchmark set. Inputs (3.1 GB) are larger than L2, so no flush is needed.
 
-  value   Gbases/s with the input already resident in HBM: k_pack -> k_cut_seq
+  value   Gbases/s with the input already resident in HBM: k_pack -> k_cut_fixed/k_cut_seq
           -> k_scan -> k_plan -> k_keys -> k_count, results left on the device
           (stats also give distinct k-mers/s and k-mer updates/s)
   e2e     the same through the public C ABI from the FASTA file's bytes
@@ -61,10 +61,12 @@ def parse_args():
     ap.add_argument("--no-small", action="store_true", help="skip the small read-set section")
     ap.add_argument("--no-passes", action="store_true", help="skip the memory-budget (passes) section")
     ap.add_argument("--batch-samples", type=int, default=2000)
-    ap.add_argument("--batch-scales", default="0.004,0.02",
+    ap.add_argument("--batch-scales", default="0.004,0.02,0.05",
                     help="genome sizes of the batched mix: log-uniform 10 kbp - 50 Mbp times each of these")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="length of the arrival trace")
     ap.add_argument("--serve-scale", type=float, default=1.0, help="request sizes: median 20 Mbp times this")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="group size fixed at half the table (profiling: no trial launches in the warm-up step)")
     ap.add_argument("--no-parity-cpu", action="store_true",
                     help="skip the oracle port's digest of the full-size results (about 30 s of host work each)")
     ap.add_argument("--cpu-mbp", type=float, default=1200.0,
@@ -268,7 +270,10 @@ def _pinned_copy(a):
 
 def batched_vs_plain(ctx, n_samples: int, scale: float):
     """The 2,000-sample mix, counted sample by sample through tg_count_seq (the
-    plain path) and all at once through tg_count_batch; same pairs required."""
+    plain path) and all at once through tg_count_batch; same pairs required.
+    Samples go to tg_count_batch in calls of at most 8 Gbp, so that one call's
+    pairs fit a reused host buffer (one call up to the 0.02 scale); inside a
+    call the library counts runs of samples that fit the device."""
     import ctypes
     import tuna_gb300 as T
     from tuna_gb300 import synth
@@ -293,45 +298,71 @@ def batched_vs_plain(ctx, n_samples: int, scale: float):
     t0 = time.perf_counter()
     per_plain = [plain(i) for i in range(len(seqs))]
     t_plain = time.perf_counter() - t0
-    off = np.zeros(len(seqs) + 1, dtype=np.uint64)
-    ptrs = (ctypes.c_void_p * len(seqs))(*[s.ctypes.data for s in seqs])
-    lens = (ctypes.c_size_t * len(seqs))(*[int(s.size) for s in seqs])
-    # the pairs' count, from a call with no room (TG_ERR_ARG with n_out set)
-    rc = L.tg_count_batch(ctx.h, ctypes.byref(o), len(seqs), ptrs, lens, None, None, None, 0,
-                          ctypes.byref(n_out), ctypes.byref(st))
-    cap = int(n_out.value) + 1024 if rc == 1 else bases
+    budget = 8_000_000_000  # bases per call
+    runs, cur, acc = [], [], 0
+    for i, sq in enumerate(seqs):
+        if cur and acc + sq.size > budget:
+            runs.append(cur)
+            cur, acc = [], 0
+        cur.append(i)
+        acc += int(sq.size)
+    runs.append(cur)
+    calls = []
+    for r in runs:
+        ptrs = (ctypes.c_void_p * len(r))(*[seqs[i].ctypes.data for i in r])
+        lens = (ctypes.c_size_t * len(r))(*[int(seqs[i].size) for i in r])
+        # the pairs' count, from a call with no room (TG_ERR_ARG with n_out set)
+        rc = L.tg_count_batch(ctx.h, ctypes.byref(o), len(r), ptrs, lens, None, None, None, 0,
+                              ctypes.byref(n_out), ctypes.byref(st))
+        cap_r = int(n_out.value) + 1024 if rc == 1 else int(sum(lens))
+        calls.append((r, ptrs, lens, cap_r, np.zeros(len(r) + 1, dtype=np.uint64)))
+    cap = max(c[3] for c in calls)
     kb, cb = host_array(cap, np.uint64), host_array(cap, np.uint32)
 
-    def batch():
-        rc = L.tg_count_batch(ctx.h, ctypes.byref(o), len(seqs), ptrs, lens, ctypes.c_void_p(kb.ctypes.data),
+    def run_call(c):
+        r, ptrs, lens, cap_r, off = c
+        rc = L.tg_count_batch(ctx.h, ctypes.byref(o), len(r), ptrs, lens, ctypes.c_void_p(kb.ctypes.data),
                               ctypes.c_void_p(cb.ctypes.data), ctypes.c_void_p(off.ctypes.data), cap,
                               ctypes.byref(n_out), ctypes.byref(st))
         ctx.check(rc)
 
+    def batch():
+        for c in calls:
+            run_call(c)
+
     batch()  # warm
+    per_batch = [0] * len(seqs)
+    for r, _, _, _, off in calls:
+        for j, i in enumerate(r):
+            per_batch[i] = int(off[j + 1] - off[j])
     ts = []
     for _ in range(3):
         t0 = time.perf_counter()
         batch()
         ts.append(time.perf_counter() - t0)
     t_batch = statistics.median(ts)
-    per_batch = np.diff(off.astype(np.int64)).tolist()
     same_sizes = per_batch == per_plain
     # bit-exact against the oracle on 12 samples across the size range: the
-    # digest of the sample's range of the batch equals the oracle's digest of
-    # that sample counted alone (and the plain path's, on the same samples)
+    # digest of the sample's range of its batch call equals the oracle's digest
+    # of that sample counted alone (and the plain path's, on the same samples)
     from oracle import oracle as O
     order = np.argsort([s.size for s in seqs])
     picks = sorted(set(int(order[int(q * (len(seqs) - 1))]) for q in np.linspace(0, 1, 12)))
     exact, checked = True, 0
-    for i in picks:
-        lo, hi = int(off[i]), int(off[i + 1])
-        got = O.digest_pairs(kb[lo:hi].reshape(-1, 1), cb[lo:hi], 31, threads=os.cpu_count() or 1)
-        want, _ = O.digest_stream(seqs[i], 31, 21, 16, threads=os.cpu_count() or 1)
-        n = plain(i)
-        alone = O.digest_pairs(k1[:n].reshape(-1, 1), c1[:n], 31)
-        exact &= got == want == alone
-        checked += 1
+    for c in calls:
+        mine = [(j, i) for j, i in enumerate(c[0]) if i in picks]
+        if not mine:
+            continue
+        run_call(c)  # this call's pairs back in kb/cb
+        off = c[4]
+        for j, i in mine:
+            lo, hi = int(off[j]), int(off[j + 1])
+            got = O.digest_pairs(kb[lo:hi].reshape(-1, 1), cb[lo:hi], 31, threads=os.cpu_count() or 1)
+            want, _ = O.digest_stream(seqs[i], 31, 21, 16, threads=os.cpu_count() or 1)
+            n = plain(i)
+            alone = O.digest_pairs(k1[:n].reshape(-1, 1), c1[:n], 31)
+            exact &= got == want == alone
+            checked += 1
     release(k1, c1, kb, cb, *seqs)
     return {"workload": f"{len(seqs)} samples, genome sizes log-uniform 10 kbp - 50 Mbp scaled by {scale:g} "
                         f"(so {max(1000, 10_000 * scale) / 1e3:g} kbp floor - {50e6 * scale / 1e3:g} kbp), "
@@ -339,7 +370,9 @@ def batched_vs_plain(ctx, n_samples: int, scale: float):
             "samples": len(seqs), "bases": bases,
             "plain_gbases_s": bases / t_plain / 1e9, "batched_gbases_s": bases / t_batch / 1e9,
             "speedup": t_plain / t_batch, "plain_s": t_plain, "batched_s": t_batch,
-            "api": "tg_count_seq per sample vs tg_count_batch, pinned host buffers, results in host memory",
+            "batch_calls": len(calls), "max_call_bases": budget,
+            "api": "tg_count_seq per sample vs tg_count_batch (calls of at most 8 Gbp), "
+                   "pinned host buffers, results in host memory",
             "same_pairs_per_sample": bool(same_sizes), "oracle_checked_samples": checked,
             "bit_exact_checked_samples": bool(exact)}
 
@@ -580,14 +613,17 @@ def gz_input(fasta: np.ndarray, mbytes: float = 300.0):
     return res
 
 
-def served(seconds: float, scale: float, pool_size: int = 48):
+def served(seconds: float, scale: float, pool_size: int = 48, burst_rate: float = 400.0,
+           burst_seconds: float = 4.0):
     """Poisson arrivals at 50 requests/s replayed in real time against the
     continuous-batching server; latency from arrival to result in host memory.
     Request sizes follow the configured distribution (log-normal, median 20 Mbp
     x scale, sigma 1.5, cap 2 Gbp x scale); the replay reuses a pool of
     `pool_size` generated requests (one third per k), the i-th arrival taking
     the next pooled request of its k. Answers are dropped as they arrive, so the
-    server's result slabs are recycled."""
+    server's result slabs are recycled. Then a burst: `burst_rate` requests/s
+    for `burst_seconds` (more bases than the device counts in that time), which
+    queues requests while batches run, so that they merge."""
     import threading
     from tuna_gb300 import synth
     from tuna_gb300.serve import Server
@@ -597,28 +633,29 @@ def served(seconds: float, scale: float, pool_size: int = 48):
         lst = by_k.setdefault(r.k, [])
         if len(lst) < max(1, pool_size // 3):
             lst.append((r, _pinned_copy(synth.fastq_sequence_stream(synth.request_fastq(r, i)))))
-    nxt = {k: 0 for k in by_k}
-    replay = []
-    for r in plan:
-        lst = by_k.get(r.k) or next(iter(by_k.values()))
-        pr, seq = lst[nxt.get(r.k, 0) % len(lst)]
-        nxt[r.k] = nxt.get(r.k, 0) + 1
-        replay.append((r.arrival_s, pr.k, pr.m, seq))
-    lat, batch_of, done_t = [], [], []
-    mu = threading.Lock()
-    left = threading.Semaphore(0)
 
-    def record(f):
-        a = f.result()
-        with mu:
-            lat.append(a.latency_s * 1e3)
-            batch_of.append(a.batch)
-            done_t.append(a.done)
-        left.release()
+    def replay_of(p):
+        nxt = {k: 0 for k in by_k}
+        out = []
+        for r in p:
+            lst = by_k.get(r.k) or next(iter(by_k.values()))
+            pr, seq = lst[nxt.get(r.k, 0) % len(lst)]
+            nxt[r.k] = nxt.get(r.k, 0) + 1
+            out.append((r.arrival_s, pr.k, pr.m, seq))
+        return out
 
-    with Server(0, workers=2) as srv:
-        for f in [srv.submit(replay[0][3], replay[0][1], replay[0][2]) for _ in range(2)]:  # warm both workers
-            f.result()
+    def run(srv, replay, length_s):
+        lat, done_t = [], []
+        mu = threading.Lock()
+        left = threading.Semaphore(0)
+
+        def record(f):
+            a = f.result()
+            with mu:
+                lat.append(a.latency_s * 1e3)
+                done_t.append(a.done)
+            left.release()
+
         srv.batches = 0
         srv.batch_sizes.clear()
         bases = 0
@@ -633,20 +670,33 @@ def served(seconds: float, scale: float, pool_size: int = 48):
             left.acquire()
         t_end = max(done_t)
         sizes = list(srv.batch_sizes)
-    lat_a = np.array(lat)
-    hist = {}
-    for n in sizes:
-        hist[str(n)] = hist.get(str(n), 0) + 1
-    return {"workload": f"Poisson 50 req/s for {seconds:g} s, sizes log-normal median {20 * scale:g} Mbp "
-                        f"(sigma 1.5, cap {2000 * scale:g} Mbp), reads 100-250 bp at 0.5% error, "
-                        f"k in {{21, 25, 31}}; {sum(len(v) for v in by_k.values())} generated requests replayed",
-            "requests": len(replay), "bases": bases, "p50_ms": float(np.percentile(lat_a, 50)),
-            "p99_ms": float(np.percentile(lat_a, 99)), "max_ms": float(lat_a.max()),
-            "offered_gbases_s": bases / max(seconds, 1e-9) / 1e9,
-            "gbases_s": bases / (t_end - t0) / 1e9, "batches": len(sizes),
-            "requests_per_batch_mean": float(np.mean(sizes)) if sizes else 0.0,
-            "requests_per_batch_hist": hist, "workers": 2,
-            "api": "tuna_gb300.serve.Server over tg_count_batch, results in page-locked host memory"}
+        lat_a = np.array(lat)
+        hist = {}
+        for n in sizes:
+            hist[str(n)] = hist.get(str(n), 0) + 1
+        return {"requests": len(replay), "bases": bases, "p50_ms": float(np.percentile(lat_a, 50)),
+                "p99_ms": float(np.percentile(lat_a, 99)), "max_ms": float(lat_a.max()),
+                "offered_gbases_s": bases / max(length_s, 1e-9) / 1e9,
+                "gbases_s": bases / (t_end - t0) / 1e9, "batches": len(sizes),
+                "requests_per_batch_mean": float(np.mean(sizes)) if sizes else 0.0,
+                "requests_per_batch_hist": dict(sorted(hist.items(), key=lambda kv: int(kv[0])))}
+
+    with Server(0, workers=2) as srv:
+        for f in [srv.submit(by_k[k][0][1], k, by_k[k][0][0].m) for k in by_k for _ in range(2)]:
+            f.result()  # warm both workers
+        res = run(srv, replay_of(plan), seconds)
+        burst = run(srv, replay_of(synth.served_plan(burst_rate, burst_seconds, seed=29, scale=scale)),
+                    burst_seconds)
+    n_pool = sum(len(v) for v in by_k.values())
+    res = {"workload": f"Poisson 50 req/s for {seconds:g} s, sizes log-normal median {20 * scale:g} Mbp "
+                       f"(sigma 1.5, cap {2000 * scale:g} Mbp), reads 100-250 bp at 0.5% error, "
+                       f"k in {{21, 25, 31}}; {n_pool} generated requests replayed", **res}
+    burst["workload"] = (f"Poisson {burst_rate:g} req/s for {burst_seconds:g} s, the same sizes and pool "
+                         f"(more bases than the device counts in that time: requests queue and merge)")
+    res["burst"] = burst
+    res["workers"] = 2
+    res["api"] = "tuna_gb300.serve.Server over the job API (several samples per job), results in page-locked host memory"
+    return res
 
 
 # ------------------------------------------------------------------ reference arm
@@ -706,6 +756,7 @@ def main():
     if args.impl == "reference":
         run_reference(args, rank)
         return
+    t_start = time.perf_counter()
     import numpy as np
     import torch
     import tuna_gb300 as T
@@ -722,7 +773,7 @@ def main():
 
     stream_h, bases, lens, fasta_h = workload(args.scale, want_fasta=True)
     dev = torch.from_numpy(stream_h).to(f"cuda:{local}")
-    ctx = T.Context(local, autotune=True)  # the first warm-up step times the group sizes
+    ctx = T.Context(local, autotune=not args.no_autotune)  # the first warm-up step times the group sizes
     ext = torch.cuda.ExternalStream(ctx.stream_ptr, device=f"cuda:{local}")
     torch.cuda.synchronize()
 
@@ -792,18 +843,20 @@ def main():
     }
     dom = max(("cut", "keys", "count", "pack"), key=lambda x: avg[x])
     achieved = alg[dom] / (avg[dom] / 1e3) / 1e9
-    kernel_names = {"cut": "k_cut_seq", "keys": "k_scan+k_plan+k_keys", "count": "k_count", "pack": "k_pack"}
+    cut_name = "k_cut_fixed" if (K, M) in ((31, 21), (31, 23), (21, 17), (25, 21)) else "k_cut_seq"
+    kernel_names = {"cut": cut_name, "keys": "k_scan+k_plan+k_keys", "count": "k_count", "pack": "k_pack"}
     # phase 1 against the reference's algorithmic bytes B1 = N/4 + record bytes (~1.82 B/base)
     ref_record_bytes = 2 * recs + (st["kmers"] + recs * (K - 1)) / 4
     b1 = bases / 4 + ref_record_bytes
     p1_gbs = b1 / (avg["phase1"] / 1e3) / 1e9
-    traffic = None
+    traffic, traffic_source = None, None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
             tj = json.load(f)
         if dom in tj:
             traffic = tj[dom].get("bytes_per_launch_full_size")
+            traffic_source = tj[dom].get("source")
 
     # ---- end to end through the C ABI: pinned host input -> counts in pinned host memory
     e2e = None
@@ -881,34 +934,44 @@ def main():
             parity_full["ok"] = parity_full["ok"] and parity_full["e2e_digests_same"]
         release(h_fa, h_keys, h_cnt)
 
+    section_s = {"main": time.perf_counter() - t_start}
+
+    def section(name, fn, *a, **kw):
+        t = time.perf_counter()
+        r = fn(*a, **kw)
+        section_s[name] = time.perf_counter() - t
+        return r
+
     small = None
     if rank == 0 and not args.no_small:
-        small = small_reads(ctx, args.steps)
+        small = section("small_reads", small_reads, ctx, args.steps)
     gz = None
     if rank == 0 and not args.no_gz and fasta_h is not None:
-        gz = gz_input(fasta_h)
+        gz = section("gz", gz_input, fasta_h)
     output = None
     if rank == 0 and not args.no_output:
-        output = output_drain(ctx, dev, n_stream)
+        output = section("output", output_drain, ctx, dev, n_stream)
     passes = None
     if rank == 0 and not args.no_passes:
-        passes = passes_section(dev, n_stream, int(st["kmers"]), 2)
+        passes = section("passes", passes_section, dev, n_stream, int(st["kmers"]), 2)
     del dev
     large = None
     if rank == 0 and not args.no_large_k:
-        large = large_k(ctx, args.large_k_scale, max(1, min(args.steps, 3)), parity_cpu=not args.no_parity_cpu)
+        large = section("large_k", large_k, ctx, args.large_k_scale, max(1, min(args.steps, 3)),
+                        parity_cpu=not args.no_parity_cpu)
 
     batched = None
     if rank == 0 and not args.no_batch:
-        batched = {f"scale_{sc}": batched_vs_plain(ctx, args.batch_samples, float(sc))
+        batched = {f"scale_{sc}": section(f"batched_{sc}", batched_vs_plain, ctx, args.batch_samples, float(sc))
                    for sc in args.batch_scales.split(",") if sc}
     serve = None
     if rank == 0 and not args.no_serve:
-        serve = served(args.serve_seconds, args.serve_scale)
+        serve = section("serve", served, args.serve_seconds, args.serve_scale)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        cpu = time_cpu(os.cpu_count() or 1, cpu_sample(stream_h, args.cpu_mbp, os.cpu_count() or 1))
+        cpu = section("cpu_baseline", lambda: time_cpu(os.cpu_count() or 1,
+                                                       cpu_sample(stream_h, args.cpu_mbp, os.cpu_count() or 1)))
 
     if rank == 0:
         line = {
@@ -919,8 +982,8 @@ def main():
                     "stands in for the reference's genome assemblies",
             "config": main_config(bases, n_stream, world),
             "gpu_config": {"gpu_parts": int(st["gpu_parts"]), "group_load_pct": int(st["group_load_pct"]),
-                           "autotune": "TG_CTX_AUTOTUNE: group size timed on the first warm-up step "
-                                       "(35/50/65 % of the table)"},
+                           "autotune": "off (--no-autotune): half the table" if args.no_autotune else
+                           "TG_CTX_AUTOTUNE: group size timed on the first warm-up step (35/50/65 % of the table)"},
             "stats": {"kmers": int(st["kmers"]), "superkmers": int(st["superkmers"]),
                       "distinct": int(st["distinct"]), "fallback_groups": int(st["fallback_groups"]),
                       "distinct_kmers_per_s": int(st["distinct"]) / (ms / 1e3),
@@ -930,7 +993,7 @@ def main():
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                          else "fallback 6.8 TB/s",
-                         "algorithmic_bytes": alg[dom], "traffic": traffic,
+                         "algorithmic_bytes": alg[dom], "traffic": traffic, "traffic_source": traffic_source,
                          "phase1_b1_gbs": p1_gbs, "phase1_b1_frac": p1_gbs / peak},
             "cpu_baseline": cpu,
             "e2e": e2e,
@@ -941,6 +1004,7 @@ def main():
             "passes": passes,
             "large_k": large,
             "batched": batched,
+            "section_seconds": {k2: round(v2, 1) for k2, v2 in section_s.items()},
             "serve": serve,
             "gpu_launches": launches,
             "clocks": clk,

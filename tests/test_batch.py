@@ -141,3 +141,76 @@ def test_count_batch_fastx_matches_alone():
             want = ctx.run(31, 21, fastx=f)[0].sorted()
             got = T.Result(keys[a:b].reshape(-1, 1).copy(), cnt[a:b].copy(), {}, 31).sorted()
             assert np.array_equal(got.keys, want.keys) and np.array_equal(got.counts, want.counts)
+
+
+def _count_batch(ctx, smp, k, m, cap, fastx=False):
+    import tuna_gb300 as T
+    L = T.library()
+    ptrs = (ctypes.c_void_p * len(smp))(*[s.ctypes.data if s.size else None for s in smp])
+    lens = (ctypes.c_size_t * len(smp))(*[int(s.size) for s in smp])
+    W = 1 if k <= 31 else 2
+    keys = np.zeros(max(1, cap) * W, dtype=np.uint64)
+    cnt = np.zeros(max(1, cap), dtype=np.uint32)
+    off = np.zeros(len(smp) + 1, dtype=np.uint64)
+    o = T._JobOpts(k, m, 16, 1, (1 << 64) - 1, 0, 0)
+    n = ctypes.c_uint64()
+    st = T._Stats()
+    fn = L.tg_count_batch_fastx if fastx else L.tg_count_batch
+    rc = fn(ctx.h, ctypes.byref(o), len(smp), ptrs, lens, keys.ctypes.data if cap else None,
+            cnt.ctypes.data if cap else None, off.ctypes.data, cap, ctypes.byref(n), ctypes.byref(st))
+    return rc, int(n.value), keys.reshape(-1, W), cnt, off, st
+
+
+@pytest.mark.parametrize("k,m", [(31, 21), (63, 21)])
+def test_count_batch_in_runs_of_samples(k, m):
+    """A batch larger than the context's device budget runs as consecutive runs
+    of samples, each run's result copy overlapping the next run's counting
+    (and samples larger than a run alone, counted in passes): every sample's
+    range equals its pairs alone, the offsets are consecutive, a call with no
+    room reports the total, and a short buffer gets the samples that fit."""
+    import tuna_gb300 as T
+    smp = _samples(24, 11)
+    total = sum(int(s.size) for s in smp)
+    with T.Context(0) as ref, T.Context(0, hbm_budget=40 << 20) as ctx:
+        want = [ref.run(k, m, seq=s)[0] for s in smp]
+        n_all = sum(len(w) for w in want)
+        assert total > (40 << 20) // 40 * 4  # several runs
+        rc, n, keys, cnt, off, st = _count_batch(ctx, smp, k, m, 0)
+        assert rc == 1 and n == n_all  # TG_ERR_ARG: no room, the count reported
+        rc, n, keys, cnt, off, st = _count_batch(ctx, smp, k, m, n_all)
+        assert rc == 0, T.library().tg_last_error(ctx.h)
+        assert n == n_all and int(off[0]) == 0 and int(off[-1]) == n_all
+        assert st.kmers == sum(int(w.stats["kmers"]) for w in want)
+        for i, w in enumerate(want):
+            a, b = int(off[i]), int(off[i + 1])
+            got = T.Result(keys[a:b].copy(), cnt[a:b].copy(), {}, k)
+            assert _same(got, w), f"sample {i}"
+        # a buffer for half the pairs: the samples that end within it are complete
+        # (the order of a sample's pairs is not fixed from one call to the next)
+        half = n_all // 2
+        rc, n, keys2, cnt2, off2, _ = _count_batch(ctx, smp, k, m, half)
+        assert rc == 1 and n == n_all and np.array_equal(off2, off)
+        full = [i for i in range(len(smp)) if int(off2[i + 1]) <= half]
+        assert len(full) >= 2
+        for i in full:
+            a, b = int(off2[i]), int(off2[i + 1])
+            assert _same(T.Result(keys2[a:b].copy(), cnt2[a:b].copy(), {}, k), want[i]), f"sample {i}"
+
+
+def test_count_batch_fastx_in_runs():
+    """tg_count_batch_fastx under a small device budget: runs of files."""
+    import tuna_gb300 as T
+    from tuna_gb300 import synth
+    files = []
+    for i in range(10):
+        g = synth.genome(40_000 + 20_000 * i, 500 + i, 0.45)
+        files.append(synth.reads_fastq(g, 2_000 + 300 * i, (100, 250), 0.005, 0.001, 90 + i) if i % 2
+                     else synth.fasta(g, [g.size // 3, g.size - g.size // 3]))
+    with T.Context(0) as ref, T.Context(0, hbm_budget=16 << 20) as ctx:
+        want = [ref.run(31, 21, fastx=f)[0] for f in files]
+        n_all = sum(len(w) for w in want)
+        rc, n, keys, cnt, off, _ = _count_batch(ctx, files, 31, 21, n_all, fastx=True)
+        assert rc == 0 and n == n_all
+        for i, w in enumerate(want):
+            a, b = int(off[i]), int(off[i + 1])
+            assert _same(T.Result(keys[a:b].copy(), cnt[a:b].copy(), {}, 31), w), f"file {i}"

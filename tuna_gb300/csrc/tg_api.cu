@@ -155,6 +155,10 @@ struct tg_ctx {
     unsigned long long* wave_out = nullptr;  // mapped pinned host, OVERLAP_WORDS entries
     unsigned long long* wave_out_dev = nullptr;
     cudaEvent_t wave_ev[16] = {};
+    // a batch in runs of samples (count_host): the last run's result copy on
+    // st_copy, which the next run's sample-major scatter waits for
+    cudaEvent_t ev_copied = nullptr;
+    bool copy_pending = false;
     tg_job* active = nullptr;
     int prepared_m = -1;
 
@@ -173,7 +177,12 @@ struct tg_ctx {
     }
     cudaError_t ensure(DevBuf& b, size_t bytes) {
         if (bytes <= b.cap && b.p) return cudaSuccess;
-        if (b.p) { cudaFree(b.p); b.p = nullptr; b.cap = 0; }
+        if (b.p) {
+            if (st_copy) cudaStreamSynchronize(st_copy);  // a result copy may still read it
+            cudaFree(b.p);
+            b.p = nullptr;
+            b.cap = 0;
+        }
         const size_t want = std::max<size_t>(bytes, 256);
         cudaError_t e = cudaMalloc(&b.p, want);
         if (e != cudaSuccess) { b.p = nullptr; (void)cudaGetLastError(); return e; }
@@ -228,6 +237,8 @@ struct tg_job {
     tg_stats st{};
     // optional: output ranges handed out as phase 2 finishes them
     const P2Overlap* overlap = nullptr;
+    // several samples: the sample-major copy waits for this event (count_host)
+    cudaEvent_t reorder_after = nullptr;
     // samples: sample i starts at stream position sample_start[i]
     std::vector<unsigned long long> sample_start{0};
     int lex_launches = 0;  // lexer kernels of the feeds
@@ -329,6 +340,7 @@ static tg_status tg_ctx_create_impl(const tg_ctx_opts* opts, tg_ctx** out) {
         e = cudaHostAlloc(&ctx->wave_out, OVERLAP_WORDS * sizeof(unsigned long long), cudaHostAllocMapped);
     if (e == cudaSuccess) e = cudaHostGetDevicePointer(reinterpret_cast<void**>(&ctx->wave_out_dev), ctx->wave_out, 0);
     for (int i = 0; i < 16 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&ctx->wave_ev[i], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_copied, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         tg_ctx_destroy(ctx);  // whatever was created so far
         (void)cudaGetLastError();
@@ -346,20 +358,19 @@ tg_status tg_ctx_destroy(tg_ctx* ctx) {
     if (!ctx) return TG_ERR_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->st) cudaStreamSynchronize(ctx->st);
+    if (ctx->st_copy) cudaStreamSynchronize(ctx->st_copy);
     DevBuf* bufs[] = {&ctx->seq, &ctx->packed, &ctx->valid, &ctx->desc, &ctx->xdesc, &ctx->hist,
                       &ctx->scratch,
                       &ctx->okeys, &ctx->ocnt, &ctx->osamp, &ctx->samp, &ctx->okeys2, &ctx->ocnt2, &ctx->osoff, &ctx->misc, &ctx->fbtab, &ctx->tables,
-                      &ctx->raw, &ctx->lexs, &ctx->fbuf, &ctx->fscr};
+                      &ctx->raw, &ctx->lexs, &ctx->fbuf, &ctx->fscr, &ctx->sp_desc, &ctx->sp_bytes, &ctx->sp_aux};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
     for (auto& e : ctx->ev)
         if (e) cudaEventDestroy(e);
     for (auto& e : ctx->wave_ev)
         if (e) cudaEventDestroy(e);
-    if (ctx->st_copy) {
-        cudaStreamSynchronize(ctx->st_copy);
-        cudaStreamDestroy(ctx->st_copy);
-    }
+    if (ctx->ev_copied) cudaEventDestroy(ctx->ev_copied);
+    if (ctx->st_copy) cudaStreamDestroy(ctx->st_copy);
     if (ctx->wave_out) cudaFreeHost(ctx->wave_out);
     for (uint8_t* h : ctx->fhost) tgh::pinned_free(h);
     for (uint8_t* h : ctx->stage) tgh::pinned_free(h);
@@ -1012,6 +1023,7 @@ static tg_status tg_job_run_impl(tg_job* j) {
             out.keys2 = ctx->okeys2.p;
             out.counts2 = ctx->ocnt2.as<uint32_t>();
             out.sample_off = ctx->osoff.as<unsigned long long>();
+            out.reorder_after = j->reorder_after;
         }
         out.cap = out_cap;
         // group size: the context's tuned one, else half the table; with
@@ -1758,30 +1770,40 @@ tg_status tg_job_end(tg_job* j) {
     return TG_OK;
 }
 
-// The one-call entry points: feed, run with the counting pass in waves whose
-// pairs are copied to the caller's buffers (on the copy stream) while the
-// next waves count, wait for the copies.
-static tg_status count_host(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_samples, const uint8_t* const* seqs,
-                            const size_t* lens, uint64_t* keys, uint32_t* counts, uint64_t* sample_off, uint64_t cap,
-                            uint64_t* n_out, tg_stats* stats, bool fastx = false) {
-    if (!ctx || !opts || !n_out || (n_samples && (!seqs || !lens))) return TG_ERR_ARG;
-    *n_out = 0;
-    if (n_samples > TG_MAX_SAMPLES) return ctx->fail(TG_ERR_ARG, "too many samples in one job");
+// One job of a one-call entry point over samples [a, b) (all of tg_count_seq /
+// tg_count_fastx; a run of the samples of tg_count_batch*): feed, run, results
+// to keys/counts from pair `base` on (at most `cap` pairs in all), the samples'
+// offsets to sample_off[a..b] (absolute). One sample: the counting pass in waves
+// whose pairs are copied to the caller's buffers (on the copy stream) while the
+// next waves count, the copies waited for. Several samples: the pairs are
+// reordered sample-major at the end and copied then; with `pipelined` that copy
+// is left running on the copy stream (ctx->ev_copied), and the next job's
+// sample-major scatter waits for it, so the copy overlaps the next job's
+// phases 1 and 2.
+static tg_status count_run(tg_ctx* ctx, const tg_job_opts* opts, uint32_t a, uint32_t b, const uint8_t* const* seqs,
+                           const size_t* lens, uint64_t* keys, uint32_t* counts, uint64_t* sample_off, uint64_t base,
+                           uint64_t cap, bool fastx, bool pipelined, uint64_t& n_run, tg_stats& st_run) {
+    n_run = 0;
     tg_job* j = nullptr;
     tg_status s = tg_job_begin(ctx, opts, &j);
     if (s != TG_OK) return s;
     const JobEnd end_job{j};
+    const uint32_t n = b - a;
+    const uint64_t room = cap > base ? cap - base : 0;
+    const int W = j->W;
+    uint64_t* kdst = keys ? keys + base * W : nullptr;
+    uint32_t* cdst = counts ? counts + base : nullptr;
     // one buffer, separators everywhere, then every sample copied to its place
     uint64_t total = 0;
-    for (uint32_t i = 0; i < n_samples; ++i) {
+    for (uint32_t i = a; i < b; ++i) {
         if (!seqs[i] && lens[i]) s = TG_ERR_ARG;
         total += lens[i] + 1;
     }
     if (s == TG_OK && fastx) {
         // each sample's FASTA/FASTQ bytes lexed on the device into its own sample
         // (an empty sample stays empty)
-        for (uint32_t i = 0; i < n_samples && s == TG_OK; ++i) {
-            if (i > 0) s = tg_job_next_sample(j);
+        for (uint32_t i = a; i < b && s == TG_OK; ++i) {
+            if (i > a) s = tg_job_next_sample(j);
             if (s == TG_OK && lens[i]) s = lex_append_host(j, seqs[i], lens[i]);
         }
     } else if (s == TG_OK && total) {
@@ -1790,8 +1812,8 @@ static tg_status count_host(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_sam
         if (e == cudaSuccess) e = ctx->ensure(ctx->seq, total + 1);
         if (e == cudaSuccess) e = cudaMemsetAsync(ctx->seq.p, '\n', total, ctx->st);
         uint64_t off = 0;
-        for (uint32_t i = 0; i < n_samples && e == cudaSuccess; ++i) {
-            if (i > 0) j->sample_start.push_back(off);
+        for (uint32_t i = a; i < b && e == cudaSuccess; ++i) {
+            if (i > a) j->sample_start.push_back(off);
             if (lens[i])
                 e = link_copy(ctx->seq.as<uint8_t>() + off, seqs[i], lens[i], cudaMemcpyHostToDevice, ctx->st, ctx->n_sm);
             off += lens[i] + 1;
@@ -1809,46 +1831,165 @@ static tg_status count_host(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_sam
     ov.wave_out_dev = ctx->wave_out_dev;
     ov.wave_ev = ctx->wave_ev;
     double d2h_issue_ms = 0;
-    const int W = j->W;
-    const bool multi = n_samples > 1;
+    const bool multi = n > 1;
     ov.on_range = [&](uint64_t lo, uint64_t hi) -> tg_status {
-        const uint64_t h = std::min<uint64_t>(hi, cap);
+        const uint64_t h = std::min<uint64_t>(hi, room);
         if (h <= lo) return TG_OK;
         const double t0 = now_ms();
-        if (keys)
-            CK(link_copy(keys + lo * W, ctx->okeys.as<uint8_t>() + lo * key_bytes(W), (h - lo) * key_bytes(W),
+        if (kdst)
+            CK(link_copy(kdst + lo * W, ctx->okeys.as<uint8_t>() + lo * key_bytes(W), (h - lo) * key_bytes(W),
                          cudaMemcpyDeviceToHost, ctx->st_copy, ctx->n_sm), "d2h keys");
-        if (counts)
-            CK(link_copy(counts + lo, ctx->ocnt.as<uint32_t>() + lo, (h - lo) * 4, cudaMemcpyDeviceToHost,
+        if (cdst)
+            CK(link_copy(cdst + lo, ctx->ocnt.as<uint32_t>() + lo, (h - lo) * 4, cudaMemcpyDeviceToHost,
                          ctx->st_copy, ctx->n_sm), "d2h counts");
         d2h_issue_ms += now_ms() - t0;
         return TG_OK;
     };
-    // several samples: the pairs are reordered sample-major at the end, so they
-    // are copied once the run is over
     j->overlap = multi ? nullptr : &ov;
+    j->reorder_after = multi && ctx->copy_pending ? ctx->ev_copied : nullptr;
     // a run in passes (memory budget) copies each pass's pairs here itself
-    j->sink_keys = keys;
-    j->sink_counts = counts;
-    j->sink_cap = cap;
+    j->sink_keys = kdst;
+    j->sink_counts = cdst;
+    j->sink_cap = room;
     if (s == TG_OK) s = tg_job_run(j);
     if (s == TG_OK && multi) {
-        const uint64_t h = std::min<uint64_t>(j->n_out, cap);
+        const uint64_t h = std::min<uint64_t>(j->n_out, room);
         const double t0 = now_ms();
-        if (h) s = tg_job_result_copy(j, keys, counts, 0, h);
-        if (s == TG_OK && sample_off) s = tg_job_sample_offsets(j, sample_off);
+        if (h && (kdst || cdst)) {
+            if (pipelined && !j->spilled) {
+                // the run left the sample-major pairs in okeys2/ocnt2 and its stream idle
+                if (kdst)
+                    CK(link_copy(kdst, ctx->okeys2.as<uint8_t>(), h * key_bytes(W), cudaMemcpyDeviceToHost,
+                                 ctx->st_copy, ctx->n_sm), "d2h keys");
+                if (cdst)
+                    CK(link_copy(cdst, ctx->ocnt2.as<uint32_t>(), h * 4, cudaMemcpyDeviceToHost, ctx->st_copy,
+                                 ctx->n_sm), "d2h counts");
+                CK(cudaEventRecord(ctx->ev_copied, ctx->st_copy), "event");
+                ctx->copy_pending = true;
+            } else {
+                s = tg_job_result_copy(j, kdst, cdst, 0, h);
+            }
+        }
+        if (s == TG_OK && sample_off) {
+            std::vector<uint64_t> off(n + 1);
+            s = tg_job_sample_offsets(j, off.data());
+            for (uint32_t i = 0; i <= n && s == TG_OK; ++i) sample_off[a + i] = base + off[i];
+        }
         d2h_issue_ms += now_ms() - t0;
     }
-    const double t_wait = now_ms();
-    const cudaError_t ce = cudaStreamSynchronize(ctx->st_copy);
-    j->st.d2h_ms += d2h_issue_ms + (now_ms() - t_wait);
-    if (s == TG_OK && ce != cudaSuccess) s = ctx->cuda_fail(ce, "d2h");
-    if (s == TG_OK) {
-        *n_out = j->n_out;
-        if (j->n_out > cap) s = ctx->fail(TG_ERR_ARG, "result buffer too small");
-        else if (sample_off && !multi) { sample_off[0] = 0; sample_off[1] = j->n_out; }
+    if (!pipelined || !multi) {
+        const double t_wait = now_ms();
+        const cudaError_t ce = cudaStreamSynchronize(ctx->st_copy);
+        j->st.d2h_ms += now_ms() - t_wait;
+        if (s == TG_OK && ce != cudaSuccess) s = ctx->cuda_fail(ce, "d2h");
+        ctx->copy_pending = false;
     }
-    if (stats) *stats = j->st;
+    j->st.d2h_ms += d2h_issue_ms;
+    if (s == TG_OK) {
+        n_run = j->n_out;
+        if (sample_off && !multi) { sample_off[a] = base; sample_off[b] = base + j->n_out; }
+    }
+    st_run = j->st;
+    return s;
+}
+
+// Sums the counters and times of one run of a batch into the batch's stats.
+static void add_run_stats(tg_stats& t, const tg_stats& r) {
+    t.input_bytes += r.input_bytes;
+    t.bases += r.bases;
+    t.runs += r.runs;
+    t.kmers += r.kmers;
+    t.superkmers += r.superkmers;
+    t.distinct += r.distinct;
+    t.out += r.out;
+    t.gpu_parts = r.gpu_parts;
+    t.heavy_groups += r.heavy_groups;
+    t.fallback_groups += r.fallback_groups;
+    t.h2d_ms += r.h2d_ms;
+    t.pack_ms += r.pack_ms;
+    t.phase1_ms += r.phase1_ms;
+    t.phase2_ms += r.phase2_ms;
+    t.d2h_ms += r.d2h_ms;
+    t.phase1_cut_ms += r.phase1_cut_ms;
+    t.phase1_scatter_ms += r.phase1_scatter_ms;
+    t.record_bytes += r.record_bytes;
+    t.gpu_launches += r.gpu_launches;
+    t.phase2_count_ms += r.phase2_count_ms;
+    t.phase2_keys_ms += r.phase2_keys_ms;
+    t.groups += r.groups;
+    t.lex_ms += r.lex_ms;
+    t.fastx_bytes += r.fastx_bytes;
+    t.host_parsed_bytes += r.host_parsed_bytes;
+    t.phase2_passes = std::max(t.phase2_passes, r.phase2_passes);
+    t.group_load_pct = r.group_load_pct;
+    t.autotune_trials += r.autotune_trials;
+}
+
+// A batch (several samples) larger than the device budget runs as
+// consecutive runs of samples of at most budget / BATCH_BYTES_PER_BASE input
+// bytes (a job of several samples is not counted in passes, so each run must
+// fit; a sample is never split), each run's result copy left running while the
+// next run counts. Cutting batches that fit into runs as well, only to overlap
+// the copies, was measured slower: the copy kernels cannot sit beside the cut
+// and key kernels on an SM (registers), so little overlapped, and smaller jobs
+// cost more (2,000 samples, 1.23 Gbp: 40 -> 73 ms in four runs).
+constexpr uint64_t BATCH_BYTES_PER_BASE = 40;  // keys, pairs and their sample-major copy, records, stream
+
+// The one-call entry points.
+static tg_status count_host(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_samples, const uint8_t* const* seqs,
+                            const size_t* lens, uint64_t* keys, uint32_t* counts, uint64_t* sample_off, uint64_t cap,
+                            uint64_t* n_out, tg_stats* stats, bool fastx = false) {
+    if (!ctx || !opts || !n_out || (n_samples && (!seqs || !lens))) return TG_ERR_ARG;
+    *n_out = 0;
+    if (n_samples > TG_MAX_SAMPLES) return ctx->fail(TG_ERR_ARG, "too many samples in one job");
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < n_samples; ++i) total += lens[i];
+    // runs of samples [cut[r], cut[r + 1])
+    std::vector<uint32_t> cut{0};  // tg_count_batch* take at least one sample, the others exactly one
+    uint64_t target = ~0ull;
+    if (n_samples > 1) {
+        CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+        uint64_t budget = 0;
+        const tg_status bs = phase2_budget(ctx, &budget);
+        if (bs != TG_OK) return bs;
+        target = std::max<uint64_t>(1, budget / BATCH_BYTES_PER_BASE);
+    }
+    if (total > target) {
+        uint64_t acc = 0;
+        for (uint32_t i = 0; i < n_samples; ++i) {
+            if (acc && acc + lens[i] > target) {
+                cut.push_back(i);
+                acc = 0;
+            }
+            acc += lens[i];
+        }
+    }
+    cut.push_back(n_samples);
+    const bool pipelined = cut.size() > 2;
+    tg_stats all{};
+    uint64_t done = 0;
+    tg_status s = TG_OK;
+    for (size_t r = 0; r + 1 < cut.size() && s == TG_OK; ++r) {
+        uint64_t nr = 0;
+        tg_stats sr{};
+        s = count_run(ctx, opts, cut[r], cut[r + 1], seqs, lens, keys, counts, sample_off, done, cap, fastx,
+                      pipelined, nr, sr);
+        if (r == 0) all = sr;
+        else add_run_stats(all, sr);
+        done += nr;
+    }
+    if (ctx->copy_pending) {
+        const double t_wait = now_ms();
+        const cudaError_t ce = cudaStreamSynchronize(ctx->st_copy);
+        all.d2h_ms += now_ms() - t_wait;
+        ctx->copy_pending = false;
+        if (s == TG_OK && ce != cudaSuccess) s = ctx->cuda_fail(ce, "d2h");
+    }
+    if (s == TG_OK) {
+        *n_out = done;
+        if (done > cap) s = ctx->fail(TG_ERR_ARG, "result buffer too small");
+    }
+    if (stats) *stats = all;
     return s;
 }
 

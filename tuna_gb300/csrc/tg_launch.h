@@ -119,6 +119,9 @@ struct P2Output {
     unsigned long long* sample_off = nullptr;
     uint64_t cap;
     uint64_t n_out, distinct, groups, heavy_groups, fallback_groups;
+    // the sample-major scatter waits for this event first (an earlier job's
+    // copy of keys2/counts2 to the host may still be running), or null
+    cudaEvent_t reorder_after = nullptr;
 };
 // Results handed out while phase 2 still runs: the first counting pass runs in
 // `waves` launches, and after each one on_range(lo, hi) is called (on the host,

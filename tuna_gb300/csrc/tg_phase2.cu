@@ -225,7 +225,8 @@ __global__ void __launch_bounds__(PLAN_THREADS) k_plan(KeysParams P) {
 // inside it, with about a third as many places being written at once (groups
 // of ~3 bins), so more of the partly written sectors are completed in L2.
 // The descriptors are loaded two batches ahead and the next batch's gfirst
-// entries one batch ahead, so neither load delays the atomic.
+// entries one batch ahead, and each batch's atomic is issued before the
+// previous batch's keys are made (k_keys 19.8 -> 19.1 ms at 3.1 G keys).
 //
 // A run restricted to a range of bins (the passes of a job larger than the
 // memory budget) keeps only the records of those bins, moved to the front of
@@ -249,12 +250,11 @@ __global__ void __launch_bounds__(P2_THREADS) k_keys(KeysParams P) {
     uint64_t dnext = load_desc(b0);                 // batch i + 1 (loaded)
     uint32_t gnext = group_of(dnext);
     uint64_t dnext2 = load_desc(b0 + P2_THREADS);   // batch i + 2 (in flight)
-    for (uint32_t base = (uint32_t)wid * 32; base < n; base += P2_THREADS) {
-        uint64_t dv = dnext;
-        uint32_t gv = gnext;
-        dnext = dnext2;
-        gnext = group_of(dnext);
-        dnext2 = load_desc(base + 2 * P2_THREADS + lane);
+    // A batch is prepared (restricted to this run's bins, moved to the front of
+    // the warp; its places reserved by the atomic) one batch ahead: the atomic's
+    // round trip overlaps the previous batch's keys.
+    auto prepare = [&](uint64_t& dv, uint32_t gv, unsigned long long& koff) {
+        koff = 0;
         if (filt) {
             const uint32_t b = desc_bin(dv);
             const bool keep = desc_nk(dv) && b >= P.bin_lo && b < P.bin_hi;
@@ -268,11 +268,34 @@ __global__ void __launch_bounds__(P2_THREADS) k_keys(KeysParams P) {
             dv = lane < __popc(m) ? s_keep[wid * 32 + lane] : 0;
             gv = lane < __popc(m) ? s_keepg[wid * 32 + lane] : 0;
             __syncwarp();
-            if (m == 0) continue;
         }
         const uint32_t nk = desc_nk(dv);  // 0 past the slice; at least 1 otherwise
-        unsigned long long koff = 0;
         if (nk) koff = atomicAdd(&P.kofs[gv], (unsigned long long)nk);
+    };
+    uint64_t cdv = dnext;
+    unsigned long long ckoff;
+    {
+        const uint32_t cg = gnext;
+        dnext = dnext2;
+        gnext = group_of(dnext);
+        dnext2 = load_desc(b0 + 2 * P2_THREADS);
+        prepare(cdv, cg, ckoff);
+    }
+    for (uint32_t base = (uint32_t)wid * 32; base < n; base += P2_THREADS) {
+        uint64_t ndv = dnext;
+        unsigned long long nkoff;
+        {
+            const uint32_t ng = gnext;
+            dnext = dnext2;
+            gnext = group_of(dnext);
+            dnext2 = load_desc(base + 3 * P2_THREADS + lane);
+            prepare(ndv, ng, nkoff);
+        }
+        const uint64_t dv = cdv;
+        const unsigned long long koff = ckoff;
+        cdv = ndv;
+        ckoff = nkoff;
+        const uint32_t nk = desc_nk(dv);
         uint32_t incl = nk;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -1179,6 +1202,7 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
               "scan");
         unsigned long long* cur = R.scur;  // the offsets, copied, as cursors
         P2_CK(cudaMemcpyAsync(cur, out.sample_off, 8 * (size_t)out.n_samples, cudaMemcpyDeviceToDevice, st), "copy");
+        if (out.reorder_after) P2_CK(cudaStreamWaitEvent(st, out.reorder_after, 0), "wait");
         if (W == 1) k_samp_scatter<1><<<grid, 256, 0, st>>>(out.keys, out.counts, out.samples, n, cur, out.keys2, out.counts2);
         else k_samp_scatter<2><<<grid, 256, 0, st>>>(out.keys, out.counts, out.samples, n, cur, out.keys2, out.counts2);
         P2_CK(cudaGetLastError(), "k_samp_scatter");
