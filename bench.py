@@ -849,6 +849,10 @@ def main():
     ref_record_bytes = 2 * recs + (st["kmers"] + recs * (K - 1)) / 4
     b1 = bases / 4 + ref_record_bytes
     p1_gbs = b1 / (avg["phase1"] / 1e3) / 1e9
+    # phase 2 against the reference's algorithmic bytes B2 = record bytes read once +
+    # one (key, u32 count) pair written per distinct k-mer (no key array round trip)
+    b2 = ref_record_bytes + int(st["distinct"]) * (8 * ((K + 32) // 32) + 4)
+    p2_gbs = b2 / (avg["phase2"] / 1e3) / 1e9
     traffic, traffic_source = None, None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
@@ -994,7 +998,8 @@ def main():
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                          else "fallback 6.8 TB/s",
                          "algorithmic_bytes": alg[dom], "traffic": traffic, "traffic_source": traffic_source,
-                         "phase1_b1_gbs": p1_gbs, "phase1_b1_frac": p1_gbs / peak},
+                         "phase1_b1_gbs": p1_gbs, "phase1_b1_frac": p1_gbs / peak,
+                         "phase2_b2_gbs": p2_gbs, "phase2_b2_frac": p2_gbs / peak},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "parity": parity_full,
