@@ -300,7 +300,13 @@ tg_status tg_fastx_to_stream(tg_ctx* ctx, const uint8_t* data, size_t len, uint8
                              size_t* out_len);
 /* The same for n_samples host sequence streams counted as separate samples in
  * one job: the pairs come back sample-major, sample i's being
- * [sample_offsets[i], sample_offsets[i+1]) (n_samples + 1 entries, may be NULL). */
+ * [sample_offsets[i], sample_offsets[i+1]) (n_samples + 1 entries, may be NULL).
+ * A batch larger than the device budget (hbm_budget_bytes, else free memory)
+ * is counted as consecutive runs of whole samples, each run a job whose result
+ * copy overlaps the next run; the call returns as one: the same offsets and
+ * pairs, stats summed over the runs. With too small a cap, *n_out still
+ * receives the total, TG_ERR_ARG is returned, and the samples that end within
+ * cap are complete in keys/counts. */
 tg_status tg_count_batch(tg_ctx* ctx, const tg_job_opts* opts, uint32_t n_samples,
                          const uint8_t* const* seqs, const size_t* lens, uint64_t* keys,
                          uint32_t* counts, uint64_t* sample_offsets, uint64_t cap, uint64_t* n_out,
