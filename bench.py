@@ -569,10 +569,14 @@ def small_reads(ctx, steps: int):
             "api": "tg_count_fastx from pinned FASTQ bytes; CPU: the oracle port (tor_count_fastx)"}
 
 
-def gz_input(fasta: np.ndarray, mbytes: float = 300.0):
+def gz_input(ctx, fasta: np.ndarray, mbytes: float = 300.0):
     """Reading gzip input on the host (tg_read_input): a BGZF file inflated on
     1 and on all host threads, and the same bytes as one gzip member (one
-    stream, as the reference's GzInput reads every .gz file)."""
+    stream, as the reference's GzInput reads every .gz file). Then the whole
+    path from a file (tg_job_feed_file: reading and inflating on host threads,
+    H2D, lexing on the device, both phases; the pairs' digest on the device,
+    which must equal the plain file's), from the BGZF file and from the same
+    FASTA uncompressed."""
     import gzip
     import zlib
     from concurrent.futures import ThreadPoolExecutor
@@ -606,10 +610,24 @@ def gz_input(fasta: np.ndarray, mbytes: float = 300.0):
         t = time.perf_counter() - t0
         assert got == raw
         res[name] = {"seconds": t, "gbytes_s": len(raw) / t / 1e9, "threads": th}
-    for p in (p_bg, p_one):
+    p_plain = os.path.join(d, "c.fa")
+    with open(p_plain, "wb") as f:
+        f.write(raw)
+    dg = {}
+    for name, path in (("count_from_plain_file", p_plain), ("count_from_bgzf_file", p_bg)):
+        ctx.run(K, M, files=[path], n_parts=NPARTS, want_results=False)  # page cache, buffers
+        t0 = time.perf_counter()
+        r, _ = ctx.run(K, M, files=[path], n_parts=NPARTS, want_results=False, digest=True)
+        t = time.perf_counter() - t0
+        dg[name] = r.digest
+        res[name] = {"seconds": t, "gbases_s": int(r.stats["bases"]) / t / 1e9, "bases": int(r.stats["bases"]),
+                     "pairs": len(r) if r.keys is not None else int(r.stats["out"])}
+    res["count_from_file_digests_same"] = dg["count_from_plain_file"] == dg["count_from_bgzf_file"]
+    for p in (p_bg, p_one, p_plain):
         os.remove(p)
     os.rmdir(d)
-    res["api"] = "tg_read_input (include/tuna_gpu.h), the reading step of tg_job_feed_file"
+    res["api"] = ("tg_read_input (include/tuna_gpu.h), the reading step of tg_job_feed_file; "
+                  "count_from_*: tg_job_feed_file + tg_job_run, pairs left on the device (digest)")
     return res
 
 
@@ -951,7 +969,7 @@ def main():
         small = section("small_reads", small_reads, ctx, args.steps)
     gz = None
     if rank == 0 and not args.no_gz and fasta_h is not None:
-        gz = section("gz", gz_input, fasta_h)
+        gz = section("gz", gz_input, ctx, fasta_h)
     output = None
     if rank == 0 and not args.no_output:
         output = section("output", output_drain, ctx, dev, n_stream)
