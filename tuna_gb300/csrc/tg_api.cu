@@ -1857,7 +1857,9 @@ static tg_status count_run(tg_ctx* ctx, const tg_job_opts* opts, uint32_t a, uin
         const double t0 = now_ms();
         if (h && (kdst || cdst)) {
             if (pipelined && !j->spilled) {
-                // the run left the sample-major pairs in okeys2/ocnt2 and its stream idle
+                // the run left the sample-major pairs in okeys2/ocnt2 and its stream idle;
+                // pending from the first copy on, so that any return waits for it
+                ctx->copy_pending = true;
                 if (kdst)
                     CK(link_copy(kdst, ctx->okeys2.as<uint8_t>(), h * key_bytes(W), cudaMemcpyDeviceToHost,
                                  ctx->st_copy, ctx->n_sm), "d2h keys");
@@ -1865,7 +1867,6 @@ static tg_status count_run(tg_ctx* ctx, const tg_job_opts* opts, uint32_t a, uin
                     CK(link_copy(cdst, ctx->ocnt2.as<uint32_t>(), h * 4, cudaMemcpyDeviceToHost, ctx->st_copy,
                                  ctx->n_sm), "d2h counts");
                 CK(cudaEventRecord(ctx->ev_copied, ctx->st_copy), "event");
-                ctx->copy_pending = true;
             } else {
                 s = tg_job_result_copy(j, kdst, cdst, 0, h);
             }
