@@ -1042,11 +1042,12 @@ tg_status phase2_run(const P2Input& in, void* scratch, size_t scratch_cap, P2Out
     ++*launches;
     if (L.n_slices) {
         // Large jobs: two launches, each writing the keys of half of the bins.
-        // A record's keys land at its bin's cursor; with all 2^20 bins open the
-        // partly written sectors do not stay in L2 until their neighbours fill
-        // them (DRAM traffic about twice the key bytes); with half of them open
-        // more do (3.1 G keys: 28.0 -> 23.4 ms, though every launch reads all
-        // descriptors; four launches: 25.1, eight: 39.4).
+        // A record's keys land at its group's cursor; with every group open at
+        // once fewer of the partly written sectors stay in L2 until their
+        // neighbours fill them; with half of them open more do (3.1 G keys, bin
+        // cursors: 28.0 -> 23.4 ms, four launches 25.1, eight 39.4; group
+        // cursors: one launch 22.9, two 19.8), though every launch reads all
+        // descriptors.
         const uint32_t KP = in.n_kmers > (1ull << 28) ? 2 : 1;
         const uint32_t span = in.bin_hi - in.bin_lo;
         for (uint32_t kp = 0; kp < KP; ++kp) {
