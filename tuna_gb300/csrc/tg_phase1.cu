@@ -503,7 +503,7 @@ constexpr int SEG = 128;
 static_assert(SEG * 256 <= CUT_SPAN, "a cut tile must fit the packed arrays' slack");
 
 struct SeqSmem {
-    size_t tables, pk, vb, vh, vs, sum, total;
+    size_t tables, pk, vb, vh, sum, total;
     uint32_t npk, nvb;
     __host__ __device__ static size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
     __host__ __device__ void layout(int w, int nt, int k) {
@@ -515,14 +515,15 @@ struct SeqSmem {
         tables = o; o = align16(o + sizeof(HashTables));
         pk = o; o = align16(o + 4 * (size_t)npk);
         vb = o; o = align16(o + 4 * (size_t)nvb);
+        // one block of w + 1 hashes per thread: the block being filled, and from
+        // its end back to the current offset the previous block's suffix minima
         vh = o; o = align16(o + 8 * (size_t)(w + 1) * nt);
-        vs = o; o = align16(o + 8 * (size_t)(w + 1) * nt);
         sum = o; o = align16(o + 20 * (size_t)nt);  // i64 chain, i64 first cut, u32 chain mlo
         total = o;
     }
 };
 
-// Threads of the sequential cut for window w (the block buffers hold 2(w+1)
+// Threads of the sequential cut for window w (the block buffer holds w + 1
 // hashes per thread).
 __host__ __device__ inline int seq_threads(int w) { return w <= 15 ? 256 : (w <= 31 ? 128 : 64); }
 
@@ -597,7 +598,10 @@ k_cut_seq(CutParams P, const HashTables* __restrict__ gT) {
     uint32_t* s_pk = reinterpret_cast<uint32_t*>(smem + L.pk);
     uint32_t* s_vb = reinterpret_cast<uint32_t*>(smem + L.vb);
     uint64_t* vH = reinterpret_cast<uint64_t*>(smem + L.vh);
-    uint64_t* vS = reinterpret_cast<uint64_t*>(smem + L.vs);
+    // the previous block's suffix minima share the buffer: at offset o a step
+    // writes hash o and reads suffix minimum o + 1, which is overwritten only at
+    // the next step (k=63 m=21: half the shared memory, more CTAs per SM)
+    uint64_t* vS = vH;
     int64_t* s_cs = reinterpret_cast<int64_t*>(smem + L.sum);  // chain in force after the segment's last cut
     int64_t* s_fe = s_cs + NT;                                  // the segment's first cut (-1: none)
     uint32_t* s_cm = reinterpret_cast<uint32_t*>(s_fe + NT);    // mlo of s_cs
@@ -1263,7 +1267,8 @@ uint32_t cut_ctas_per_sm(int w, int k, uint32_t p1, bool exp) {
     if (!exp && fixed_cut(k, w)) return std::max<uint32_t>(1, std::min<uint32_t>(FIXED_CUT_CTAS, by_smem));
     // the sequential cut: up to 768 threads per SM (three CTAs of 256; for wide
     // windows, 64-thread CTAs as many as shared memory allows: k=63 m=21 reads,
-    // 3 -> 4 CTAs, 11.9 -> 9.0 ms for 0.9 Gbp)
+    // 3 -> 4 CTAs, 11.9 -> 9.0 ms for 0.9 Gbp; one block buffer instead of two,
+    // 4 -> 7 CTAs)
     return std::max<uint32_t>(1, std::min<uint32_t>(exp ? 2u : 768u / (uint32_t)seq_threads(w), by_smem));
 }
 
