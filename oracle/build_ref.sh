@@ -8,13 +8,13 @@
 # and the KFF stand-in in oracle/ref_stub/ (TSV output only).
 #
 # Usage: oracle/build_ref.sh [REF_ROOT] [k:m ...]
-# REF_ROOT defaults to $TUNA_REFERENCE, else the benchmark's reference_path.
+# REF_ROOT defaults to $TUNA_REFERENCE, else a "reference" directory beside the
+# repository.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
 REF="${1:-${TUNA_REFERENCE:-}}"
 if [ -z "$REF" ]; then
-  REF="$(python3 -c 'import json,sys; print(json.load(open(sys.argv[1])).get("reference_path", ""))' \
-         "$HERE/../BASELINE.json" 2>/dev/null || true)"
+  REF="$(cd "$HERE/../.." && pwd)/reference"
 fi
 shift || true
 PAIRS=("$@")

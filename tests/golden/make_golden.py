@@ -27,7 +27,7 @@ sum, h1, h2), the line count and the superkmers: value.
 
 Usage: python tests/golden/make_golden.py [--scale [NAME ...]]   (needs
 oracle/_ref/, i.e. the reference sources: TUNA_REFERENCE names their root,
-else the benchmark's reference_path)
+else a `reference` directory beside the repository)
 """
 from __future__ import annotations
 
@@ -51,13 +51,12 @@ REF = os.path.join(ROOT, "oracle", "_ref")
 
 
 def reference_root() -> str:
-    """Root of the reference sources: $TUNA_REFERENCE, else the benchmark's
-    reference_path."""
+    """Root of the reference sources: $TUNA_REFERENCE, else a `reference`
+    directory beside the repository."""
     env = os.environ.get("TUNA_REFERENCE")
     if env:
         return env
-    with open(os.path.join(ROOT, "BASELINE.json")) as f:
-        return json.load(f)["reference_path"]
+    return os.path.join(os.path.dirname(ROOT), "reference")
 
 
 def ref_bin(k: int, m: int) -> str:
