@@ -502,6 +502,8 @@ k_cut(CutParams P, const HashTables* __restrict__ gT) {
 constexpr int SEG = 128;
 static_assert(SEG * 256 <= CUT_SPAN, "a cut tile must fit the packed arrays' slack");
 
+constexpr size_t SEQ_TABLE_BYTES = offsetof(HashTables, GF);
+
 struct SeqSmem {
     size_t tables, pk, vb, vh, sum, total;
     uint32_t npk, nvb;
@@ -512,7 +514,9 @@ struct SeqSmem {
         npk = span / 16 + 2;
         nvb = span / 32 + 2;
         size_t o = 0;
-        tables = o; o = align16(o + sizeof(HashTables));
+        // the roll terms only (FW, RV, CTF, CTR): each thread's one initial hash
+        // reads the 4-base group terms from global memory
+        tables = o; o = align16(o + SEQ_TABLE_BYTES);
         pk = o; o = align16(o + 4 * (size_t)npk);
         vb = o; o = align16(o + 4 * (size_t)nvb);
         // one block of w + 1 hashes per thread: the block being filled, and from
@@ -618,8 +622,8 @@ k_cut_seq(CutParams P, const HashTables* __restrict__ gT) {
     const uint32_t c = blockIdx.x;
     {
         const uint64_t* src = reinterpret_cast<const uint64_t*>(gT);
-        uint64_t* dst = reinterpret_cast<uint64_t*>(&T);
-        for (int i = tid; i < (int)(sizeof(HashTables) / 8); i += NT) dst[i] = src[i];
+        uint64_t* dst = reinterpret_cast<uint64_t*>(&T);  // T.GF and T.GR are not staged
+        for (int i = tid; i < (int)(SEQ_TABLE_BYTES / 8); i += NT) dst[i] = src[i];
         if (tid == 0) { s_carry_cs = -1; s_carry_m = 0; s_open = -1; s_open_m = 0; s_open_own = 0; s_ndesc = 0; }
     }
     __syncthreads();
@@ -686,7 +690,7 @@ k_cut_seq(CutParams P, const HashTables* __restrict__ gT) {
         }
         const uint32_t ra = (uint32_t)((uint64_t)(pb + TG_PAD) - A0);  // staged index of base pb
         uint64_t f, r;
-        nt_init(T, s_pk, ra, m, f, r);
+        nt_init(*gT, s_pk, ra, m, f, r);
         int il;  // last invalid base entered so far, relative to pb (-1: none)
         {
             const uint64_t inval = ~valid64(s_vb, ra) & kmask;  // bases pb .. pb + k - 1
