@@ -185,6 +185,12 @@ def test_count_batch_in_runs_of_samples(k, m):
             a, b = int(off[i]), int(off[i + 1])
             got = T.Result(keys[a:b].copy(), cnt[a:b].copy(), {}, k)
             assert _same(got, w), f"sample {i}"
+        # and against the oracle, sample by sample (its digest of the sample
+        # counted alone on the CPU)
+        from oracle import oracle as O
+        for i in (0, 1, 11, 23):
+            a, b = int(off[i]), int(off[i + 1])
+            assert O.digest_pairs(keys[a:b], cnt[a:b], k) == O.digest_stream(smp[i], k, m, 16)[0], f"sample {i}"
         # a buffer for half the pairs: the samples that end within it are complete
         # (the order of a sample's pairs is not fixed from one call to the next)
         half = n_all // 2
